@@ -1,0 +1,627 @@
+// api.cpp -- the C ABI of include/axx.h over the walk kernels.
+//
+// A context owns one CUDA stream on one device, eight timing events and a
+// host-mapped abort word.  A plan owns one device arena holding every table
+// of one walk (geometry, slots, waveforms, coefficients), the per-block FP64
+// partials, the reduced sums and the counters; it is built once and launched
+// any number of times.  The one-shot calls (axx_run_lattice, axx_run_single)
+// build a plan, launch it, read it back and free it, mirroring the
+// allocate-copy-run-copy-free sequence of runAcquisitionLattice
+// (src/acquisition/phaseAcquisitionStream.cuh:126-190).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/axx.h"
+#include "host_plan.h"
+#include "walk_launch.h"
+
+using namespace axx;
+
+struct axx_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[8] = {};
+  std::string err;
+  int nsm = 0, ccmaj = 0, ccmin = 0;
+  size_t gmem = 0;
+  volatile int *abort_host = nullptr;
+  int *abort_dev = nullptr;
+};
+
+struct axx_plan {
+  axx_ctx *ctx = nullptr;
+  WalkParams P{};
+  int geom = 0, kmax = 1, grid = 0, M = 0, K = 0, n_inst = 0;
+  size_t smem = 0;
+  void *arena = nullptr;
+  double *out = nullptr;  // [M*5]
+  unsigned long long *counters = nullptr;
+  long long walker_steps = 0;
+  bool launched = false;
+};
+
+namespace {
+
+axx_status fail(axx_ctx *ctx, axx_status s, const std::string &msg) {
+  if (ctx) ctx->err = msg;
+  return s;
+}
+
+axx_status cuda_fail(axx_ctx *ctx, cudaError_t e, const char *where) {
+  if (ctx) ctx->err = std::string(where) + ": " + cudaGetErrorString(e);
+  if (e == cudaErrorMemoryAllocation) return AXX_ERR_OUT_OF_MEMORY;
+  return AXX_ERR_CUDA;
+}
+
+#define AXX_CUDA(ctx, call)                                  \
+  do {                                                       \
+    cudaError_t e_ = (call);                                 \
+    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
+  } while (0)
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+cudaError_t launch_geom(int geom, int kmax, bool trace, const WalkParams &P, const TraceParams &T,
+                        int grid, size_t smem, cudaStream_t s) {
+  switch (geom) {
+    case AXX_GEOM_FREE: return launch_walk_free(kmax, trace, P, T, grid, smem, s);
+    case AXX_GEOM_CYL: return launch_walk_cyl(kmax, trace, P, T, grid, smem, s);
+    case AXX_GEOM_SPH: return launch_walk_sph(kmax, trace, P, T, grid, smem, s);
+    default: return launch_walk_mix(kmax, trace, P, T, grid, smem, s);
+  }
+}
+
+int kmax_for(int K) {
+  int k = 1;
+  while (k < K) k <<= 1;
+  return k;
+}
+
+axx_status check_params(axx_ctx *ctx, const axx_run_params *p) {
+  if (!p) return fail(ctx, AXX_ERR_INVALID_ARG, "params is NULL");
+  if (p->num_walkers < 1) return fail(ctx, AXX_ERR_INVALID_ARG, "num_walkers must be >= 1");
+  if (p->steps < 1) return fail(ctx, AXX_ERR_INVALID_ARG, "steps must be >= 1");
+  if (!(p->timestep > 0.0) || !std::isfinite(p->timestep))
+    return fail(ctx, AXX_ERR_INVALID_ARG, "timestep must be > 0");
+  if (!std::isfinite(p->gamma) || p->gamma < 0.0)
+    return fail(ctx, AXX_ERR_INVALID_ARG, "gamma must be finite and >= 0");
+  if (p->walker_offset < 0) return fail(ctx, AXX_ERR_INVALID_ARG, "walker_offset must be >= 0");
+  if (p->init_mode < 0 || p->init_mode > 2)
+    return fail(ctx, AXX_ERR_INVALID_ARG, "unknown init_mode");
+  return AXX_OK;
+}
+
+// Builds the plan's device arena and kernel parameters.
+axx_status build_plan(axx_ctx *ctx, const GeomPlan &g, const SeqPlan &sq, int M,
+                      const axx_run_params *p, int mode, float sspeed, float sstep,
+                      int init_inst, int init_sph, double init_R, double init_cx,
+                      double init_cy, double init_cz, axx_plan **out) {
+  const int K = (int)sq.channels.size();
+  if (K > AXX_KMAX)
+    return fail(ctx, AXX_ERR_UNSUPPORTED,
+                "more than 16 phase channels (distinct waveform x direction) in one plan");
+  auto *pl = new axx_plan();
+  pl->ctx = ctx;
+  pl->geom = g.geom;
+  pl->K = K;
+  pl->M = M;
+  pl->kmax = kmax_for(std::max(K, 1));
+  pl->n_inst = (int)g.geo.size();
+  const int steps = p->steps;
+  const int ncell = (int)g.cstart.size() - 1;
+  // grid: resident capacity of the device, at most one warp per 32 walkers
+  const size_t wsum_bytes = (size_t)(AXX_BLOCK / 32) * M * 5 * sizeof(double);
+  const size_t geo_bytes = (size_t)pl->n_inst * 32 + (size_t)(ncell + 1) * 4 +
+                           ((g.clist.size() * 2 + 15) & ~(size_t)15);
+  const bool smem_geom = g.geom != AXX_GEOM_FREE && geo_bytes <= 96 * 1024;
+  // the geometry staging area starts right after the per-warp sums (160*M
+  // bytes, a multiple of 16)
+  pl->smem = wsum_bytes + (smem_geom ? geo_bytes : 0);
+  const int occ = occupancy_walk(g.geom, pl->kmax, false, pl->smem);
+  if (occ <= 0) {
+    delete pl;
+    return fail(ctx, AXX_ERR_CUDA, "walk kernel cannot be resident (occupancy 0)");
+  }
+  const long long ntask = (p->num_walkers + 31) / 32;
+  const long long want = (ntask + AXX_BLOCK / 32 - 1) / (AXX_BLOCK / 32);
+  pl->grid = (int)std::min<long long>(want, (long long)occ * ctx->nsm);
+  // arena
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    size_t o = off;
+    off = align256(off + std::max<size_t>(bytes, 1));
+    return o;
+  };
+  const size_t o_geo = take(g.geo.size() * sizeof(float4));
+  const size_t o_aux = take(g.aux.size() * sizeof(float4));
+  const size_t o_cs = take(g.cstart.size() * 4);
+  const size_t o_cl = take(g.clist.size() * 2);
+  const size_t o_slot = take(g.slot_tab.size() * sizeof(float4));
+  const size_t o_reg = take(g.slot_region.size() * 4);
+  const size_t o_wave = take(sq.wave.size() * 4);
+  const size_t o_coef = take(sq.coef.size() * 8);
+  const size_t o_part = take((size_t)pl->grid * M * 5 * 8);
+  const size_t o_out = take((size_t)M * 5 * 8);
+  const size_t o_cnt = take(AXX_CNT_N * 8);
+  cudaError_t e = cudaMalloc(&pl->arena, off);
+  if (e != cudaSuccess) {
+    delete pl;
+    return cuda_fail(ctx, e, "cudaMalloc(plan arena)");
+  }
+  char *base = (char *)pl->arena;
+  auto up = [&](size_t o, const void *src, size_t bytes) {
+    if (bytes == 0) return cudaSuccess;
+    return cudaMemcpyAsync(base + o, src, bytes, cudaMemcpyHostToDevice, ctx->stream);
+  };
+  cudaError_t es[8] = {
+      up(o_geo, g.geo.data(), g.geo.size() * sizeof(float4)),
+      up(o_aux, g.aux.data(), g.aux.size() * sizeof(float4)),
+      up(o_cs, g.cstart.data(), g.cstart.size() * 4),
+      up(o_cl, g.clist.data(), g.clist.size() * 2),
+      up(o_slot, g.slot_tab.data(), g.slot_tab.size() * sizeof(float4)),
+      up(o_reg, g.slot_region.data(), g.slot_region.size() * 4),
+      up(o_wave, sq.wave.data(), sq.wave.size() * 4),
+      up(o_coef, sq.coef.data(), sq.coef.size() * 8)};
+  for (cudaError_t x : es)
+    if (x != cudaSuccess) {
+      cudaFree(pl->arena);
+      delete pl;
+      return cuda_fail(ctx, x, "cudaMemcpyAsync(plan tables)");
+    }
+  e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) {
+    cudaFree(pl->arena);
+    delete pl;
+    return cuda_fail(ctx, e, "cudaStreamSynchronize(plan upload)");
+  }
+  WalkParams &P = pl->P;
+  std::memset(&P, 0, sizeof(P));
+  P.mode = mode;
+  P.n_inst = pl->n_inst;
+  P.n_list = (int)g.clist.size();
+  P.ncell = ncell;
+  P.smem_geom = smem_geom ? 1 : 0;
+  P.inst_geo = (const float4 *)(base + o_geo);
+  P.inst_aux = (const float4 *)(base + o_aux);
+  P.cell_start = (const uint32_t *)(base + o_cs);
+  P.cell_list = (const uint16_t *)(base + o_cl);
+  P.gx = g.gx;
+  P.gy = g.gy;
+  P.gz = g.gz;
+  P.inv_hx = g.inv_hx;
+  P.inv_hy = g.inv_hy;
+  P.inv_hz = g.inv_hz;
+  P.slot_tab = (const float4 *)(base + o_slot);
+  P.slot_region = (const int *)(base + o_reg);
+  P.ecs_slot = g.ecs_slot;
+  P.steps = steps;
+  P.n_walkers = p->num_walkers;
+  P.walker_offset = p->walker_offset;
+  P.seed_lo = (uint32_t)p->seed;
+  P.seed_hi = (uint32_t)(p->seed >> 32);
+  P.flags = p->flags;
+  P.init_mode = p->init_mode;
+  P.init_arg = p->init_arg;
+  P.init_quirk = (mode == AXX_MODE_SINGLE) && !(p->flags & AXX_FLAG_FIX_INIT_QUIRK);
+  P.init_inst = init_inst;
+  P.init_sph = init_sph;
+  P.init_R = (float)init_R;
+  P.init_cx = (float)init_cx;
+  P.init_cy = (float)init_cy;
+  P.init_cz = (float)init_cz;
+  P.single_speed = sspeed;
+  P.single_step = sstep;
+  P.K = K;
+  P.wave = (const float *)(base + o_wave);
+  for (int c = 0; c < K; ++c) {
+    P.ch_wave[c] = sq.channels[c].wave;
+    for (int k = 0; k < 3; ++k) P.ch_p[c][k] = sq.channels[c].p[k];
+  }
+  P.M = M;
+  P.coef = (const double *)(base + o_coef);
+  P.partials = (double *)(base + o_part);
+  P.counters = (unsigned long long *)(base + o_cnt);
+  P.abort_flag = ctx->abort_dev;
+  pl->out = (double *)(base + o_out);
+  pl->counters = P.counters;
+  pl->walker_steps = p->num_walkers * (long long)(steps - 1);
+  if (mode == AXX_MODE_LATTICE) {
+    P.a = 0.f;  // set by the caller
+  }
+  *out = pl;
+  return AXX_OK;
+}
+
+axx_status make_lattice_plan(axx_ctx *ctx, const axx_lattice *lat, const axx_basis *basis,
+                             int nbasis, const axx_sequence *seqs, int nseq,
+                             const axx_run_params *params, axx_plan **out) {
+  axx_status s = check_params(ctx, params);
+  if (s != AXX_OK) return s;
+  const double gamma = params->gamma > 0.0 ? params->gamma : kGammaDefault;
+  GeomPlan g;
+  std::string e = plan_lattice(lat, basis, nbasis, params->timestep, params->flags, g);
+  if (!e.empty()) return fail(ctx, AXX_ERR_INVALID_ARG, e);
+  SeqPlan sq;
+  e = plan_sequences(seqs, nseq, params->steps, params->timestep, gamma, sq);
+  if (!e.empty()) return fail(ctx, AXX_ERR_INVALID_ARG, e);
+  int init_inst = 0, init_sph = 0;
+  double R = 0, cx = 0, cy = 0, cz = 0;
+  if (params->init_mode == AXX_INIT_IN_BASIS) {
+    if (params->init_arg < 0 || params->init_arg >= nbasis)
+      return fail(ctx, AXX_ERR_INVALID_ARG, "init_arg must name a basis for AXX_INIT_IN_BASIS");
+    for (int n = 0; n < (int)g.aux.size(); ++n) {
+      int slot;
+      std::memcpy(&slot, &g.aux[n].z, 4);
+      if (slot == params->init_arg) {
+        init_inst = n;
+        break;
+      }
+    }
+    const axx_basis &b = basis[params->init_arg];
+    init_sph = b.type == AXX_PRIM_SPHERE;
+    R = b.radius;
+    cx = b.cx;
+    cy = b.cy;
+    cz = b.cz;
+  }
+  s = build_plan(ctx, g, sq, nseq, params, AXX_MODE_LATTICE, 0.f, 0.f, init_inst, init_sph, R,
+                 cx, cy, cz, out);
+  if (s != AXX_OK) return s;
+  (*out)->P.a = (float)lat->a;
+  (*out)->P.b = (float)lat->b;
+  (*out)->P.c = (float)lat->c;
+  return AXX_OK;
+}
+
+axx_status make_single_plan(axx_ctx *ctx, const axx_basis *basis, const axx_sequence *seqs,
+                            int nseq, const axx_run_params *params, axx_plan **out) {
+  axx_status s = check_params(ctx, params);
+  if (s != AXX_OK) return s;
+  if (params->flags & (AXX_FLAG_PERMEABLE | AXX_FLAG_RELAXATION))
+    return fail(ctx, AXX_ERR_INVALID_ARG,
+                "the single-pore walk has no permeability or relaxation (kernelPhase.cuh:4-66)");
+  const double gamma = params->gamma > 0.0 ? params->gamma : kGammaDefault;
+  GeomPlan g;
+  float sp = 0.f, st = 0.f;
+  std::string e = plan_single(basis, params->timestep, g, sp, st);
+  if (!e.empty()) return fail(ctx, AXX_ERR_INVALID_ARG, e);
+  SeqPlan sq;
+  e = plan_sequences(seqs, nseq, params->steps, params->timestep, gamma, sq);
+  if (!e.empty()) return fail(ctx, AXX_ERR_INVALID_ARG, e);
+  s = build_plan(ctx, g, sq, nseq, params, AXX_MODE_SINGLE, sp, st, 0,
+                 basis->type == AXX_PRIM_SPHERE, basis->radius, basis->cx, basis->cy, basis->cz,
+                 out);
+  if (s != AXX_OK) return s;
+  (*out)->P.a = (*out)->P.b = (*out)->P.c = 1.0f;
+  return AXX_OK;
+}
+
+axx_status read_results(axx_plan *pl, double *mx, double *my, axx_stats *stats) {
+  axx_ctx *ctx = pl->ctx;
+  AXX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  std::vector<double> h((size_t)pl->M * 5);
+  unsigned long long cnt[AXX_CNT_N] = {0};
+  if (pl->M > 0)
+    AXX_CUDA(ctx, cudaMemcpy(h.data(), pl->out, h.size() * 8, cudaMemcpyDeviceToHost));
+  AXX_CUDA(ctx, cudaMemcpy(cnt, pl->counters, sizeof(cnt), cudaMemcpyDeviceToHost));
+  for (int m = 0; m < pl->M; ++m) {
+    if (mx) mx[m] = h[m * 5 + 0];
+    if (my) my[m] = h[m * 5 + 1];
+    if (stats) {
+      if (stats->sxx) stats->sxx[m] = h[m * 5 + 2];
+      if (stats->syy) stats->syy[m] = h[m * 5 + 3];
+      if (stats->sxy) stats->sxy[m] = h[m * 5 + 4];
+    }
+  }
+  if (stats) {
+    stats->reflection_cap_hits = (int64_t)cnt[AXX_CNT_CAP];
+    stats->walker_steps = pl->walker_steps;
+    stats->boundary_hits = (int64_t)cnt[AXX_CNT_HITS];
+  }
+  if (cnt[AXX_CNT_ABORTED]) return fail(ctx, AXX_ERR_ABORTED, "run aborted by axx_abort");
+  if (cnt[AXX_CNT_INIT_FAIL])
+    return fail(ctx, AXX_ERR_INVALID_ARG,
+                "start-position rejection sampling found no point in the requested region");
+  for (int m = 0; m < pl->M; ++m)
+    if (!std::isfinite(h[m * 5]) || !std::isfinite(h[m * 5 + 1]))
+      return fail(ctx, AXX_ERR_NUMERIC, "non-finite signal");
+  if (cnt[AXX_CNT_CAP])
+    return fail(ctx, AXX_ERR_REFLECTION_CAP, "some moves hit the reflection cap of 16");
+  return AXX_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int axx_abi_version(void) { return AXX_ABI_VERSION; }
+
+const char *axx_status_string(axx_status s) {
+  switch (s) {
+    case AXX_OK: return "ok";
+    case AXX_ERR_INVALID_ARG: return "invalid argument";
+    case AXX_ERR_CUDA: return "CUDA error";
+    case AXX_ERR_REFLECTION_CAP: return "reflection cap hit";
+    case AXX_ERR_TIMEOUT: return "timeout";
+    case AXX_ERR_NO_DEVICE: return "no CUDA device";
+    case AXX_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case AXX_ERR_ABORTED: return "aborted";
+    case AXX_ERR_UNSUPPORTED: return "unsupported";
+    case AXX_ERR_NUMERIC: return "non-finite value";
+  }
+  return "unknown status";
+}
+
+axx_status axx_create(axx_ctx **out, int device) {
+  if (!out) return AXX_ERR_INVALID_ARG;
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return AXX_ERR_NO_DEVICE;
+  if (device < 0 || device >= n) return AXX_ERR_INVALID_ARG;
+  auto *ctx = new axx_ctx();
+  ctx->device = device;
+  cudaError_t e = cudaSetDevice(device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+  for (int i = 0; i < 8 && e == cudaSuccess; ++i) e = cudaEventCreate(&ctx->ev[i]);
+  cudaDeviceProp prop;
+  if (e == cudaSuccess) e = cudaGetDeviceProperties(&prop, device);
+  int *h = nullptr;
+  if (e == cudaSuccess) e = cudaHostAlloc((void **)&h, sizeof(int), cudaHostAllocMapped);
+  if (e == cudaSuccess) {
+    *h = 0;
+    ctx->abort_host = h;
+    e = cudaHostGetDevicePointer((void **)&ctx->abort_dev, h, 0);
+  }
+  if (e != cudaSuccess) {
+    axx_destroy(ctx);
+    return AXX_ERR_CUDA;
+  }
+  ctx->nsm = prop.multiProcessorCount;
+  ctx->ccmaj = prop.major;
+  ctx->ccmin = prop.minor;
+  ctx->gmem = prop.totalGlobalMem;
+  *out = ctx;
+  return AXX_OK;
+}
+
+axx_status axx_destroy(axx_ctx *ctx) {
+  if (!ctx) return AXX_OK;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  for (auto &e : ctx->ev)
+    if (e) cudaEventDestroy(e);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  if (ctx->abort_host) cudaFreeHost((void *)ctx->abort_host);
+  delete ctx;
+  return AXX_OK;
+}
+
+const char *axx_last_error(const axx_ctx *ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+
+axx_status axx_device_info(axx_ctx *ctx, int *num_sms, int *cc_major, int *cc_minor,
+                           size_t *global_mem_bytes) {
+  if (!ctx) return AXX_ERR_INVALID_ARG;
+  if (num_sms) *num_sms = ctx->nsm;
+  if (cc_major) *cc_major = ctx->ccmaj;
+  if (cc_minor) *cc_minor = ctx->ccmin;
+  if (global_mem_bytes) *global_mem_bytes = ctx->gmem;
+  return AXX_OK;
+}
+
+axx_status axx_abort(axx_ctx *ctx) {
+  if (!ctx || !ctx->abort_host) return AXX_ERR_INVALID_ARG;
+  *ctx->abort_host = 1;
+  return AXX_OK;
+}
+
+axx_status axx_plan_lattice(axx_ctx *ctx, const axx_lattice *lat, const axx_basis *basis,
+                            int nbasis, const axx_sequence *seqs, int nseq,
+                            const axx_run_params *params, axx_plan **out) {
+  if (!ctx || !out) return AXX_ERR_INVALID_ARG;
+  *out = nullptr;
+  AXX_CUDA(ctx, cudaSetDevice(ctx->device));
+  return make_lattice_plan(ctx, lat, basis, nbasis, seqs, nseq, params, out);
+}
+
+axx_status axx_plan_single(axx_ctx *ctx, const axx_basis *basis, const axx_sequence *seqs,
+                           int nseq, const axx_run_params *params, axx_plan **out) {
+  if (!ctx || !out) return AXX_ERR_INVALID_ARG;
+  *out = nullptr;
+  AXX_CUDA(ctx, cudaSetDevice(ctx->device));
+  return make_single_plan(ctx, basis, seqs, nseq, params, out);
+}
+
+axx_status axx_plan_launch(axx_plan *pl) {
+  if (!pl) return AXX_ERR_INVALID_ARG;
+  axx_ctx *ctx = pl->ctx;
+  *ctx->abort_host = 0;
+  AXX_CUDA(ctx, cudaMemsetAsync(pl->counters, 0, AXX_CNT_N * 8, ctx->stream));
+  TraceParams T{};
+  AXX_CUDA(ctx, launch_geom(pl->geom, pl->kmax, false, pl->P, T, pl->grid, pl->smem, ctx->stream));
+  AXX_CUDA(ctx, launch_reduce_partials(pl->P.partials, pl->grid, pl->M * 5, pl->out, ctx->stream));
+  pl->launched = true;
+  return AXX_OK;
+}
+
+axx_status axx_plan_read(axx_plan *pl, double *mx, double *my, axx_stats *stats) {
+  if (!pl) return AXX_ERR_INVALID_ARG;
+  if (!pl->launched) return fail(pl->ctx, AXX_ERR_INVALID_ARG, "plan was never launched");
+  return read_results(pl, mx, my, stats);
+}
+
+axx_status axx_plan_info(const axx_plan *pl, int *channels, int *instances, int *kernel_launches,
+                         int64_t *walker_steps) {
+  if (!pl) return AXX_ERR_INVALID_ARG;
+  if (channels) *channels = pl->K;
+  if (instances) *instances = pl->n_inst;
+  if (kernel_launches) *kernel_launches = 2;
+  if (walker_steps) *walker_steps = pl->walker_steps;
+  return AXX_OK;
+}
+
+axx_status axx_plan_destroy(axx_plan *pl) {
+  if (!pl) return AXX_OK;
+  cudaStreamSynchronize(pl->ctx->stream);
+  cudaFree(pl->arena);
+  delete pl;
+  return AXX_OK;
+}
+
+axx_status axx_event_record(axx_ctx *ctx, int slot) {
+  if (!ctx || slot < 0 || slot >= 8) return AXX_ERR_INVALID_ARG;
+  AXX_CUDA(ctx, cudaEventRecord(ctx->ev[slot], ctx->stream));
+  return AXX_OK;
+}
+
+axx_status axx_event_elapsed(axx_ctx *ctx, int a, int b, float *ms) {
+  if (!ctx || a < 0 || a >= 8 || b < 0 || b >= 8 || !ms) return AXX_ERR_INVALID_ARG;
+  AXX_CUDA(ctx, cudaEventSynchronize(ctx->ev[b]));
+  AXX_CUDA(ctx, cudaEventElapsedTime(ms, ctx->ev[a], ctx->ev[b]));
+  return AXX_OK;
+}
+
+axx_status axx_sync(axx_ctx *ctx) {
+  if (!ctx) return AXX_ERR_INVALID_ARG;
+  AXX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return AXX_OK;
+}
+
+axx_status axx_run_lattice(axx_ctx *ctx, const axx_lattice *lat, const axx_basis *basis,
+                           int nbasis, const axx_sequence *seqs, int nseq,
+                           const axx_run_params *params, double *mx, double *my,
+                           axx_stats *stats) {
+  axx_plan *pl = nullptr;
+  axx_status s = axx_plan_lattice(ctx, lat, basis, nbasis, seqs, nseq, params, &pl);
+  if (s != AXX_OK) return s;
+  s = axx_plan_launch(pl);
+  if (s == AXX_OK) s = read_results(pl, mx, my, stats);
+  axx_plan_destroy(pl);
+  return s;
+}
+
+axx_status axx_run_single(axx_ctx *ctx, const axx_basis *basis, const axx_sequence *seqs,
+                          int nseq, const axx_run_params *params, double *mx, double *my,
+                          axx_stats *stats) {
+  axx_plan *pl = nullptr;
+  axx_status s = axx_plan_single(ctx, basis, seqs, nseq, params, &pl);
+  if (s != AXX_OK) return s;
+  s = axx_plan_launch(pl);
+  if (s == AXX_OK) s = read_results(pl, mx, my, stats);
+  axx_plan_destroy(pl);
+  return s;
+}
+
+axx_status axx_fp32_fma_peak(axx_ctx *ctx, double *fma_per_s) {
+  if (!ctx || !fma_per_s) return AXX_ERR_INVALID_ARG;
+  AXX_CUDA(ctx, cudaSetDevice(ctx->device));
+  float *d = nullptr;
+  const int grid = ctx->nsm * 8, block = 256, iters = 4096;
+  AXX_CUDA(ctx, cudaMalloc(&d, (size_t)grid * block * sizeof(float)));
+  cudaError_t e = launch_fma_peak(grid, block, iters, d, ctx->stream);  // warm-up
+  if (e == cudaSuccess) e = cudaEventRecord(ctx->ev[6], ctx->stream);
+  for (int r = 0; r < 5 && e == cudaSuccess; ++r) e = launch_fma_peak(grid, block, iters, d, ctx->stream);
+  if (e == cudaSuccess) e = cudaEventRecord(ctx->ev[7], ctx->stream);
+  float ms = 0.f;
+  if (e == cudaSuccess) e = cudaEventSynchronize(ctx->ev[7]);
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, ctx->ev[6], ctx->ev[7]);
+  cudaFree(d);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "axx_fp32_fma_peak");
+  *fma_per_s = 5.0 * (double)grid * block * iters * kFmaPerIter / (ms * 1e-3);
+  return AXX_OK;
+}
+
+axx_status axx_bvalue(const axx_sequence *seq, double gamma, double *b) {
+  if (!seq || !b) return AXX_ERR_INVALID_ARG;
+  *b = bvalue(*seq, gamma > 0.0 ? gamma : kGammaDefault);
+  return AXX_OK;
+}
+
+axx_status axx_gradient_eval(const axx_sequence *seq, const double *t, int n, double *out) {
+  if (!seq || n < 0 || (n > 0 && (!t || !out))) return AXX_ERR_INVALID_ARG;
+  for (int i = 0; i < n; ++i) gradient(*seq, t[i], out + 3 * i);
+  return AXX_OK;
+}
+
+axx_status axx_philox_words(axx_ctx *ctx, uint64_t seed, uint64_t walker, int n, uint32_t *out) {
+  if (!ctx || n < 0 || (n > 0 && !out)) return AXX_ERR_INVALID_ARG;
+  if (n == 0) return AXX_OK;
+  AXX_CUDA(ctx, cudaSetDevice(ctx->device));
+  uint32_t *d = nullptr;
+  AXX_CUDA(ctx, cudaMalloc(&d, (size_t)n * 4));
+  cudaError_t e = launch_philox_words(seed, walker, n, d, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e == cudaSuccess) e = cudaMemcpy(out, d, (size_t)n * 4, cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "axx_philox_words");
+  return AXX_OK;
+}
+
+static axx_status run_trace(axx_ctx *ctx, axx_plan *pl, int ntrace, float *init_pos, float *pos,
+                            int32_t *region, int32_t *hits, int32_t *words) {
+  const int steps = pl->P.steps;
+  const size_t nrec = (size_t)ntrace * (size_t)std::max(steps - 1, 0);
+  void *buf = nullptr;
+  const size_t bytes = align256(ntrace * 12) + align256(nrec * 12) + 3 * align256(nrec * 4);
+  AXX_CUDA(ctx, cudaMalloc(&buf, bytes));
+  char *b = (char *)buf;
+  TraceParams T;
+  T.ntrace = ntrace;
+  T.init_pos = (float *)b;
+  b += align256(ntrace * 12);
+  T.pos = (float *)b;
+  b += align256(nrec * 12);
+  T.region = (int32_t *)b;
+  b += align256(nrec * 4);
+  T.hits = (int32_t *)b;
+  b += align256(nrec * 4);
+  T.words = (int32_t *)b;
+  cudaError_t e = cudaMemsetAsync(pl->counters, 0, AXX_CNT_N * 8, ctx->stream);
+  const int grid = (ntrace + AXX_BLOCK - 1) / AXX_BLOCK;
+  if (e == cudaSuccess) e = launch_geom(pl->geom, 1, true, pl->P, T, grid, pl->smem, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e == cudaSuccess && init_pos) e = cudaMemcpy(init_pos, T.init_pos, ntrace * 12, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && pos) e = cudaMemcpy(pos, T.pos, nrec * 12, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && region) e = cudaMemcpy(region, T.region, nrec * 4, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && hits) e = cudaMemcpy(hits, T.hits, nrec * 4, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && words) e = cudaMemcpy(words, T.words, nrec * 4, cudaMemcpyDeviceToHost);
+  cudaFree(buf);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "trace");
+  return AXX_OK;
+}
+
+axx_status axx_trace_lattice(axx_ctx *ctx, const axx_lattice *lat, const axx_basis *basis,
+                             int nbasis, const axx_run_params *params, int ntrace,
+                             float *init_pos, float *pos, int32_t *region, int32_t *hits,
+                             int32_t *words) {
+  if (!ctx || !params || ntrace < 1) return AXX_ERR_INVALID_ARG;
+  axx_run_params p = *params;
+  p.num_walkers = ntrace;
+  axx_plan *pl = nullptr;
+  axx_status s = axx_plan_lattice(ctx, lat, basis, nbasis, nullptr, 0, &p, &pl);
+  if (s != AXX_OK) return s;
+  s = run_trace(ctx, pl, ntrace, init_pos, pos, region, hits, words);
+  axx_plan_destroy(pl);
+  return s;
+}
+
+axx_status axx_trace_single(axx_ctx *ctx, const axx_basis *basis, const axx_run_params *params,
+                            int ntrace, float *init_pos, float *pos, int32_t *region,
+                            int32_t *hits, int32_t *words) {
+  if (!ctx || !params || ntrace < 1) return AXX_ERR_INVALID_ARG;
+  axx_run_params p = *params;
+  p.num_walkers = ntrace;
+  axx_plan *pl = nullptr;
+  axx_status s = axx_plan_single(ctx, basis, nullptr, 0, &p, &pl);
+  if (s != AXX_OK) return s;
+  s = run_trace(ctx, pl, ntrace, init_pos, pos, region, hits, words);
+  axx_plan_destroy(pl);
+  return s;
+}
+
+}  // extern "C"

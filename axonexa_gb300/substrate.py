@@ -1,0 +1,46 @@
+"""Substrate builders: gamma-radius random packings (native) and the
+hexagonal four-cylinder cell of the reference's hexPhase example."""
+from __future__ import annotations
+
+import ctypes as C
+import math
+
+from . import _native as N
+from .acquisition import Cylinder_XY, Lattice
+
+
+def rps_gamma_pack(seed: int, n: int, shape: float, mean: float, fraction: float, *,
+                   rmin: float = None, rmax: float = None, D_in: float, T2_in: float,
+                   D_ex: float, T2_ex: float, permeability: float = 0.0):
+    """n cylinders with gamma(shape, mean/shape) radii at area fraction
+    `fraction` in a periodic square cell (axx_substrate_rps_gamma).
+    Returns (Lattice, [Cylinder_XY...], achieved_fraction); the list holds the
+    originals then the periodic images of edge-crossing cylinders."""
+    rmin = mean * 0.05 if rmin is None else rmin
+    rmax = mean * 4.0 if rmax is None else rmax
+    cap = n * 9
+    out = (N.Basis * cap)()
+    nout, side, ach = C.c_int(), C.c_double(), C.c_double()
+    N.check(N.lib().axx_substrate_rps_gamma(seed, n, shape, mean, rmin, rmax, fraction, D_in,
+                                            T2_in, permeability, cap, out, C.byref(nout),
+                                            C.byref(side), C.byref(ach)))
+    L = side.value
+    cyl = []
+    for i in range(nout.value):
+        b = out[i]
+        cyl.append(Cylinder_XY(b.cx, b.cy, b.radius, b.T2, b.T1, b.D, b.region, b.permeability,
+                               b.eps))
+    lat = Lattice(L, L, L, T2_ex, 0.0, D_ex, len(cyl))
+    return lat, cyl, ach.value
+
+
+def hex_cell(radius: float, fraction: float, *, D_in, T2_in, D_ex, T2_ex, permeability=0.0):
+    """Hexagonal packing as a periodic d x 2h cell holding four cylinders
+    (examples/hexPhase.cu:110-124): d = sqrt(2 pi r^2 / (sqrt(3) f))."""
+    d = math.sqrt(2.0 * math.pi * radius * radius / (math.sqrt(3.0) * fraction))
+    h = d * 0.86602540378443864676372317075294
+    cyl = [Cylinder_XY(d / 2.0, 0.0, radius, T2_in, 0.0, D_in, 1, permeability),
+           Cylinder_XY(0.0, h, radius, T2_in, 0.0, D_in, 2, permeability),
+           Cylinder_XY(d / 2.0, 2.0 * h, radius, T2_in, 0.0, D_in, 3, permeability),
+           Cylinder_XY(d, h, radius, T2_in, 0.0, D_in, 4, permeability)]
+    return Lattice(d, 2.0 * h, d, T2_ex, 0.0, D_ex, 4), cyl

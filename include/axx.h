@@ -1,0 +1,264 @@
+/*
+ * axx.h -- C ABI of the GB300-native axonexa random-walker phase path.
+ *
+ * One process drives one GPU through an opaque context.  Every entry point
+ * returns an axx_status; nothing aborts the process or traps on the device.
+ * Inputs are plain structs of doubles and ints in the reference's own units
+ * (lengths in mm, time in ms, gradients in T/mm, D in mm^2/ms, kappa in mm/ms,
+ * gamma in rad/(ms*T)); any consistent unit set works as long as `gamma`
+ * matches it.  Outputs are the reference's unnormalised sums
+ *   mx[j] = sum_walkers cos(phase_j) * exp(-T2factor)
+ *   my[j] = sum_walkers sin(phase_j) * exp(-T2factor)
+ * in FP64, plus optional second moments for standard errors.
+ *
+ * Reference interfaces replaced (paths relative to the axonexa project root):
+ *   axx_run_lattice  <- phaseAcquisitionStream<F>::runAcquisitionLattice
+ *                       (src/acquisition/phaseAcquisitionStream.cuh:126-190),
+ *                       whose device work is updateWalkersLatticePhase
+ *                       (src/kernels/kernelLattice.cuh:1-104) followed by
+ *                       cudaVector::transformAndSumTwoVectors
+ *                       (src/util/cudaVector.cu:143-172).
+ *   axx_run_single   <- phaseAcquisitionStream<F>::runAcquisition
+ *                       (src/acquisition/phaseAcquisitionStream.cuh:37-88),
+ *                       device work updateWalkersPhase
+ *                       (src/kernels/kernelPhase.cuh:4-66).
+ *   axx_run_batch    <- phaseAcquisitionStream<F>::runAcquisitionStreamLattice
+ *                       (src/acquisition/phaseAcquisitionStream.cuh:425-613) and
+ *                       runAcquisitionStream (:254-423): many acquisitions,
+ *                       here in one persistent launch.
+ *   axx_bvalue       <- RectGrad/CosGFunc/SinGFunc/ApodCosGFunc/SWOGSEFunc::getB
+ *                       (src/functors/gfunctors.cuh:31-33, 89-91, 143-145,
+ *                       196-199, 257-263).
+ *   axx_gradient_eval<- the same functors' operator()(time)
+ *                       (src/functors/gfunctors.cuh:36-54, 94-113, 148-167,
+ *                       202-228, 265-283).
+ *   axx_substrate_rps_gamma <- RPSLatticeInitializer<Basis>::gammaRadialDist +
+ *                       uniformCenterDist + correctEdges
+ *                       (src/substrate/RPSinitializer.h:76-186).
+ */
+#ifndef AXX_H_
+#define AXX_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define AXX_ABI_VERSION 1
+
+typedef enum {
+  AXX_OK = 0,
+  AXX_ERR_INVALID_ARG = 1,     /* a size, pointer or parameter is out of range */
+  AXX_ERR_CUDA = 2,            /* a CUDA runtime call failed (text in axx_last_error) */
+  AXX_ERR_REFLECTION_CAP = 3,  /* some walker hit the per-step reflection cap;
+                                  results are still written, the count is in stats */
+  AXX_ERR_TIMEOUT = 4,         /* a bounded device wait ran out */
+  AXX_ERR_NO_DEVICE = 5,       /* no CUDA device, or the library was built without one */
+  AXX_ERR_OUT_OF_MEMORY = 6,
+  AXX_ERR_ABORTED = 7,         /* axx_abort() was called while the run was in flight */
+  AXX_ERR_UNSUPPORTED = 8,     /* a valid request this build does not implement */
+  AXX_ERR_NUMERIC = 9          /* a non-finite input or result */
+} axx_status;
+
+typedef struct axx_ctx axx_ctx;
+typedef struct axx_plan axx_plan;
+
+/* ---- geometry ------------------------------------------------------------ */
+
+enum { AXX_PRIM_CYLINDER_Z = 0, /* Cylinder_XY: infinite cylinder, axis along z */
+       AXX_PRIM_SPHERE = 1 };   /* Sphere */
+
+/* One basis object (src/primitives/cylinderXY.cuh:1-40, Sphere.cuh:4-44). */
+typedef struct {
+  int32_t type;          /* AXX_PRIM_* */
+  int32_t region;        /* value reported by the region lookup (Lattice::inRegion) */
+  double cx, cy, cz;     /* centre; cz is ignored for cylinders */
+  double radius;
+  double D;              /* diffusion coefficient inside */
+  double T2;             /* transverse relaxation time inside */
+  double T1;             /* carried for layout parity; unused on the phase path */
+  double permeability;   /* kappa; transmission probability is 4*kappa/v */
+  double eps;            /* minimum hit distance (cylEPS / sphereEPS) */
+} axx_basis;
+
+/* Periodic cell (src/substrate/lattice.cuh:3-23): a x b x c box with the
+ * extracellular D, T2, T1. */
+typedef struct {
+  double a, b, c;
+  double T2, T1, D;
+} axx_lattice;
+
+/* ---- gradient sequences (src/functors/gfunctors.cuh) --------------------- */
+
+enum { AXX_SEQ_PGSE = 0,      /* RectGrad(G, duration, spacing) */
+       AXX_SEQ_COS = 1,       /* CosGFunc */
+       AXX_SEQ_SIN = 2,       /* SinGFunc */
+       AXX_SEQ_APODCOS = 3,   /* ApodCosGFunc */
+       AXX_SEQ_SQUARE = 4 };  /* SWOGSEFunc (square wave, sign (-1)^floor(2 t nu)) */
+
+typedef struct {
+  int32_t kind;          /* AXX_SEQ_* */
+  int32_t num_periods;   /* OGSE periods per lobe; ignored for PGSE */
+  double G;              /* gradient amplitude */
+  double duration;       /* delta: lobe length */
+  double spacing;        /* gap between lobes (Delta - delta) */
+  double gx, gy, gz;     /* gradient direction (the reference's gHat) */
+} axx_sequence;
+
+/* ---- run parameters ------------------------------------------------------ */
+
+enum {
+  AXX_FLAG_RELAXATION = 1u << 0,        /* USE_RELAXATION: weight by exp(-sum dt/T2) */
+  AXX_FLAG_PERMEABLE = 1u << 1,         /* USE_PERMEABLE: boundaryCheckPermeable */
+  AXX_FLAG_SIMPLE_REJECTION = 1u << 2,  /* no SPECULAR_REFLECTION: reject moves that
+                                           change region */
+  AXX_FLAG_KEEP_INIT_QUIRK = 1u << 3,   /* single pore: the start position draws from a
+                                           copy of the stream, as unifRand(curandState)
+                                           by value does (Sphere.cuh:55); default on in
+                                           axx_run_single unless AXX_FLAG_FIX_INIT_QUIRK */
+  AXX_FLAG_FIX_INIT_QUIRK = 1u << 4
+};
+
+enum { AXX_INIT_UNIFORM = 0,     /* Lattice::initializeUniformly (lattice.cuh:31-37) */
+       AXX_INIT_IN_REGION = 1,   /* Lattice::initializeInRegion(region = init_arg) */
+       AXX_INIT_IN_BASIS = 2 };  /* basis[init_arg].randUnif (kernelLattice.cuh:29-34) */
+
+typedef struct {
+  int64_t num_walkers;   /* any N >= 1 (no multiple-of-block-size requirement) */
+  int32_t steps;         /* SimuParamsPhase::steps: the walk makes steps-1 moves */
+  int32_t init_mode;     /* AXX_INIT_* */
+  int32_t init_arg;
+  uint32_t flags;        /* AXX_FLAG_* */
+  uint64_t seed;         /* Philox4x32-10 key; walker w uses stream (seed, w) */
+  double timestep;
+  double gamma;          /* gyromagnetic ratio; 0 selects 267500 rad/(ms*T) */
+  int64_t walker_offset; /* first global walker id (sharding keeps streams fixed) */
+} axx_run_params;
+
+/* Optional per-sequence statistics.  Each array has nseq entries. */
+typedef struct {
+  double *sxx;           /* sum of x^2, x = cos(phase) exp(-T2factor) */
+  double *syy;           /* sum of y^2 */
+  double *sxy;           /* sum of x*y */
+  int64_t reflection_cap_hits; /* walker-steps that hit the reflection cap */
+  int64_t walker_steps;  /* moves simulated (num_walkers * (steps - 1)) */
+  int64_t boundary_hits; /* reflections and transmissions over all moves */
+} axx_stats;
+
+/* ---- context ------------------------------------------------------------- */
+
+int axx_abi_version(void);
+const char *axx_status_string(axx_status s);
+
+/* Creates a context on `device` with its own stream.  One context per host
+ * thread; contexts do not share state. */
+axx_status axx_create(axx_ctx **out, int device);
+axx_status axx_destroy(axx_ctx *ctx);
+/* Text of the last error on this context (valid until the next call). */
+const char *axx_last_error(const axx_ctx *ctx);
+/* Device properties used for grid sizing. */
+axx_status axx_device_info(axx_ctx *ctx, int *num_sms, int *cc_major, int *cc_minor,
+                           size_t *global_mem_bytes);
+/* Requests an in-flight run to stop at its next step boundary; the run then
+ * returns AXX_ERR_ABORTED.  Safe to call from another host thread. */
+axx_status axx_abort(axx_ctx *ctx);
+
+/* ---- one-shot runs (host buffers in and out; synchronous) ---------------- */
+
+/* Lattice walk: replaces runAcquisitionLattice.  basis may be NULL when
+ * nbasis == 0 (free diffusion in the periodic box). */
+axx_status axx_run_lattice(axx_ctx *ctx, const axx_lattice *lat, const axx_basis *basis,
+                           int nbasis, const axx_sequence *seqs, int nseq,
+                           const axx_run_params *params, double *mx, double *my,
+                           axx_stats *stats);
+
+/* Single-pore walk: replaces runAcquisition (walkers start inside basis[0],
+ * phase uses the bounded position, no lattice, no relaxation). */
+axx_status axx_run_single(axx_ctx *ctx, const axx_basis *basis, const axx_sequence *seqs,
+                          int nseq, const axx_run_params *params, double *mx, double *my,
+                          axx_stats *stats);
+
+/* ---- device-resident plans (inputs uploaded once, launched repeatedly) ---- */
+
+axx_status axx_plan_lattice(axx_ctx *ctx, const axx_lattice *lat, const axx_basis *basis,
+                            int nbasis, const axx_sequence *seqs, int nseq,
+                            const axx_run_params *params, axx_plan **out);
+axx_status axx_plan_single(axx_ctx *ctx, const axx_basis *basis, const axx_sequence *seqs,
+                           int nseq, const axx_run_params *params, axx_plan **out);
+/* Enqueues the walk and the signal reduction on the context stream; returns
+ * without waiting. */
+axx_status axx_plan_launch(axx_plan *plan);
+/* Waits for the last launch and copies its results to host memory. */
+axx_status axx_plan_read(axx_plan *plan, double *mx, double *my, axx_stats *stats);
+/* Per-plan facts: channels = distinct (waveform, direction) phase
+ * accumulators, instances = basis objects plus periodic ghosts,
+ * kernel_launches = kernels one axx_plan_launch enqueues. */
+axx_status axx_plan_info(const axx_plan *plan, int *channels, int *instances,
+                         int *kernel_launches, int64_t *walker_steps);
+axx_status axx_plan_destroy(axx_plan *plan);
+
+/* Timing on the context stream: record event `slot` (0..7), and read the
+ * elapsed milliseconds between two recorded slots after a sync. */
+axx_status axx_event_record(axx_ctx *ctx, int slot);
+axx_status axx_event_elapsed(axx_ctx *ctx, int slot_a, int slot_b, float *ms);
+axx_status axx_sync(axx_ctx *ctx);
+
+/* Measured FP32 issue peak of this device: fused multiply-adds per second of
+ * a register-resident FMA kernel on every SM (one FMA counts as one op, the
+ * convention of the walker's roofline).  Diagnostics for roofline reports;
+ * no reference counterpart. */
+axx_status axx_fp32_fma_peak(axx_ctx *ctx, double *fma_per_s);
+
+/* ---- sequences ----------------------------------------------------------- */
+
+/* b-value of one sequence, as the reference functor's getB(). */
+axx_status axx_bvalue(const axx_sequence *seq, double gamma, double *b);
+/* Gradient vector of one sequence at `n` times, out[3*i..3*i+2]. */
+axx_status axx_gradient_eval(const axx_sequence *seq, const double *t, int n, double *out);
+
+/* ---- randomness ---------------------------------------------------------- */
+
+/* The first n 32-bit words of walker `walker`'s stream for `seed`, computed
+ * on the device (stream word k = Philox4x32-10(key = seed, counter =
+ * (k/4, walker))[k % 4]; the walk uses words 1, 2, 3, ...). */
+axx_status axx_philox_words(axx_ctx *ctx, uint64_t seed, uint64_t walker, int n,
+                            uint32_t *out);
+
+/* ---- parity instrumentation ---------------------------------------------- */
+
+/* Runs the lattice walk for walkers [walker_offset, walker_offset+ntrace) and
+ * records, after every move i = 1..steps-1: the wrapped position, the region
+ * index (-1 = extracellular), the number of boundary hits of that move and
+ * the number of random words consumed so far.  Layout: pos[(w*(steps-1)+i-1)*3+k],
+ * region/hits/words[w*(steps-1)+i-1].  init_pos[w*3+k] is the start position. */
+axx_status axx_trace_lattice(axx_ctx *ctx, const axx_lattice *lat, const axx_basis *basis,
+                             int nbasis, const axx_run_params *params, int ntrace,
+                             float *init_pos, float *pos, int32_t *region, int32_t *hits,
+                             int32_t *words);
+/* The same for the single-pore walk. */
+axx_status axx_trace_single(axx_ctx *ctx, const axx_basis *basis,
+                            const axx_run_params *params, int ntrace, float *init_pos,
+                            float *pos, int32_t *region, int32_t *hits, int32_t *words);
+
+/* ---- substrates (host) ---------------------------------------------------- */
+
+/* Random sequential packing of `n` cylinders with gamma(shape, mean/shape)
+ * radii in a periodic square cell whose side is chosen so the intracellular
+ * area fraction is `fraction`; radii are truncated to [rmin, rmax].  Writes
+ * the cell side to *side and up to max_out bases (originals first, then the
+ * periodic images of the ones that cross the cell edge) to out, their count to
+ * *nout and the achieved area fraction to *achieved.  D_in, T2_in and
+ * permeability fill the basis records; region = index+1 as correctEdges sets. */
+axx_status axx_substrate_rps_gamma(uint64_t seed, int n, double shape, double mean,
+                                   double rmin, double rmax, double fraction,
+                                   double D_in, double T2_in, double permeability,
+                                   int max_out, axx_basis *out, int *nout, double *side,
+                                   double *achieved);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* AXX_H_ */

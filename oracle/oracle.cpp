@@ -1,0 +1,1061 @@
+// oracle.cpp -- CPU oracle of the axonexa random-walker phase path.
+//
+// TEST INFRASTRUCTURE ONLY (the checker; see oracle.h).  Compile with
+// -ffp-contract=off so that no multiply-add is fused behind the code's back:
+// every fused operation here is an explicit std::fma.
+//
+// Reference citations are to the axonexa project tree (src/...).
+#include "oracle.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <thread>
+#include <type_traits>
+#include <vector>
+
+namespace {
+
+const double kPI = 3.1415926535897932384626433832795;  // examples/*.cu PI
+const double kGAMMA = 267500.0;                          // examples/gammadist.cu:5
+
+// ---------------------------------------------------------------- Philox ---
+// Philox4x32-10 (Salmon et al., SC'11): multipliers 0xD2511F53, 0xCD9E8D57,
+// Weyl increments 0x9E3779B9, 0xBB67AE85.
+void philox(uint32_t c[4], uint32_t k0, uint32_t k1) {
+  for (int r = 0; r < 10; ++r) {
+    const uint64_t p0 = (uint64_t)0xD2511F53u * c[0];
+    const uint64_t p1 = (uint64_t)0xCD9E8D57u * c[2];
+    const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c[1] ^ k0;
+    const uint32_t n2 = (uint32_t)(p0 >> 32) ^ c[3] ^ k1;
+    c[0] = n0;
+    c[1] = (uint32_t)p1;
+    c[2] = n2;
+    c[3] = (uint32_t)p0;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+}
+
+// The per-walker stream: word k = Philox(key = seed, ctr = (k/4, 0, w_lo,
+// w_hi))[k % 4]; draws start at word 1.  This is what the reference's
+// curandState stands for (curand_init(seed, tid, 0), kernelSetup.cuh:1-5).
+struct Stream {
+  uint64_t seed, walker;
+  uint32_t word;  // next word index
+  uint32_t cached_blk = 0xffffffffu;
+  uint32_t buf[4];
+  uint32_t next_word() {
+    const uint32_t blk = word >> 2;
+    if (blk != cached_blk) {
+      uint32_t c[4] = {blk, 0u, (uint32_t)walker, (uint32_t)(walker >> 32)};
+      philox(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+      std::memcpy(buf, c, 16);
+      cached_blk = blk;
+    }
+    return buf[word++ & 3u];
+  }
+  // curand_uniform stand-in: ((x >> 9) + 1/2) * 2^-23, a float in (0, 1)
+  float uniform() { return (float)(next_word() >> 9) * 1.1920928955078125e-07f + 5.9604644775390625e-08f; }
+};
+
+// ------------------------------------------------------------- sequences ---
+struct V3 {
+  double x, y, z;
+};
+V3 operator+(V3 a, V3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+V3 operator-(V3 a, V3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+V3 operator*(V3 a, double s) { return {a.x * s, a.y * s, a.z * s}; }
+V3 operator/(V3 a, double s) { return {a.x / s, a.y / s, a.z / s}; }
+double dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }  // vector3.cuh:155-158
+double mag(V3 a) { return std::sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }
+
+// G(t) of one sequence: RectGrad :36-54, CosGFunc :94-113, SinGFunc
+// :148-167, ApodCosGFunc :202-228, SWOGSEFunc :265-283 (gfunctors.cuh).  The
+// square wave uses (-1)^floor(2 t nu); the reference's pow(-1., 2 t nu) is
+// NaN for non-integer exponents.
+V3 gfunc(const orc_sequence &q, double time) {
+  const V3 gh = {q.gx, q.gy, q.gz};
+  const double G = q.G, dur = q.duration, sp = q.spacing;
+  const double n = (double)q.num_periods;
+  auto amp = [&](double t) -> double {
+    switch (q.kind) {
+      case 1: return std::cos(2.0 * kPI * t / (dur / n));
+      case 2: return std::sin(2.0 * kPI * t / (dur / n));
+      case 3: {
+        const double period = dur / n;
+        if (t >= period / 4.0 && t < dur - period / 4.0) return std::cos(2.0 * kPI * t / period);
+        return std::sin(4.0 * kPI * t / period);
+      }
+      case 4: {
+        const double k = std::floor(2.0 * t * (n / dur));
+        return std::fmod(k, 2.0) != 0.0 ? -1.0 : 1.0;
+      }
+    }
+    return 1.0;
+  };
+  if (q.kind == 0) {
+    if (time < dur) return gh * G;
+    if (time >= sp + dur && time < 2.0 * dur + sp) return gh * -G;
+    return gh * 0.0;
+  }
+  if (time < dur) return (gh * G) * amp(time);
+  if (time >= sp + dur && time < 2.0 * dur + sp) return (gh * -G) * amp(time - sp - dur);
+  return {0.0, 0.0, 0.0};
+}
+
+// ----------------------------------------------------- reference geometry ---
+// Cylinder_XY (cylinderXY.cuh) and Sphere (Sphere.cuh) in FP64 with the
+// reference's operation order.
+int sgn(double v) { return (0.0 < v) - (v < 0.0); }  // misc.cuh:3
+
+struct RefBasis {
+  const orc_basis *b;
+  bool sph() const { return b->type == 1; }
+  bool inside(V3 r) const {  // cylinderXY.cuh:69-74, Sphere.cuh:89-94
+    const double cx = b->cx, cy = b->cy, cz = b->cz, R = b->radius;
+    if (sph())
+      return (r.x - cx) * (r.x - cx) + (r.y - cy) * (r.y - cy) + (r.z - cz) * (r.z - cz) < R * R;
+    return (r.x - cx) * (r.x - cx) + (r.y - cy) * (r.y - cy) < R * R;
+  }
+  // cylinderXY.cuh:82-122, Sphere.cuh:102-139
+  bool intersect(V3 ri, V3 rf, double &v) const {
+    const double cx = b->cx, cy = b->cy, cz = b->cz, R = b->radius;
+    const V3 dr = rf - ri;
+    const double step_mag = mag(dr);
+    double a, bb, c;
+    if (sph()) {
+      a = dr.x * dr.x + dr.y * dr.y + dr.z * dr.z;
+      bb = 2.0 * ri.x * dr.x - 2.0 * dr.x * cx + 2.0 * ri.y * dr.y - 2.0 * dr.y * cy +
+           2.0 * ri.z * dr.z - 2.0 * dr.z * cz;
+      c = ri.x * ri.x + ri.y * ri.y + ri.z * ri.z - 2 * ri.x * cx - 2 * ri.y * cy - 2 * ri.z * cz +
+          cx * cx + cy * cy + cz * cz - R * R;
+    } else {
+      a = dr.x * dr.x + dr.y * dr.y;
+      bb = 2.0 * ri.x * dr.x - 2.0 * dr.x * cx + 2.0 * ri.y * dr.y - 2.0 * dr.y * cy;
+      c = ri.x * ri.x + ri.y * ri.y - 2.0 * ri.x * cx - 2.0 * ri.y * cy + cx * cx + cy * cy -
+          R * R;
+    }
+    const double q = -.5 * (bb + sgn(bb) * std::sqrt(bb * bb - 4 * a * c));
+    const double root1 = q / a, root2 = c / q;
+    const double eps = b->eps;
+    const bool s1 = root1 > 0.0 && root1 < 1.0 && bb * bb > 4 * a * c &&
+                    !(std::fabs(root1 * step_mag - 0.0) < eps);
+    const bool s2 = root2 > 0.0 && root2 < 1.0 && bb * bb > 4 * a * c &&
+                    !(std::fabs(root2 * step_mag - 0.0) < eps);
+    const bool s3 = std::fabs(root1) < std::fabs(root2);
+    if ((s1 && s2 && s3) || (s1 && !s2)) {
+      v = root1;
+      return true;
+    }
+    if ((s1 && s2 && !s3) || (s2 && !s1)) {
+      v = root2;
+      return true;
+    }
+    return false;
+  }
+  V3 normal(V3 r) const {  // cylinderXY.cuh:125-131, Sphere.cuh:142-149
+    const double nx = r.x - b->cx, ny = r.y - b->cy;
+    if (sph()) {
+      const double nz = r.z - b->cz;
+      const double m = std::sqrt(nx * nx + ny * ny + nz * nz);
+      return {nx / m, ny / m, nz / m};
+    }
+    const double m = std::sqrt(nx * nx + ny * ny);
+    return {nx / m, ny / m, 0.0};
+  }
+};
+
+// Lattice (lattice.cuh:3-254) over the listed bases only.
+struct RefLattice {
+  double a, b, c, D, T2;
+  std::vector<RefBasis> B;
+  void lmod(V3 &r) const {  // :66-88
+    if (r.x > a) r.x = std::fmod(r.x, a);
+    if (r.x < 0.0) r.x = std::fmod(r.x, a) + a;
+    if (r.y > b) r.y = std::fmod(r.y, b);
+    if (r.y < 0.0) r.y = std::fmod(r.y, b) + b;
+    if (r.z > c) r.z = std::fmod(r.z, c);
+    if (r.z < 0.0) r.z = std::fmod(r.z, c) + c;
+  }
+  bool in_cell(V3 r) const {  // :150-156
+    return !(r.x > a || r.x < 0.0 || r.y > b || r.y < 0.0 || r.z > c || r.z < 0.0);
+  }
+  void correct(V3 &r) const {  // :60-64
+    if (!in_cell(r)) lmod(r);
+  }
+  double getD(V3 r) const {  // :118-132 (a basis counts if its value is > 0)
+    lmod(r);
+    for (auto &q : B)
+      if (q.inside(r) && q.b->D > 0) return q.b->D;
+    return D;
+  }
+  double getT2(V3 r) const {  // :90-102
+    lmod(r);
+    for (auto &q : B)
+      if (q.inside(r) && q.b->T2 > 0) return q.b->T2;
+    return T2;
+  }
+  int first_inside(V3 r) const {  // index form of inRegion (:134-148)
+    lmod(r);
+    for (size_t i = 0; i < B.size(); ++i)
+      if (B[i].inside(r)) return (int)i;
+    return -1;
+  }
+  int region(V3 r) const {
+    const int i = first_inside(r);
+    return i < 0 ? 0 : B[i].b->region;
+  }
+  // intersectionCheckPermeable / Impermeable (:158-247)
+  bool check(V3 ri, V3 rf, double &v, V3 &n, double &perm) const {
+    const V3 dr = rf - ri;
+    V3 m1f = rf;
+    lmod(m1f);
+    const V3 m1i = m1f - dr;
+    V3 m2i = ri;
+    lmod(m2i);
+    const V3 m2f = m2i + dr;
+    double vt = 0.0, best = 10.0;
+    for (auto &q : B) {
+      if (q.intersect(m1i, m1f, vt) && vt < best) {
+        best = vt;
+        n = q.normal(dr * best + m1i);
+        perm = q.b->permeability;
+      }
+      if (q.intersect(m2i, m2f, vt) && vt < best) {
+        best = vt;
+        n = q.normal(dr * best + m2i);
+        perm = q.b->permeability;
+      }
+    }
+    v = best;
+    return best < 5.0;
+  }
+};
+
+// --------------------------------------------------------- kernel geometry ---
+// The GPU kernel's formulation (axonexa_gb300/csrc/walk_kernel.cuh restated):
+// instances = bases plus periodic ghosts, centre-relative quadratic in the
+// distance along the unit direction, last-hit instance tested on its surface.
+template <typename T>
+T fmaT(T a, T b, T c) {
+  return std::fma(a, b, c);
+}
+
+template <typename T>
+struct KInst {
+  T cx, cy, cz, negR2, invR, eps;
+  int slot;
+  bool sph;
+};
+
+template <typename T>
+struct KGeom {
+  std::vector<KInst<T>> inst;
+  std::vector<T> speed, step, t2term, kappa4;
+  std::vector<int> region;
+  int ecs = 0;
+  T a = 0, b = 0, c = 0;
+};
+
+template <typename T>
+T c0_of(const KInst<T> &g, T x, T y, T z) {
+  const T px = x - g.cx, py = y - g.cy;
+  if (g.sph) {
+    const T pz = z - g.cz;
+    return fmaT(px, px, fmaT(py, py, fmaT(pz, pz, g.negR2)));
+  }
+  return fmaT(px, px, fmaT(py, py, g.negR2));
+}
+
+template <typename T>
+int k_lookup(const KGeom<T> &G, T x, T y, T z) {
+  for (const auto &g : G.inst)
+    if (c0_of(g, x, y, z) < T(0)) return g.slot;
+  return G.ecs;
+}
+
+template <typename T>
+T k_seg_hit(const KInst<T> &g, bool on_surface, T sx, T sy, T sz, T dx, T dy, T dz, T aa, T rem) {
+  const T inf = std::numeric_limits<T>::infinity();
+  const T px = sx - g.cx, py = sy - g.cy;
+  const T pz = g.sph ? (sz - g.cz) : T(0);
+  T bh, c0, c1;
+  const T ex = fmaT(rem, dx, px), ey = fmaT(rem, dy, py);
+  if (g.sph) {
+    const T ez = fmaT(rem, dz, pz);
+    bh = fmaT(px, dx, fmaT(py, dy, pz * dz));
+    c0 = fmaT(px, px, fmaT(py, py, fmaT(pz, pz, g.negR2)));
+    c1 = fmaT(ex, ex, fmaT(ey, ey, fmaT(ez, ez, g.negR2)));
+  } else {
+    bh = fmaT(px, dx, py * dy);
+    c0 = fmaT(px, px, fmaT(py, py, g.negR2));
+    c1 = fmaT(ex, ex, fmaT(ey, ey, g.negR2));
+  }
+  if (on_surface) c0 = T(0);
+  T s;
+  if (c0 < T(0)) {
+    if (c1 < T(0)) return inf;
+    const T disc = fmaT(bh, bh, -(aa * c0));
+    const T sq = std::sqrt(disc);
+    s = (bh <= T(0)) ? (sq - bh) / aa : (-c0) / (bh + sq);
+  } else if (c0 > T(0)) {
+    if (bh >= T(0)) return inf;
+    if (c1 > T(0) && fmaT(aa, rem, bh) <= T(0)) return inf;
+    const T disc = fmaT(bh, bh, -(aa * c0));
+    if (disc <= T(0)) return inf;
+    const T sq = std::sqrt(disc);
+    s = c0 / (sq - bh);
+  } else {
+    if (bh >= T(0)) return inf;
+    s = (T(-2) * bh) / aa;
+  }
+  if (!(s > T(0) && s < rem && s >= g.eps)) return inf;
+  return s;
+}
+
+template <typename T>
+struct KMove {
+  T fx, fy, fz;
+  int hits;
+  bool capped;
+};
+
+template <typename T>
+KMove<T> k_boundary(const KGeom<T> &G, T sx, T sy, T sz, T dx, T dy, T dz, T L, T v, bool perm,
+                    Stream &st) {
+  KMove<T> o{T(0), T(0), T(0), 0, false};
+  T rem = L;
+  int last = -1;
+  for (;;) {
+    const T aa_c = fmaT(dx, dx, dy * dy);
+    const T aa_s = fmaT(dx, dx, fmaT(dy, dy, dz * dz));
+    T best = std::numeric_limits<T>::infinity();
+    int bk = -1;
+    for (size_t k = 0; k < G.inst.size(); ++k) {
+      const KInst<T> &g = G.inst[k];
+      const T s = k_seg_hit(g, (int)k == last, sx, sy, sz, dx, dy, dz, g.sph ? aa_s : aa_c, rem);
+      if (s < best) {
+        best = s;
+        bk = (int)k;
+      }
+    }
+    if (bk < 0) break;
+    if (o.hits == 16) {
+      o.capped = true;
+      o.fx = sx;
+      o.fy = sy;
+      o.fz = sz;
+      return o;
+    }
+    ++o.hits;
+    const T hx = fmaT(best, dx, sx), hy = fmaT(best, dy, sy), hz = fmaT(best, dz, sz);
+    const T rem_before = rem;
+    rem = rem - best;
+    const KInst<T> &g = G.inst[bk];
+    if (perm) {
+      const T u = (T)st.uniform();
+      const T ptr = G.kappa4[g.slot] / v;
+      if (!(u > ptr)) {
+        const T tx = fmaT(rem_before, dx, sx), ty = fmaT(rem_before, dy, sy),
+                tz = fmaT(rem_before, dz, sz);
+        const int ts = k_lookup(G, tx, ty, tz);
+        const T remt = (rem * G.speed[ts]) / v;
+        o.fx = fmaT(remt, dx, hx);
+        o.fy = fmaT(remt, dy, hy);
+        o.fz = fmaT(remt, dz, hz);
+        return o;
+      }
+    }
+    const T nx = (hx - g.cx) * g.invR, ny = (hy - g.cy) * g.invR;
+    const T nz = g.sph ? (hz - g.cz) * g.invR : T(0);
+    const T dn = g.sph ? fmaT(dx, nx, fmaT(dy, ny, dz * nz)) : fmaT(dx, nx, dy * ny);
+    const T t = T(-2) * dn;
+    dx = fmaT(t, nx, dx);
+    dy = fmaT(t, ny, dy);
+    if (g.sph) dz = fmaT(t, nz, dz);
+    sx = hx;
+    sy = hy;
+    sz = hz;
+    last = bk;
+  }
+  o.fx = fmaT(rem, dx, sx);
+  o.fy = fmaT(rem, dy, sy);
+  o.fz = fmaT(rem, dz, sz);
+  return o;
+}
+
+// sin/cos(2*pi*u): quadrant reduction of u and Taylor polynomials of
+// sin(2*pi*f), cos(2*pi*f), |f| <= 1/8, coefficients (2*pi)^k/k! rounded to
+// the working precision.
+template <typename T>
+void k_sincos_2pi(T u, T &s, T &c) {
+  const T q = std::nearbyint(u * T(4));
+  const T f = fmaT(q, T(-0.25), u);
+  const T f2 = f * f;
+  T ps, pc;
+  if (std::is_same<T, float>::value) {
+    ps = fmaT(f2, (T)0x1.5078340p+5f, (T)-0x1.32d2ccp+6f);
+    ps = fmaT(f2, ps, (T)0x1.466bc6p+6f);
+    ps = fmaT(f2, ps, (T)-0x1.4abbcep+5f);
+    ps = fmaT(f2, ps, (T)0x1.921fb6p+2f);
+    pc = fmaT(f2, (T)-0x1.a6d1f2p+4f, (T)0x1.e1f506p+5f);
+    pc = fmaT(f2, pc, (T)-0x1.55d3c8p+6f);
+    pc = fmaT(f2, pc, (T)0x1.03c1f0p+6f);
+    pc = fmaT(f2, pc, (T)-0x1.3bd3ccp+4f);
+  } else {
+    // FP64: more terms of the same series
+    const double tp = 2.0 * kPI;
+    double cs_[9], cc_[9];
+    double fac = 1.0, pw = 1.0;
+    int ns = 0, nc = 0;
+    for (int k = 0; k <= 17; ++k) {
+      if (k > 0) {
+        fac *= k;
+        pw *= tp;
+      }
+      const double term = pw / fac * (((k / 2) % 2) ? -1.0 : 1.0);
+      if (k % 2) cs_[ns++] = term;
+      else cc_[nc++] = term;
+    }
+    T a = (T)cs_[ns - 1];
+    for (int k = ns - 2; k >= 0; --k) a = fmaT(f2, a, (T)cs_[k]);
+    ps = a;
+    T b = (T)cc_[nc - 1];
+    for (int k = nc - 2; k >= 1; --k) b = fmaT(f2, b, (T)cc_[k]);
+    pc = b;
+  }
+  const T sn = f * ps;
+  const T cs = fmaT(f2, pc, T(1));
+  const int qi = ((int)q) & 3;
+  const T s1 = (qi & 1) ? cs : sn;
+  const T c1 = (qi & 1) ? sn : cs;
+  s = (qi & 2) ? -s1 : s1;
+  c = ((qi + 1) & 2) ? -c1 : c1;
+}
+
+template <typename T>
+void k_direction(T u1, T u2, T &dx, T &dy, T &dz) {
+  T sp, cp;
+  k_sincos_2pi(u1, sp, cp);
+  const T z = fmaT(T(2), u2, T(-1));
+  const T st = std::sqrt(fmaT(-z, z, T(1)));
+  dx = st * cp;
+  dy = st * sp;
+  dz = z;
+}
+
+template <typename T>
+T k_wrap(T x, T a) {
+  if (x > a) return x - a;
+  if (x < T(0)) return x + a;
+  return x;
+}
+
+// Kernel geometry: slot tables (speed, step, dt/T2, 4 kappa) from FP64
+// formulas rounded to T, bases then all periodic ghosts that coincide with no
+// listed basis.
+template <typename T>
+void k_build(const orc_lattice *lat, const orc_basis *basis, int nbasis, double dt, bool relax,
+             bool single, KGeom<T> &G) {
+  auto slot = [&](double D, double T2, double kappa) {
+    const double sp = std::sqrt(6.0 * D / dt);
+    G.speed.push_back((T)sp);
+    G.step.push_back((T)(sp * dt));
+    G.t2term.push_back((relax && T2 > 0.0) ? (T)(dt / T2) : T(0));
+    G.kappa4.push_back((T)(4.0 * kappa));
+  };
+  for (int k = 0; k < nbasis; ++k) {
+    slot(basis[k].D, basis[k].T2, basis[k].permeability);
+    G.region.push_back(basis[k].region);
+  }
+  if (single) slot(basis[0].D, basis[0].T2, 0.0);
+  else slot(lat->D, lat->T2, 0.0);
+  G.region.push_back(0);
+  G.ecs = nbasis;
+  auto add = [&](int k, double cx, double cy, double cz) {
+    const orc_basis &b = basis[k];
+    KInst<T> g;
+    g.cx = (T)cx;
+    g.cy = (T)cy;
+    g.cz = (T)cz;
+    g.negR2 = (T)(-(b.radius * b.radius));
+    g.invR = (T)(1.0 / b.radius);
+    g.eps = (T)b.eps;
+    g.slot = k;
+    g.sph = b.type == 1;
+    G.inst.push_back(g);
+  };
+  if (single) {
+    add(0, basis[0].cx, basis[0].cy, basis[0].cz);
+    return;
+  }
+  G.a = (T)lat->a;
+  G.b = (T)lat->b;
+  G.c = (T)lat->c;
+  const double A = lat->a, B = lat->b, C = lat->c;
+  const double tol = 1e-9 * std::max(A, std::max(B, C));
+  for (int k = 0; k < nbasis; ++k) {
+    const orc_basis &b = basis[k];
+    add(k, b.cx, b.cy, b.cz);
+    const int zr = b.type == 1 ? 1 : 0;
+    for (int i = -1; i <= 1; ++i)
+      for (int j = -1; j <= 1; ++j)
+        for (int l = -zr; l <= zr; ++l) {
+          if (i == 0 && j == 0 && l == 0) continue;
+          const double cx = b.cx + A * i, cy = b.cy + B * j, cz = b.cz + C * l;
+          bool dup = false;
+          for (int o = 0; o < nbasis && !dup; ++o) {
+            const orc_basis &q = basis[o];
+            if (q.type != b.type || std::fabs(q.radius - b.radius) > tol) continue;
+            if (std::fabs(q.cx - cx) > tol || std::fabs(q.cy - cy) > tol) continue;
+            if (b.type == 1 && std::fabs(q.cz - cz) > tol) continue;
+            dup = true;
+          }
+          if (!dup) add(k, cx, cy, cz);
+        }
+  }
+}
+
+// ------------------------------------------------------------- one walker ---
+struct WalkIn {
+  const orc_lattice *lat;
+  const orc_basis *basis;
+  int nbasis;
+  const orc_sequence *seqs;
+  int nseq;
+  const orc_params *p;
+  double gamma;
+  bool single, relax, perm, reject;
+};
+
+struct WalkOut {
+  std::vector<double> phase;
+  double t2factor = 0.0;  // the value whose exp weights the signal
+  int64_t caps = 0;
+};
+
+struct TraceRow {
+  double *init_pos, *pos;
+  int32_t *region, *hits, *words;
+};
+
+// Reference-order FP64 walk: updateWalkersLatticePhase
+// (kernelLattice.cuh:1-104) or updateWalkersPhase (kernelPhase.cuh:4-66).
+void walk_ref(const WalkIn &in, const RefLattice &L, int64_t w, WalkOut &out, TraceRow *tr) {
+  const orc_params &p = *in.p;
+  const double dt = p.timestep;
+  Stream st{p.seed, (uint64_t)(w + p.walker_offset), 1u};
+  V3 r{0, 0, 0};
+  if (in.single) {
+    // Basis::unifRand(curandState) by value: draws on a copy of the stream
+    // (cylinderXY.cuh:45-55, Sphere.cuh:55-63)
+    Stream cp = st;
+    const orc_basis &b = in.basis[0];
+    const RefBasis rb{&b};
+    if (b.type == 1) {
+      const double R = b.radius;
+      // first draw: three statements x, y, z (Sphere.cuh:57-59); retries pass
+      // three draws as Vector3 constructor arguments (:62-64), an evaluation
+      // order C++ leaves unspecified -- drawn here z, y, x, as the compiled
+      // reference consumes them
+      r.x = R * (2.0 * cp.uniform() - 1);
+      r.y = R * (2.0 * cp.uniform() - 1);
+      r.z = R * (2.0 * cp.uniform() - 1);
+      for (int t = 0; t < 100000 && !rb.inside(r); ++t) {
+        r.z = R * (2.0 * cp.uniform() - 1);
+        r.y = R * (2.0 * cp.uniform() - 1);
+        r.x = R * (2.0 * cp.uniform() - 1);
+      }
+    } else {
+      const double R = b.radius;
+      for (int t = 0; t < 100000; ++t) {
+        r.x = R * (2.0 * cp.uniform() - 1) + b.cx;
+        r.y = R * (2.0 * cp.uniform() - 1) + b.cy;
+        r.z = 2.0 * R * cp.uniform();
+        if (rb.inside(r)) break;
+      }
+    }
+  } else if (p.init_mode == 2) {
+    // Basis::randUnif (cylinderXY.cuh:176-183, Sphere.cuh:384-391)
+    const orc_basis &b = in.basis[p.init_arg];
+    const RefBasis rb{&b};
+    const V3 cen = {b.cx, b.cy, b.type == 1 ? b.cz : 0.0};
+    for (int t = 0; t < 100000; ++t) {
+      // constructor arguments: drawn z, y, x (see the single-pore sphere above)
+      const double z = (2.0 * st.uniform() - 1.0) * b.radius;
+      const double y = (2.0 * st.uniform() - 1.0) * b.radius;
+      const double x = (2.0 * st.uniform() - 1.0) * b.radius;
+      r = V3{x, y, z} + cen;
+      if (rb.inside(r)) break;
+    }
+  } else {
+    // Lattice::initializeUniformly / initializeInRegion (lattice.cuh:31-58)
+    for (int t = 0; t < 100000; ++t) {
+      r.x = st.uniform() * L.a;
+      r.y = st.uniform() * L.b;
+      r.z = st.uniform() * L.c;
+      if (p.init_mode == 0 || L.region(r) == p.init_arg) break;
+    }
+  }
+  if (tr) {
+    tr->init_pos[0] = r.x;
+    tr->init_pos[1] = r.y;
+    tr->init_pos[2] = r.z;
+  }
+  V3 ru = r;
+  for (int j = 0; j < in.nseq; ++j) out.phase[j] = in.gamma * dot(gfunc(in.seqs[j], 0.0), r) * dt;
+  double T2f = 0.0;
+  const orc_basis *b0 = in.single ? &in.basis[0] : nullptr;
+  const double speed0 = in.single ? std::sqrt(6.0 * b0->D / dt) : 0.0;
+  for (int i = 1; i < p.steps; ++i) {
+    V3 ri = r;
+    const double speed = in.single ? speed0 : std::sqrt(6.0 * L.getD(r) / dt);
+    const double phi = 2.0 * kPI * st.uniform();
+    const double theta = std::acos(2.0 * st.uniform() - 1);
+    r = r + V3{speed * dt * std::sin(theta) * std::cos(phi), speed * dt * std::sin(theta) * std::sin(phi),
+               speed * dt * std::cos(theta)};
+    int hits = 0;
+    if (in.single) {
+      const RefBasis rb{b0};
+      if (!in.reject) {
+        // boundaryNormal (boundaryCheck.cuh:2-32)
+        double v = 0.0, acc = 0.0;
+        while (rb.intersect(ri, r, v)) {
+          ++hits;
+          r = (r - ri) * v + ri;
+          const V3 I = r - ri;
+          const double Im = mag(I);
+          acc += Im / speed;
+          const V3 n = rb.normal(r);
+          ri = r;
+          r = r + ((I - (n * 2.0) * dot(n, I)) * (speed / Im)) * (dt - acc);
+        }
+      } else if (!rb.inside(r)) {
+        r = ri;
+      }
+    } else if (in.reject) {
+      if (L.region(ri) != L.region(r)) r = ri;  // kernelLattice.cuh:75-77
+    } else if (!in.perm) {
+      // boundaryCheckImpermeable (boundaryCheck.cuh:34-64)
+      double v = 0.0, acc = 0.0, pm = 0.0;
+      V3 n{0, 0, 0}, rc = ri;
+      while (L.check(rc, r, v, n, pm)) {
+        ++hits;
+        r = (r - rc) * v + rc;
+        const V3 I = r - rc;
+        const double Im = mag(I);
+        acc += Im / speed;
+        rc = r;
+        r = r + ((I - (n * 2.0) * dot(n, I)) * (speed / Im)) * (dt - acc);
+      }
+    } else {
+      // boundaryCheckPermeable (boundaryCheck.cuh:66-113); accumtime enters
+      // by value, so the T2 weighting below sees 0 (kernelLattice.cuh:66-68)
+      double v = 0.0, acc = 0.0, pm = 0.0;
+      V3 n{0, 0, 0}, rc = ri;
+      bool transmitted = false;
+      const double cur = std::sqrt(6.0 * L.getD(ri) / dt);
+      while (L.check(rc, r, v, n, pm) && transmitted == false) {
+        ++hits;
+        const double trs = std::sqrt(6.0 * L.getD(r) / dt);
+        r = (r - rc) * v + rc;
+        const V3 I = r - rc;
+        const double Im = mag(I);
+        acc += Im / cur;
+        if (st.uniform() > pm * 4.0 / cur) {
+          rc = r;
+          r = r + ((I - (n * 2.0) * dot(n, I)) * (cur / Im)) * (dt - acc);
+        } else {
+          r = r + ((I / Im) * trs) * (dt - acc);
+          transmitted = true;
+        }
+      }
+    }
+    const V3 pos_for_phase = in.single ? r : (ru = ru + (r - ri), ru);
+    for (int j = 0; j < in.nseq; ++j)
+      out.phase[j] += in.gamma * dot(gfunc(in.seqs[j], dt * i), pos_for_phase) * dt;
+    if (in.relax) {
+      if (in.perm) T2f += (0.0 / L.getT2(ri)) + ((dt - 0.0) / L.getT2(r));
+      else T2f += dt / L.getT2(ri);
+    }
+    if (!in.single) L.correct(r);
+    if (tr) {
+      const size_t o = (size_t)(i - 1);
+      tr->pos[o * 3 + 0] = r.x;
+      tr->pos[o * 3 + 1] = r.y;
+      tr->pos[o * 3 + 2] = r.z;
+      tr->region[o] = in.single ? (RefBasis{b0}.inside(r) ? 0 : -1) : L.first_inside(r);
+      tr->hits[o] = hits;
+      tr->words[o] = (int32_t)st.word;
+    }
+  }
+  out.t2factor = T2f;
+}
+
+// Kernel-formulation walk in T (float: the GPU kernel bit for bit).
+template <typename T>
+void walk_kern(const WalkIn &in, const KGeom<T> &G, int64_t w, WalkOut &out, TraceRow *tr) {
+  const orc_params &p = *in.p;
+  const double dt = p.timestep;
+  Stream st{p.seed, (uint64_t)(w + p.walker_offset), 1u};
+  T x = 0, y = 0, z = 0;
+  auto U = [](Stream &s) { return (T)s.uniform(); };
+  if (in.single || p.init_mode == 2) {
+    const int k = in.single ? 0 : p.init_arg;
+    const orc_basis &b = in.basis[k];
+    const KInst<T> *g = nullptr;
+    for (auto &q : G.inst)
+      if (q.slot == k) {
+        g = &q;
+        break;
+      }
+    const T R = (T)b.radius, cx = (T)b.cx, cy = (T)b.cy, cz = (T)b.cz;
+    const bool sph = b.type == 1;
+    Stream cp = st;
+    Stream &s = in.single ? cp : st;
+    auto draw = [&](T c) { return fmaT(fmaT(T(2), U(s), T(-1)), R, c); };
+    if (in.single) {
+      x = draw(cx);
+      y = draw(cy);
+      z = sph ? draw(cz) : (T(2) * R) * U(s);
+      for (int t = 0; t < 100000 && !(c0_of(*g, x, y, z) < T(0)); ++t) {
+        if (sph) {
+          z = draw(cz);
+          y = draw(cy);
+          x = draw(cx);
+        } else {
+          x = draw(cx);
+          y = draw(cy);
+          z = (T(2) * R) * U(s);
+        }
+      }
+    } else {
+      for (int t = 0; t < 100000; ++t) {
+        const T tz = fmaT(T(2), U(s), T(-1));
+        y = draw(cy);
+        x = draw(cx);
+        z = sph ? fmaT(tz, R, cz) : tz * R;
+        if (c0_of(*g, x, y, z) < T(0)) break;
+      }
+    }
+  } else {
+    for (int t = 0; t < 100000; ++t) {
+      x = U(st) * G.a;
+      y = U(st) * G.b;
+      z = U(st) * G.c;
+      if (p.init_mode == 0 || G.region[k_lookup(G, x, y, z)] == p.init_arg) break;
+    }
+  }
+  if (tr) {
+    tr->init_pos[0] = (double)x;
+    tr->init_pos[1] = (double)y;
+    tr->init_pos[2] = (double)z;
+  }
+  T ux = x, uy = y, uz = z;
+  for (int j = 0; j < in.nseq; ++j)
+    out.phase[j] = in.gamma * dot(gfunc(in.seqs[j], 0.0), V3{(double)x, (double)y, (double)z}) * dt;
+  T t2s = 0, t2c = 0;
+  int slot = in.single ? 0 : k_lookup(G, x, y, z);
+  const bool geom = !G.inst.empty();
+  for (int i = 1; i < p.steps; ++i) {
+    const T v = G.speed[slot], Ls = G.step[slot];
+    const T u1 = U(st), u2 = U(st);
+    T dx, dy, dz;
+    k_direction(u1, u2, dx, dy, dz);
+    T fx, fy, fz;
+    int hits = 0;
+    if (!geom) {
+      fx = fmaT(Ls, dx, x);
+      fy = fmaT(Ls, dy, y);
+      fz = fmaT(Ls, dz, z);
+    } else if (in.reject) {
+      fx = fmaT(Ls, dx, x);
+      fy = fmaT(Ls, dy, y);
+      fz = fmaT(Ls, dz, z);
+      if (in.single) {
+        if (!(c0_of(G.inst[0], fx, fy, fz) < T(0))) {
+          fx = x;
+          fy = y;
+          fz = z;
+        }
+      } else if (G.region[k_lookup(G, fx, fy, fz)] != G.region[slot]) {
+        fx = x;
+        fy = y;
+        fz = z;
+      }
+    } else {
+      const KMove<T> o = k_boundary(G, x, y, z, dx, dy, dz, Ls, v, in.perm, st);
+      fx = o.fx;
+      fy = o.fy;
+      fz = o.fz;
+      hits = o.hits;
+      out.caps += o.capped ? 1 : 0;
+    }
+    V3 pp;
+    if (in.single) {
+      pp = {(double)fx, (double)fy, (double)fz};
+    } else {
+      ux = ux + (fx - x);
+      uy = uy + (fy - y);
+      uz = uz + (fz - z);
+      pp = {(double)ux, (double)uy, (double)uz};
+      fx = k_wrap(fx, G.a);
+      fy = k_wrap(fy, G.b);
+      fz = k_wrap(fz, G.c);
+    }
+    for (int j = 0; j < in.nseq; ++j) out.phase[j] += in.gamma * dot(gfunc(in.seqs[j], dt * i), pp) * dt;
+    int new_slot = slot;
+    if (!in.single && geom) new_slot = k_lookup(G, fx, fy, fz);
+    if (in.relax) {
+      const T y2 = G.t2term[in.perm ? new_slot : slot];
+      const T yy = y2 - t2c;
+      const T t = t2s + yy;
+      t2c = (t - t2s) - yy;
+      t2s = t;
+    }
+    x = fx;
+    y = fy;
+    z = fz;
+    slot = new_slot;
+    if (tr) {
+      const size_t o = (size_t)(i - 1);
+      tr->pos[o * 3 + 0] = (double)x;
+      tr->pos[o * 3 + 1] = (double)y;
+      tr->pos[o * 3 + 2] = (double)z;
+      int rs = slot;
+      if (in.single) rs = (c0_of(G.inst[0], x, y, z) < T(0)) ? 0 : -1;
+      tr->region[o] = (!in.single && rs == G.ecs) ? -1 : rs;
+      tr->hits[o] = hits;
+      tr->words[o] = (int32_t)st.word;
+    }
+  }
+  out.t2factor = in.relax ? ((double)t2s - (double)t2c) : 0.0;
+}
+
+}  // namespace
+
+extern "C" {
+
+void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+  uint32_t c[4] = {ctr[0], ctr[1], ctr[2], ctr[3]};
+  philox(c, key[0], key[1]);
+  std::memcpy(out, c, 16);
+}
+
+void orc_stream_words(uint64_t seed, uint64_t walker, int n, uint32_t *out) {
+  Stream s{seed, walker, 0u};
+  for (int i = 0; i < n; ++i) out[i] = s.next_word();
+}
+
+void orc_sincos_2pi_f32(float u, float *s, float *c) { k_sincos_2pi<float>(u, *s, *c); }
+
+double orc_bvalue(const orc_sequence *q, double gamma) {
+  const double G = q->G, d = q->duration, sp = q->spacing, n = (double)q->num_periods;
+  if (gamma <= 0.0) gamma = kGAMMA;
+  switch (q->kind) {
+    case 0: return G * G * d * d * gamma * gamma * ((2.0 / 3.0) * d + sp);
+    case 1: return gamma * gamma * (1.0 / 4.0) * G * G * d * d * d / (kPI * kPI * n * n);
+    case 2: return gamma * gamma * (3.0 / 4.0) * G * G * d * d * d / (kPI * kPI * n * n);
+    case 3:
+      return gamma * gamma * (1.0 / 4.0) * G * G * d * d * d / (kPI * kPI * n * n) *
+             (1.0 - 1.0 / (8.0 * n));
+    case 4: {
+      const double nu = n / d;
+      const double a1 = (1. - std::pow(-1., 2. * n) + 4. * d * nu) / (4. * nu);
+      return G * G * gamma * gamma * (d / (6. * nu * nu) + sp * (d - a1) * (d - a1));
+    }
+  }
+  return 0.0;
+}
+
+void orc_gradient(const orc_sequence *q, double t, double out[3]) {
+  const V3 g = gfunc(*q, t);
+  out[0] = g.x;
+  out[1] = g.y;
+  out[2] = g.z;
+}
+
+int orc_walk(const orc_lattice *lat, const orc_basis *basis, int nbasis, const orc_sequence *seqs,
+             int nseq, const orc_params *p, int mode, int nthreads, double *sums, orc_trace *trace,
+             int64_t *cap_hits) {
+  if (!p || p->num_walkers < 1 || p->steps < 1 || !(p->timestep > 0.0)) return -1;
+  if (nbasis < 0 || (nbasis > 0 && !basis) || (nseq > 0 && (!seqs || !sums))) return -1;
+  if (!lat && nbasis < 1) return -1;
+  if (mode < 0 || mode > 2) return -1;
+  WalkIn in{lat, basis, nbasis, seqs, nseq, p, p->gamma > 0.0 ? p->gamma : kGAMMA,
+            lat == nullptr, false, false, (p->flags & 4u) != 0};
+  in.relax = !in.single && (p->flags & 1u);
+  in.perm = !in.single && (p->flags & 2u);
+  RefLattice L{};
+  if (!in.single) {
+    L.a = lat->a;
+    L.b = lat->b;
+    L.c = lat->c;
+    L.D = lat->D;
+    L.T2 = lat->T2;
+    for (int k = 0; k < nbasis; ++k) L.B.push_back(RefBasis{&basis[k]});
+  }
+  KGeom<double> G64;
+  KGeom<float> G32;
+  if (mode == ORC_KERN64) k_build(lat, basis, nbasis, p->timestep, in.relax, in.single, G64);
+  if (mode == ORC_KERN32) k_build(lat, basis, nbasis, p->timestep, in.relax, in.single, G32);
+  const int64_t N = p->num_walkers;
+  if (nthreads < 1) nthreads = 1;
+  if ((int64_t)nthreads > N) nthreads = (int)N;
+  std::vector<std::vector<double>> part(nthreads, std::vector<double>((size_t)nseq * 5, 0.0));
+  std::vector<int64_t> caps(nthreads, 0);
+  auto work = [&](int t) {
+    const int64_t w0 = N * t / nthreads, w1 = N * (t + 1) / nthreads;
+    WalkOut out;
+    out.phase.assign(nseq, 0.0);
+    for (int64_t w = w0; w < w1; ++w) {
+      TraceRow row, *tr = nullptr;
+      if (trace && w < trace->ntrace) {
+        const size_t o = (size_t)w * (size_t)(p->steps - 1);
+        row = {trace->init_pos + w * 3, trace->pos + o * 3, trace->region + o, trace->hits + o,
+               trace->words + o};
+        tr = &row;
+      }
+      out.caps = 0;
+      if (mode == ORC_REF64) walk_ref(in, L, w, out, tr);
+      else if (mode == ORC_KERN64) walk_kern<double>(in, G64, w, out, tr);
+      else walk_kern<float>(in, G32, w, out, tr);
+      caps[t] += out.caps;
+      // transformAndSumTwoVectors / transformAndSum (cudaVector.cu:143-172):
+      // cos(phase) * exp(-T2factor) and sin(phase) * exp(-T2factor)
+      const double wgt = in.relax ? std::exp(-out.t2factor) : 1.0;
+      for (int j = 0; j < nseq; ++j) {
+        const double xv = std::cos(out.phase[j]) * wgt, yv = std::sin(out.phase[j]) * wgt;
+        double *s = &part[t][(size_t)j * 5];
+        s[0] += xv;
+        s[1] += yv;
+        s[2] += xv * xv;
+        s[3] += yv * yv;
+        s[4] += xv * yv;
+      }
+    }
+  };
+  if (nthreads == 1) {
+    work(0);
+  } else {
+    std::vector<std::thread> th;
+    for (int t = 0; t < nthreads; ++t) th.emplace_back(work, t);
+    for (auto &x : th) x.join();
+  }
+  for (int j = 0; j < nseq * 5; ++j) {
+    double s = 0.0;
+    for (int t = 0; t < nthreads; ++t) s += part[t][j];
+    sums[j] = s;
+  }
+  if (cap_hits) {
+    int64_t c = 0;
+    for (auto v : caps) c += v;
+    *cap_hits = c;
+  }
+  return 0;
+}
+
+int orc_step(const orc_lattice *lat, const orc_basis *basis, int nbasis, const orc_params *p,
+             int mode, int64_t walker, int i, const double r_in[3], int32_t word, double r_out[3],
+             int32_t *region, int32_t *hits, int32_t *word_out) {
+  if (!p || !lat || i < 1 || mode < 0 || mode > 2) return -1;
+  // A walk of two "steps" whose start is the given state: reuse the walkers
+  // above with a patched stream and start position.
+  const double dt = p->timestep;
+  const bool relax = (p->flags & 1u) != 0, perm = (p->flags & 2u) != 0,
+             reject = (p->flags & 4u) != 0;
+  Stream st{p->seed, (uint64_t)(walker + p->walker_offset), (uint32_t)word};
+  int h = 0;
+  if (mode == ORC_REF64) {
+    RefLattice L{};
+    L.a = lat->a;
+    L.b = lat->b;
+    L.c = lat->c;
+    L.D = lat->D;
+    L.T2 = lat->T2;
+    for (int k = 0; k < nbasis; ++k) L.B.push_back(RefBasis{&basis[k]});
+    V3 r{r_in[0], r_in[1], r_in[2]};
+    V3 ri = r;
+    const double speed = std::sqrt(6.0 * L.getD(r) / dt);
+    const double phi = 2.0 * kPI * st.uniform();
+    const double theta = std::acos(2.0 * st.uniform() - 1);
+    r = r + V3{speed * dt * std::sin(theta) * std::cos(phi), speed * dt * std::sin(theta) * std::sin(phi),
+               speed * dt * std::cos(theta)};
+    if (reject) {
+      if (L.region(ri) != L.region(r)) r = ri;
+    } else {
+      double v = 0.0, acc = 0.0, pm = 0.0;
+      V3 n{0, 0, 0}, rc = ri;
+      bool transmitted = false;
+      const double cur = std::sqrt(6.0 * L.getD(ri) / dt);
+      while (L.check(rc, r, v, n, pm) && transmitted == false) {
+        ++h;
+        const double trs = std::sqrt(6.0 * L.getD(r) / dt);
+        r = (r - rc) * v + rc;
+        const V3 I = r - rc;
+        const double Im = mag(I);
+        acc += Im / (perm ? cur : speed);
+        if (perm && !(st.uniform() > pm * 4.0 / cur)) {
+          r = r + ((I / Im) * trs) * (dt - acc);
+          transmitted = true;
+        } else {
+          rc = r;
+          r = r + ((I - (n * 2.0) * dot(n, I)) * ((perm ? cur : speed) / Im)) * (dt - acc);
+        }
+      }
+    }
+    L.correct(r);
+    r_out[0] = r.x;
+    r_out[1] = r.y;
+    r_out[2] = r.z;
+    *region = L.first_inside(r);
+  } else {
+    auto run = [&](auto tag) {
+      using T = decltype(tag);
+      KGeom<T> G;
+      k_build(lat, basis, nbasis, dt, relax, false, G);
+      T x = (T)r_in[0], y = (T)r_in[1], z = (T)r_in[2];
+      const int slot = G.inst.empty() ? G.ecs : k_lookup(G, x, y, z);
+      const T v = G.speed[slot], Ls = G.step[slot];
+      const T u1 = (T)st.uniform(), u2 = (T)st.uniform();
+      T dx, dy, dz;
+      k_direction(u1, u2, dx, dy, dz);
+      T fx, fy, fz;
+      if (G.inst.empty() || reject) {
+        fx = fmaT(Ls, dx, x);
+        fy = fmaT(Ls, dy, y);
+        fz = fmaT(Ls, dz, z);
+        if (reject && !G.inst.empty() && G.region[k_lookup(G, fx, fy, fz)] != G.region[slot]) {
+          fx = x;
+          fy = y;
+          fz = z;
+        }
+      } else {
+        const KMove<T> o = k_boundary(G, x, y, z, dx, dy, dz, Ls, v, perm, st);
+        fx = o.fx;
+        fy = o.fy;
+        fz = o.fz;
+        h = o.hits;
+      }
+      fx = k_wrap(fx, G.a);
+      fy = k_wrap(fy, G.b);
+      fz = k_wrap(fz, G.c);
+      r_out[0] = (double)fx;
+      r_out[1] = (double)fy;
+      r_out[2] = (double)fz;
+      const int rs = G.inst.empty() ? G.ecs : k_lookup(G, fx, fy, fz);
+      *region = rs == G.ecs ? -1 : rs;
+    };
+    if (mode == ORC_KERN64) run(double(0));
+    else run(float(0));
+  }
+  (void)relax;
+  (void)i;
+  *hits = h;
+  *word_out = (int32_t)st.word;
+  return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,103 @@
+/*
+ * oracle.h -- CPU oracle of the axonexa random-walker phase path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker: it is linked or
+ * loaded by tests/, by __graft_entry__.smoke() and by bench.py's CPU-baseline
+ * arm, and never by the product library (axonexa_gb300/libaxx.so).
+ *
+ * It restates the reference's walk in plain C++ (see oracle.cpp for the
+ * file:line each function follows) in three modes:
+ *   ORC_REF64    the reference's own algorithm and operation order in FP64:
+ *                Lattice with two wrapped copies of every move, the expanded
+ *                quadratic of Cylinder_XY/Sphere::intersect, acos-based step
+ *                directions; pinned bit-for-bit against the reference's own
+ *                headers compiled for the host (oracle/_ref) and the golden
+ *                vectors in tests/golden/.
+ *   ORC_KERN64   the GPU kernel's formulation (periodic ghost instances,
+ *                centre-relative quadratic in the distance parameter, the
+ *                polynomial direction) in FP64.
+ *   ORC_KERN32   the same in FP32 with the kernel's exact operation sequence:
+ *                a trajectory of the GPU kernel is reproduced bit for bit.
+ * In every mode the phases are accumulated per sequence in FP64 exactly as
+ * updateWalkersLatticePhase does (phase += GAMMA*(G(t).r_unbounded)*dt), and
+ * the signal sums are FP64.
+ *
+ * The record layouts are the same plain structs as the product's C ABI, so a
+ * test can hand the same bytes to both.
+ */
+#ifndef AXX_ORACLE_H_
+#define AXX_ORACLE_H_
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct {
+  int32_t type, region;
+  double cx, cy, cz, radius, D, T2, T1, permeability, eps;
+} orc_basis;
+
+typedef struct {
+  double a, b, c, T2, T1, D;
+} orc_lattice;
+
+typedef struct {
+  int32_t kind, num_periods;
+  double G, duration, spacing, gx, gy, gz;
+} orc_sequence;
+
+typedef struct {
+  int64_t num_walkers;
+  int32_t steps, init_mode, init_arg;
+  uint32_t flags;
+  uint64_t seed;
+  double timestep, gamma;
+  int64_t walker_offset;
+} orc_params;
+
+/* Trace of the first ntrace walkers: start position, then after every move
+ * i = 1..steps-1 the wrapped position, the first containing basis (-1 if
+ * none), the boundary hits of the move and the index of the next stream word. */
+typedef struct {
+  int32_t ntrace;
+  double *init_pos;  /* [ntrace*3] */
+  double *pos;       /* [ntrace*(steps-1)*3] */
+  int32_t *region;   /* [ntrace*(steps-1)] */
+  int32_t *hits;
+  int32_t *words;
+} orc_trace;
+
+enum { ORC_REF64 = 0, ORC_KERN64 = 1, ORC_KERN32 = 2 };
+
+/* Philox4x32-10 of one counter/key. */
+void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+/* Words 0..n-1 of the stream of (seed, walker). */
+void orc_stream_words(uint64_t seed, uint64_t walker, int n, uint32_t *out);
+/* sin and cos of 2*pi*u by the kernel's FP32 polynomial (for host checks). */
+void orc_sincos_2pi_f32(float u, float *s, float *c);
+
+/* Signal sums of a lattice walk (lat != NULL) or a single-pore walk
+ * (lat == NULL, walkers start in basis[0]).  sums[5*j..5*j+4] =
+ * (sum x, sum y, sum x^2, sum y^2, sum xy) for sequence j.  Walkers are
+ * split over nthreads host threads (partial sums combined in thread order).
+ * Returns 0, or a negative code for invalid input. */
+int orc_walk(const orc_lattice *lat, const orc_basis *basis, int nbasis,
+             const orc_sequence *seqs, int nseq, const orc_params *p, int mode, int nthreads,
+             double *sums, orc_trace *trace, int64_t *cap_hits);
+
+/* One move i of walker `walker` from the wrapped position r_in with the
+ * stream positioned at word `word`: writes the wrapped end position, the
+ * first containing basis there, the hits and the next word index. */
+int orc_step(const orc_lattice *lat, const orc_basis *basis, int nbasis, const orc_params *p,
+             int mode, int64_t walker, int i, const double r_in[3], int32_t word,
+             double r_out[3], int32_t *region, int32_t *hits, int32_t *word_out);
+
+/* b-value and gradient of a sequence, restating the reference functors. */
+double orc_bvalue(const orc_sequence *q, double gamma);
+void orc_gradient(const orc_sequence *q, double t, double out[3]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

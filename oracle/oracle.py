@@ -1,0 +1,201 @@
+"""ctypes binding of the CPU oracle (liboracle.so) and of the reference's own
+walker compiled for the host (_ref/libaxxref.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+CPU-baseline arm of bench.py, never by the product package.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "liboracle.so")
+REFLIB = os.path.join(HERE, "_ref", "libaxxref.so")
+REF_SRC = "/root/reference"
+
+REF64, KERN64, KERN32 = 0, 1, 2
+REF_VARIANTS = ("spec_imp", "spec_imp_t2", "spec_perm", "spec_perm_t2", "rej", "rej_t2")
+
+
+class Basis(C.Structure):
+    _fields_ = [("type", C.c_int32), ("region", C.c_int32), ("cx", C.c_double),
+                ("cy", C.c_double), ("cz", C.c_double), ("radius", C.c_double),
+                ("D", C.c_double), ("T2", C.c_double), ("T1", C.c_double),
+                ("permeability", C.c_double), ("eps", C.c_double)]
+
+
+class Lattice(C.Structure):
+    _fields_ = [("a", C.c_double), ("b", C.c_double), ("c", C.c_double),
+                ("T2", C.c_double), ("T1", C.c_double), ("D", C.c_double)]
+
+
+class Sequence(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("num_periods", C.c_int32), ("G", C.c_double),
+                ("duration", C.c_double), ("spacing", C.c_double), ("gx", C.c_double),
+                ("gy", C.c_double), ("gz", C.c_double)]
+
+
+class Params(C.Structure):
+    _fields_ = [("num_walkers", C.c_int64), ("steps", C.c_int32), ("init_mode", C.c_int32),
+                ("init_arg", C.c_int32), ("flags", C.c_uint32), ("seed", C.c_uint64),
+                ("timestep", C.c_double), ("gamma", C.c_double), ("walker_offset", C.c_int64)]
+
+
+class Trace(C.Structure):
+    _fields_ = [("ntrace", C.c_int32), ("init_pos", C.POINTER(C.c_double)),
+                ("pos", C.POINTER(C.c_double)), ("region", C.POINTER(C.c_int32)),
+                ("hits", C.POINTER(C.c_int32)), ("words", C.POINTER(C.c_int32))]
+
+
+def build(ref: bool = True) -> None:
+    """Builds liboracle.so, and _ref/libaxxref.so when the reference tree exists."""
+    subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
+    if ref and os.path.isdir(os.path.join(REF_SRC, "src")):
+        subprocess.run(["make", "-s", "-j8", "-C", HERE, "ref", "REF=" + REF_SRC], check=True)
+
+
+_lib = None
+_ref = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build(ref=False)
+        _lib = C.CDLL(LIB)
+        _lib.orc_walk.restype = C.c_int
+        _lib.orc_step.restype = C.c_int
+        _lib.orc_bvalue.restype = C.c_double
+    return _lib
+
+
+def reflib():
+    """The reference's walker, or None when it was not built here."""
+    global _ref
+    if _ref is None and os.path.exists(REFLIB):
+        _ref = C.CDLL(REFLIB)
+    return _ref
+
+
+def _arr(seq, cls):
+    seq = list(seq)
+    a = (cls * max(len(seq), 1))()
+    for i, s in enumerate(seq):
+        a[i] = s
+    return a
+
+
+def make_trace(ntrace: int, steps: int):
+    n = ntrace * max(steps - 1, 0)
+    bufs = dict(init_pos=np.zeros(ntrace * 3), pos=np.zeros(n * 3),
+                region=np.zeros(n, np.int32), hits=np.zeros(n, np.int32),
+                words=np.zeros(n, np.int32))
+    t = Trace(ntrace,
+              bufs["init_pos"].ctypes.data_as(C.POINTER(C.c_double)),
+              bufs["pos"].ctypes.data_as(C.POINTER(C.c_double)),
+              bufs["region"].ctypes.data_as(C.POINTER(C.c_int32)),
+              bufs["hits"].ctypes.data_as(C.POINTER(C.c_int32)),
+              bufs["words"].ctypes.data_as(C.POINTER(C.c_int32)))
+    return t, bufs
+
+
+def _shape_trace(bufs, ntrace, steps):
+    return dict(init_pos=bufs["init_pos"].reshape(ntrace, 3),
+                pos=bufs["pos"].reshape(ntrace, steps - 1, 3),
+                region=bufs["region"].reshape(ntrace, steps - 1),
+                hits=bufs["hits"].reshape(ntrace, steps - 1),
+                words=bufs["words"].reshape(ntrace, steps - 1))
+
+
+def walk(lat, bases, seqs, params, mode=REF64, nthreads=1, ntrace=0):
+    """Runs the oracle.  lat None = single pore.  Returns (sums[M,5], trace|None, caps)."""
+    L = lib()
+    b = _arr(bases, Basis)
+    s = _arr(seqs, Sequence)
+    sums = np.zeros(max(len(seqs), 1) * 5)
+    tr, bufs = (make_trace(ntrace, params.steps) if ntrace else (None, None))
+    caps = C.c_int64(0)
+    rc = L.orc_walk(C.byref(lat) if lat is not None else None, b, len(bases), s, len(seqs),
+                    C.byref(params), mode, nthreads,
+                    sums.ctypes.data_as(C.POINTER(C.c_double)),
+                    C.byref(tr) if tr is not None else None, C.byref(caps))
+    if rc != 0:
+        raise ValueError("orc_walk failed: %d" % rc)
+    return (sums[: len(seqs) * 5].reshape(len(seqs), 5),
+            _shape_trace(bufs, ntrace, params.steps) if ntrace else None, caps.value)
+
+
+def ref_walk(variant, lat, bases, seqs, params, nthreads=1, ntrace=0):
+    """Runs the reference's own walker (compiled here); None if unavailable."""
+    R = reflib()
+    if R is None:
+        return None
+    fn = getattr(R, "ref_walk_" + variant)
+    b = _arr(bases, Basis)
+    s = _arr(seqs, Sequence)
+    sums = np.zeros(max(len(seqs), 1) * 5)
+    tr, bufs = (make_trace(ntrace, params.steps) if ntrace else (None, None))
+    rc = fn(C.byref(lat) if lat is not None else None, b, len(bases), s, len(seqs),
+            C.byref(params), nthreads, sums.ctypes.data_as(C.POINTER(C.c_double)),
+            C.byref(tr) if tr is not None else None)
+    if rc != 0:
+        raise ValueError("ref_walk_%s failed: %d" % (variant, rc))
+    return (sums[: len(seqs) * 5].reshape(len(seqs), 5),
+            _shape_trace(bufs, ntrace, params.steps) if ntrace else None)
+
+
+def variant_for(flags: int) -> str:
+    spec = not (flags & 4)
+    t2 = bool(flags & 1)
+    perm = bool(flags & 2)
+    if spec:
+        return ("spec_perm" if perm else "spec_imp") + ("_t2" if t2 else "")
+    return "rej_t2" if t2 else "rej"
+
+
+def stream_words(seed: int, walker: int, n: int) -> np.ndarray:
+    out = np.zeros(n, np.uint32)
+    lib().orc_stream_words(C.c_uint64(seed), C.c_uint64(walker), n,
+                           out.ctypes.data_as(C.POINTER(C.c_uint32)))
+    return out
+
+
+def philox(ctr, key) -> np.ndarray:
+    c = (C.c_uint32 * 4)(*ctr)
+    k = (C.c_uint32 * 2)(*key)
+    o = (C.c_uint32 * 4)()
+    lib().orc_philox4x32_10(c, k, o)
+    return np.array(list(o), np.uint32)
+
+
+def sincos_2pi_f32(u: float):
+    s, c = C.c_float(), C.c_float()
+    lib().orc_sincos_2pi_f32(C.c_float(u), C.byref(s), C.byref(c))
+    return s.value, c.value
+
+
+def step(lat, bases, params, mode, walker, i, r_in, word):
+    b = _arr(bases, Basis)
+    rin = (C.c_double * 3)(*r_in)
+    rout = (C.c_double * 3)()
+    reg, hits, wout = C.c_int32(), C.c_int32(), C.c_int32()
+    rc = lib().orc_step(C.byref(lat), b, len(bases), C.byref(params), mode, C.c_int64(walker), i,
+                        rin, C.c_int32(word), rout, C.byref(reg), C.byref(hits), C.byref(wout))
+    if rc != 0:
+        raise ValueError("orc_step failed")
+    return np.array(list(rout)), reg.value, hits.value, wout.value
+
+
+def bvalue(seq, gamma=0.0) -> float:
+    return lib().orc_bvalue(C.byref(seq), C.c_double(gamma))
+
+
+def gradient(seq, t: float):
+    out = (C.c_double * 3)()
+    lib().orc_gradient(C.byref(seq), C.c_double(t), out)
+    return np.array(list(out))

@@ -1,0 +1,271 @@
+"""GPU walker against the CPU oracle (run on a GB300).
+
+Parity levels (the oracle is pinned to the reference's own walker by
+tests/test_oracle_pin.py):
+  1. trajectory, bit for bit: the GPU trace equals the oracle's FP32 kernel
+     formulation (positions, region indices, hit counts, stream words);
+  2. per move against the reference order in FP64: starting each move from
+     the GPU's own state, region indices and hit counts are identical and the
+     end position agrees within 1e-5 relative (near-tie moves, where an FP32
+     rounding of the start flips the FP64 outcome, are counted separately and
+     must stay rare);
+  3. signals: within 3 standard errors of the oracle's FP64 reference-order
+     walk, and within 1e-5*N of the FP32 formulation (same trajectories).
+"""
+import math
+
+import numpy as np
+import pytest
+
+import cases
+
+pytestmark = pytest.mark.gpu
+
+
+def to_product(lat, bases, seqs=()):
+    import axonexa_gb300 as A
+    L = None
+    if lat is not None:
+        L = A.Lattice(lat.a, lat.b, lat.c, lat.T2, lat.T1, lat.D, len(bases))
+    B = []
+    for b in bases:
+        if b.type == 0:
+            B.append(A.Cylinder_XY(b.cx, b.cy, b.radius, b.T2, b.T1, b.D, b.region,
+                                   b.permeability, b.eps))
+        else:
+            B.append(A.Sphere(b.cx, b.cy, b.cz, b.radius, b.T2, b.T1, b.D, b.region,
+                              b.permeability, b.eps))
+    cls = {0: A.RectGrad, 1: A.CosGFunc, 2: A.SinGFunc, 3: A.ApodCosGFunc, 4: A.SWOGSEFunc}
+    S = []
+    for q in seqs:
+        if q.kind == 0:
+            s = A.RectGrad(q.G, q.duration, q.spacing)
+            s.ghat = A.Vector3(q.gx, q.gy, q.gz)
+        else:
+            s = cls[q.kind](q.G, q.duration, q.spacing, q.num_periods, (q.gx, q.gy, q.gz))
+        S.append(s)
+    return L, B, S
+
+
+def flag_kw(flags):
+    return dict(specular=not (flags & 4), relaxation=bool(flags & 1), permeable=bool(flags & 2))
+
+
+LATTICE_CASES = [
+    ("free", lambda: (cases.lattice_box(50.0), []), 0, 0.005),
+    ("cyl", lambda: cases.one_cylinder(), 1, 0.002),
+    ("cyl_perm", lambda: cases.one_cylinder(D_in=1.7e-6, kappa=5e-5), 3, 0.002),
+    ("cyl_reject", lambda: cases.one_cylinder(), 5, 0.002),
+    ("hex_perm", lambda: cases.hex_cylinders(kappa=2e-5), 3, 0.001),
+    ("spheres", lambda: cases.sphere_lattice(), 1, 0.002),
+]
+
+
+@pytest.mark.parametrize("name,make,flags,dt", LATTICE_CASES, ids=[c[0] for c in LATTICE_CASES])
+def test_trace_bit_exact_lattice(dev, orc, name, make, flags, dt):
+    import axonexa_gb300 as A
+    lat, bases = make()
+    L, B, _ = to_product(lat, bases)
+    n, steps, seed = 64, 1500, 4321
+    g = A.trace_lattice(L, B, n, steps, dt, seed, device=dev, **flag_kw(flags))
+    p = cases.params(n, steps, seed, dt=dt, flags=flags)
+    _, o, _ = orc.walk(lat, bases, [], p, orc.KERN32, ntrace=n)
+    np.testing.assert_array_equal(g["init_pos"].astype(np.float64), o["init_pos"])
+    for k in ("region", "hits", "words"):
+        np.testing.assert_array_equal(g[k], o[k], err_msg=k)
+    np.testing.assert_array_equal(g["pos"].astype(np.float64), o["pos"])
+    if bases:
+        assert o["hits"].sum() > 0  # the case exercises the boundary code
+
+
+@pytest.mark.parametrize("sph", [0, 1])
+def test_trace_bit_exact_single_pore(dev, orc, sph):
+    import axonexa_gb300 as A
+    from oracle import oracle as O
+    b = O.Basis(sph, 1, 0.0 if sph else 0.001, 0.0 if sph else -0.002, 0.0, 0.004, cases.D2,
+                0, 0, 0, 1e-14)
+    _, B, _ = to_product(None, [b])
+    n, steps, seed = 64, 1500, 99
+    g = A.trace_single(B[0], n, steps, 0.002, seed, device=dev)
+    _, o, _ = orc.walk(None, [b], [], cases.params(n, steps, seed), orc.KERN32, ntrace=n)
+    np.testing.assert_array_equal(g["init_pos"].astype(np.float64), o["init_pos"])
+    for k in ("region", "hits", "words"):
+        np.testing.assert_array_equal(g[k], o[k], err_msg=k)
+    np.testing.assert_array_equal(g["pos"].astype(np.float64), o["pos"])
+    assert o["hits"].sum() > 0
+
+
+def test_init_modes_bit_exact(dev, orc):
+    import axonexa_gb300 as A
+    lat, bases = cases.hex_cylinders()
+    L, B, _ = to_product(lat, bases)
+    for mode, arg in ((1, 0), (1, 3), (2, 1)):
+        g = A.trace_lattice(L, B, 64, 50, 0.001, 7, init_mode=mode, init_arg=arg, device=dev)
+        p = cases.params(64, 50, 7, dt=0.001, init_mode=mode, init_arg=arg)
+        _, o, _ = orc.walk(lat, bases, [], p, orc.KERN32, ntrace=64)
+        np.testing.assert_array_equal(g["init_pos"].astype(np.float64), o["init_pos"])
+        np.testing.assert_array_equal(g["words"], o["words"])
+
+
+def _tie(orc, lat, bases, p, w, i, start, word, want_region, want_hits):
+    """True if some FP32-size nudge of the start makes the FP64 reference move
+    reproduce the GPU's events (the move sits on a rounding tie)."""
+    ulp = np.spacing(np.abs(np.asarray(start, np.float32))).astype(np.float64) * 4
+    for sx in (-1, 1):
+        for sy in (-1, 1):
+            for sz in (-1, 1):
+                s = np.asarray(start) + ulp * np.array([sx, sy, sz])
+                _, reg, hits, _ = orc.step(lat, bases, p, orc.REF64, w, i, s, word)
+                if reg == want_region and hits == want_hits:
+                    return True
+    return False
+
+
+@pytest.mark.parametrize("name,make,flags,dt", LATTICE_CASES[1:], ids=[c[0] for c in LATTICE_CASES[1:]])
+def test_per_move_against_reference_fp64(dev, orc, name, make, flags, dt):
+    import axonexa_gb300 as A
+    lat, bases = make()
+    L, B, _ = to_product(lat, bases)
+    n, steps, seed = 48, 2000, 2024
+    g = A.trace_lattice(L, B, n, steps, dt, seed, device=dev, **flag_kw(flags))
+    p = cases.params(n, steps, seed, dt=dt, flags=flags)
+    scale = max(lat.a, lat.b, lat.c)
+    worst, ties, moves = 0.0, 0, 0
+    for w in range(n):
+        prev = g["init_pos"][w].astype(np.float64)
+        word = 4  # words 1..3 start the walk
+        for i in range(1, steps):
+            moves += 1
+            r_out, reg, hits, wout = orc.step(lat, bases, p, orc.REF64, w, i, prev, word)
+            gpos = g["pos"][w, i - 1].astype(np.float64)
+            if reg != g["region"][w, i - 1] or hits != g["hits"][w, i - 1] or \
+                    wout != g["words"][w, i - 1]:
+                assert _tie(orc, lat, bases, p, w, i, prev, word, g["region"][w, i - 1],
+                            g["hits"][w, i - 1]), (w, i, reg, hits, g["region"][w, i - 1],
+                                                   g["hits"][w, i - 1])
+                ties += 1
+            else:
+                d = np.abs(r_out - gpos)
+                d = np.minimum(d, np.array([lat.a, lat.b, lat.c]) - d)
+                worst = max(worst, float(d.max()) / scale)
+            prev = gpos
+            word = int(g["words"][w, i - 1])
+    assert worst < 1e-5, worst
+    assert ties <= max(2, moves // 10000), ties
+
+
+SIGNAL_CASES = [
+    ("cyl_t2", lambda: cases.one_cylinder(), 1, 0.002, 2500),
+    ("cyl_perm_t2", lambda: cases.one_cylinder(D_in=1.7e-6, kappa=5e-5), 3, 0.002, 2500),
+    ("hex_perm_t2", lambda: cases.hex_cylinders(kappa=2e-5), 3, 0.001, 3000),
+    ("spheres", lambda: cases.sphere_lattice(), 1, 0.002, 2000),
+    ("free", lambda: (cases.lattice_box(50.0), []), 0, 0.005, 2000),
+]
+
+
+@pytest.mark.parametrize("name,make,flags,dt,steps", SIGNAL_CASES, ids=[c[0] for c in SIGNAL_CASES])
+def test_signals_against_oracle(dev, orc, name, make, flags, dt, steps):
+    import os
+    import axonexa_gb300 as A
+    lat, bases = make()
+    seqs = cases.seq_mix() + [cases.cos_ogse(50, 2, kind=4, delta=10.0, Delta=25.0)]
+    L, B, S = to_product(lat, bases, seqs)
+    n, seed = 4096, 777
+    res = A.run_lattice(L, B, S, n, steps, dt, seed, device=dev, **flag_kw(flags))
+    p = cases.params(n, steps, seed, dt=dt, flags=flags)
+    nt = os.cpu_count() or 1
+    ref, _, _ = orc.walk(lat, bases, seqs, p, orc.REF64, nthreads=nt)
+    k32, _, _ = orc.walk(lat, bases, seqs, p, orc.KERN32, nthreads=nt)
+    for j in range(len(seqs)):
+        for c, v in ((0, res.mx[j]), (1, res.my[j])):
+            var = ref[j, 2 + c] / n - (ref[j, c] / n) ** 2
+            se = math.sqrt(max(var, 0.0) / n) + 1e-12
+            assert abs(v / n - ref[j, c] / n) <= 3 * se + 1e-9, (j, c, v / n, ref[j, c] / n, se)
+            # same trajectories as the FP32 formulation: tight agreement
+            assert abs(v - k32[j, c]) <= 2e-5 * n, (j, c, v, k32[j, c])
+
+
+def test_free_diffusion_exp_minus_bD_full_size(dev):
+    """Config: empty periodic 50 um box, 65,536 walkers, dt 5 us, 6,000 steps,
+    PGSE delta 5 ms, Delta 20 ms, 16 G values 0-300 mT/m: S = exp(-b D)."""
+    import axonexa_gb300 as A
+    s = 0.05
+    L = A.Lattice(s, s, s, 0.0, 0.0, 2e-6, 0)
+    G = np.linspace(0, 300, 16) * 1e-6
+    S = [A.RectGrad(g, 5.0, 15.0) for g in G]
+    n = 65536
+    res = A.run_lattice(L, [], S, n, 6000, 0.005, 1234, device=dev)
+    b = np.array([q.getB() for q in S])
+    want = np.exp(-b * 2e-6)
+    se = res.stderr
+    assert np.all(np.abs(res.signal - want) <= 3 * se + 2e-4), (res.signal, want, se)
+
+
+def test_full_size_cylinder_properties(dev):
+    """Config: one impermeable cylinder r 5 um in a 12 um periodic cell,
+    1,048,576 walkers, dt 2 us, PGSE delta 10 / Delta 40 (25,000 steps), 32 G
+    values 0-200 mT/m plus cosine OGSE at 50/100/200 Hz (delta 20 ms)."""
+    import axonexa_gb300 as A
+    c, r = 0.012, 0.005
+    L = A.Lattice(c, c, c, 60.0, 0.0, 2e-6, 1)
+    B = [A.Cylinder_XY(c / 2, c / 2, r, 80.0, 0.0, 2e-6, 1, 0.0)]
+    G = np.linspace(0, 200, 32) * 1e-6
+    S = [A.RectGrad(g, 10.0, 30.0) for g in G] + \
+        [A.CosGFunc(100e-6, 20.0, 20.0, n) for n in (1, 2, 4)]
+    n, steps = 1 << 20, 25000
+    r1 = A.run_lattice(L, B, S, n, steps, 0.002, 1234, relaxation=True, device=dev)
+    r2 = A.run_lattice(L, B, S, n, steps, 0.002, 1234, relaxation=True, device=dev)
+    np.testing.assert_array_equal(r1.mx, r2.mx)  # deterministic reduction
+    assert r1.cap_hits == 0
+    # G = 0: volume-weighted T2 decay (f = pi r^2 / c^2)
+    f = math.pi * r * r / (c * c)
+    TE = (steps - 1) * 0.002
+    want = f * math.exp(-TE / 80.0) + (1 - f) * math.exp(-TE / 60.0)
+    assert abs(r1.signal[0] - want) < 4 * r1.stderr[0] + 2e-4, (r1.signal[0], want)
+    # PGSE signal falls monotonically with G
+    assert np.all(np.diff(r1.signal[:32]) < 1e-3)
+    # sharding by walker ranges reproduces the whole (streams keyed by walker id)
+    half = n // 2
+    a = A.run_lattice(L, B, S, half, steps, 0.002, 1234, relaxation=True, device=dev)
+    b = A.run_lattice(L, B, S, half, steps, 0.002, 1234, relaxation=True, device=dev,
+                      walker_offset=half)
+    np.testing.assert_allclose(a.mx + b.mx, r1.mx, rtol=0, atol=1e-8 * n)
+
+
+def test_edge_cases(dev, orc):
+    import axonexa_gb300 as A
+    from axonexa_gb300 import _native as N
+    lat, bases = cases.one_cylinder()
+    L, B, S = to_product(lat, bases, cases.seq_mix())
+    for n in (1, 31, 33, 129):
+        res = A.run_lattice(L, B, S, n, 200, 0.002, 5, relaxation=True, device=dev)
+        p = cases.params(n, 200, 5, flags=1)
+        k32, _, _ = orc.walk(lat, bases, cases.seq_mix(), p, orc.KERN32)
+        assert np.all(np.abs(res.mx - k32[:, 0]) <= 1e-5 * n)
+    # a single step makes no move: S = cos(gamma G(0).r dt) terms only
+    res = A.run_lattice(L, B, S, 100, 1, 0.002, 5, device=dev)
+    assert res.walker_steps == 0
+    # no sequences
+    res = A.run_lattice(L, B, [], 100, 50, 0.002, 5, device=dev)
+    assert len(res.mx) == 0
+    # 256 sequences (the per-launch maximum)
+    many = [A.RectGrad(g * 1e-6, 10.0, 30.0) for g in np.linspace(0, 200, 256)]
+    res = A.run_lattice(L, B, many, 256, 100, 0.002, 5, device=dev)
+    assert res.mx.shape == (256,) and np.all(np.isfinite(res.mx))
+    # invalid inputs are reported, not crashed on
+    with pytest.raises(N.AxxError):
+        A.run_lattice(L, B, S, 0, 10, 0.002, 5, device=dev)
+    with pytest.raises(N.AxxError):
+        A.run_lattice(L, B, S, 10, 10, -1.0, 5, device=dev)
+    bad = A.Cylinder_XY(0.006, 0.006, float("nan"), 80, 0, 2e-6, 1, 0)
+    with pytest.raises(N.AxxError):
+        A.run_lattice(L, [bad], S, 10, 10, 0.002, 5, device=dev)
+    with pytest.raises(N.AxxError):
+        A.run_lattice(L, B, many + many, 10, 10, 0.002, 5, device=dev)
+
+
+def test_philox_device_stream(dev, orc):
+    import axonexa_gb300 as A
+    for seed, w in ((1234, 0), (1234, 65535), (2 ** 40 + 3, 12345678901)):
+        np.testing.assert_array_equal(A.philox_words(seed, w, 64, device=dev),
+                                      orc.stream_words(seed, w, 64))

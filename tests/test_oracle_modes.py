@@ -1,0 +1,56 @@
+"""The oracle's kernel formulation against its reference formulation, and
+the walk against closed-form signals."""
+import math
+
+import numpy as np
+import pytest
+
+import cases
+
+
+def _events(t):
+    return np.stack([t["region"], t["hits"], t["words"]], -1)
+
+
+@pytest.mark.parametrize("flags", [0, 1, 3, 5])
+def test_kernel_formulation_reproduces_reference_events(orc, flags):
+    lat, cyl = cases.one_cylinder(D_in=1.7e-6, kappa=3e-5)
+    p = cases.params(128, 2000, 21, flags=flags)
+    _, tr, _ = orc.walk(lat, cyl, [], p, orc.REF64, ntrace=128)
+    _, tk, _ = orc.walk(lat, cyl, [], p, orc.KERN64, ntrace=128)
+    np.testing.assert_array_equal(_events(tr), _events(tk))
+    d = np.abs(tr["pos"] - tk["pos"])
+    d = np.minimum(d, lat.a - d)  # periodic images are the same point
+    assert d.max() < 1e-12 * lat.a
+
+
+def test_kernel_formulation_packs(orc):
+    for lat, bases in (cases.hex_cylinders(kappa=2e-5), cases.sphere_lattice()):
+        p = cases.params(64, 1000, 3, flags=3 if bases[0].type == 0 else 1)
+        _, tr, _ = orc.walk(lat, bases, [], p, orc.REF64, ntrace=64)
+        _, tk, _ = orc.walk(lat, bases, [], p, orc.KERN64, ntrace=64)
+        np.testing.assert_array_equal(_events(tr), _events(tk))
+
+
+def test_free_diffusion_matches_exp_minus_bD(orc):
+    # empty periodic box, PGSE along x: S = exp(-b D) within 3 standard errors
+    lat = cases.lattice_box(50.0)
+    seqs = [cases.pgse(g, delta=5.0, Delta=20.0) for g in (0, 100, 200, 300)]
+    n = 4096
+    p = cases.params(n, 6000, 1234, dt=0.005)
+    sums, _, _ = orc.walk(lat, [], seqs, p, orc.KERN64, nthreads=8)
+    for q, s in zip(seqs, sums):
+        S = math.hypot(s[0], s[1]) / n
+        b = orc.bvalue(q)
+        se = math.sqrt(max(s[2] / n - (s[0] / n) ** 2, 0) / n) + 1e-4
+        assert abs(S - math.exp(-b * cases.D2)) < 4 * se + 2e-3, (S, math.exp(-b * cases.D2))
+
+
+def test_partition_invariance(orc):
+    # walker ranges are independent streams: shards add up to the whole
+    lat, cyl = cases.one_cylinder()
+    seqs = cases.seq_mix()
+    whole, _, _ = orc.walk(lat, cyl, seqs, cases.params(60, 300, 7, flags=1), orc.KERN32)
+    a, _, _ = orc.walk(lat, cyl, seqs, cases.params(25, 300, 7, flags=1), orc.KERN32)
+    b, _, _ = orc.walk(lat, cyl, seqs, cases.params(35, 300, 7, flags=1, offset=25), orc.KERN32)
+    np.testing.assert_allclose(a + b, whole, rtol=1e-12, atol=1e-12)
