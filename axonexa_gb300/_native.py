@@ -30,7 +30,7 @@ class AxxError(RuntimeError):
 
 
 class ReflectionCapError(AxxError):
-    """Some moves needed more than 16 boundary hits; results were still written."""
+    """Some moves needed more than 1024 boundary hits; results were still written."""
 
 
 class Basis(C.Structure):

@@ -332,7 +332,7 @@ axx_status read_results(axx_plan *pl, double *mx, double *my, axx_stats *stats) 
     if (!std::isfinite(h[m * 5]) || !std::isfinite(h[m * 5 + 1]))
       return fail(ctx, AXX_ERR_NUMERIC, "non-finite signal");
   if (cnt[AXX_CNT_CAP])
-    return fail(ctx, AXX_ERR_REFLECTION_CAP, "some moves hit the reflection cap of 16");
+    return fail(ctx, AXX_ERR_REFLECTION_CAP, "some moves hit the reflection cap of 1024");
   return AXX_OK;
 }
 

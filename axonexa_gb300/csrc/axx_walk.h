@@ -19,7 +19,7 @@
 
 #define AXX_KMAX 16          // channel accumulators per pass
 #define AXX_MAX_SEQ 256      // sequences per pass (epilogue smem bound)
-#define AXX_REFL_CAP 16      // boundary hits per move before the cap flag
+#define AXX_REFL_CAP 1024    // boundary hits per move before the cap flag
 #define AXX_BLOCK 128        // threads per block of the walk kernels
 #define AXX_INIT_TRIES 100000
 

@@ -204,6 +204,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the one-shot C-ABI timing")
+    ap.add_argument("--walkers", type=int, default=N_WALKERS,
+                    help="walkers per acquisition (smaller cases for profiling)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -222,10 +225,11 @@ def main():
     dev = A.Device(local)
     L = N.lib()
     lat, cyl, acqs = workload_records(A)
-    offset = rank * N_WALKERS  # each rank walks its own walker ids (weak scaling)
+    nw = args.walkers
+    offset = rank * nw  # each rank walks its own walker ids (weak scaling)
     plans = []
     for seqs, steps in acqs:
-        p = A.acquisition._params(N_WALKERS, steps, SEED, DT, A.acquisition.run_flags(
+        p = A.acquisition._params(nw, steps, SEED, DT, A.acquisition.run_flags(
             relaxation=True), offset=offset)
         h = C.c_void_p()
         N.check(L.axx_plan_lattice(dev.h, C.byref(lat.record()),
@@ -234,7 +238,7 @@ def main():
                                    len(seqs), C.byref(p), C.byref(h)), dev.h)
         plans.append((h, len(seqs), steps, p))
     flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
-    ws = walker_steps_per_bench_step()
+    ws = walker_steps_per_bench_step(nw)
 
     def step_resident():
         for h, _, _, _ in plans:
@@ -283,15 +287,15 @@ def main():
     barrier(world)
     e2e_ms = 0.0
     h2d = d2h = 0
-    for _ in range(args.steps):
+    for _ in range(0 if args.no_e2e else args.steps):
         flush_l2(flush)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for seqs, steps in acqs:
-            r = A.run_lattice(lat, cyl, seqs, N_WALKERS, steps, DT, SEED, relaxation=True,
+            r = A.run_lattice(lat, cyl, seqs, nw, steps, DT, SEED, relaxation=True,
                               walker_offset=offset, device=dev)
         e2e_ms += (time.perf_counter() - t0) * 1e3
-    e2e_step = max_over_ranks(e2e_ms / args.steps, world)
+    e2e_step = max_over_ranks(e2e_ms / args.steps, world) if not args.no_e2e else float("nan")
     for seqs, steps in acqs:
         # tables uploaded per call: instances, cell lists, slots, waveforms, coefficients
         h2d += 32 * 2 + 8 + 2 + 16 * 2 + 4 * 2 + 4 * steps * (1 if len(seqs) > 3 else 3) + \
@@ -310,7 +314,7 @@ def main():
         N.check(L.axx_plan_info(h, C.byref(ch), None, None, None), dev.h)
         F.append(18 + 6 + 7 * ch.value + 1 + 23 * 1 + 20 * hp)
     moves = [PGSE_STEPS - 1, OGSE_STEPS - 1]
-    ops = N_WALKERS * sum(f * m for f, m in zip(F, moves))
+    ops = nw * sum(f * m for f, m in zip(F, moves))
     peak = C.c_double()
     N.check(L.axx_fp32_fma_peak(dev.h, C.byref(peak)), dev.h)
     achieved = ops / (t_step * 1e-3)
@@ -323,7 +327,7 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "restricted_cylinder_pgse32_ogse3", "walkers": N_WALKERS,
+        "config": {"workload": "restricted_cylinder_pgse32_ogse3", "walkers": nw,
                    "cell_um": 12.0, "radius_um": 5.0, "dt_us": 2.0,
                    "moves": moves, "sequences": [32, 3], "seed": SEED,
                    "parallelism": "replicas (walker ranges)" if world > 1 else "single GPU",

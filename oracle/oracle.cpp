@@ -342,7 +342,7 @@ KMove<T> k_boundary(const KGeom<T> &G, T sx, T sy, T sz, T dx, T dy, T dz, T L, 
       }
     }
     if (bk < 0) break;
-    if (o.hits == 16) {
+    if (o.hits == 1024) {  // the kernel's reflection cap
       o.capped = true;
       o.fx = sx;
       o.fy = sy;

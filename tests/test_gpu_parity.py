@@ -74,7 +74,7 @@ def test_trace_bit_exact_lattice(dev, orc, name, make, flags, dt):
     for k in ("region", "hits", "words"):
         np.testing.assert_array_equal(g[k], o[k], err_msg=k)
     np.testing.assert_array_equal(g["pos"].astype(np.float64), o["pos"])
-    if bases:
+    if bases and not (flags & 4):
         assert o["hits"].sum() > 0  # the case exercises the boundary code
 
 
