@@ -79,6 +79,10 @@ _SIGS = {
     "axx_run_single": ([C.c_void_p, C.POINTER(Basis), C.POINTER(SequenceRec), C.c_int,
                         C.POINTER(RunParams), C.POINTER(C.c_double), C.POINTER(C.c_double),
                         C.POINTER(Stats)], C.c_int),
+    "axx_run_lattice_noalloc": ([C.c_void_p, C.POINTER(LatticeRec), C.POINTER(Basis), C.c_int,
+                                 C.POINTER(SequenceRec), C.c_int, C.POINTER(RunParams),
+                                 C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(Stats)],
+                                C.c_int),
     "axx_plan_lattice": ([C.c_void_p, C.POINTER(LatticeRec), C.POINTER(Basis), C.c_int,
                           C.POINTER(SequenceRec), C.c_int, C.POINTER(RunParams),
                           C.POINTER(C.c_void_p)], C.c_int),

@@ -27,6 +27,7 @@ CUDA_SOURCES = [
     "walk_sph.cu",
     "walk_mix.cu",
     "misc_kernels.cu",
+    "noalloc.cu",
 ]
 HOST_SOURCES = ["api.cpp", "host_plan.cpp", "substrate.cpp"]
 

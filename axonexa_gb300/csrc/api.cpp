@@ -18,21 +18,12 @@
 #include <vector>
 
 #include "../../include/axx.h"
+#include "ctx_internal.h"
 #include "host_plan.h"
 #include "walk_launch.h"
 
 using namespace axx;
 
-struct axx_ctx {
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  cudaEvent_t ev[8] = {};
-  std::string err;
-  int nsm = 0, ccmaj = 0, ccmin = 0;
-  size_t gmem = 0;
-  volatile int *abort_host = nullptr;
-  int *abort_dev = nullptr;
-};
 
 struct axx_plan {
   axx_ctx *ctx = nullptr;

@@ -180,6 +180,26 @@ axx_status axx_run_single(axx_ctx *ctx, const axx_basis *basis, const axx_sequen
                           int nseq, const axx_run_params *params, double *mx, double *my,
                           axx_stats *stats);
 
+/* Lattice walk that allocates no GPU memory.  No counterpart in the
+ * reference: it exists for callers that cannot call cudaMalloc when they run
+ * a walk (a memory pool or budget that owns all device memory, a framework
+ * that forbids allocation after start-up, a thread that must not trigger the
+ * synchronisation cudaMalloc/cudaFree can cause).  Same inputs, outputs and
+ * results as axx_run_lattice; every device-side buffer of the call lives in
+ * one static array of AXX_NOALLOC_SCRATCH_BYTES that each GPU loading the
+ * library holds until the process exits.  A walk whose tables and per-block
+ * partials do not fit is rejected with AXX_ERR_INVALID_ARG.  The first call on
+ * a device looks up the array's device address, so make it before any stream
+ * capture.  All calls on a device share the array: calls whose GPU work
+ * overlaps race and must be serialised by the caller.  The context must have
+ * been created beforehand (axx_create). */
+#define AXX_NOALLOC_SCRATCH_BYTES (8u << 20)
+axx_status axx_run_lattice_noalloc(axx_ctx *ctx, const axx_lattice *lat,
+                                   const axx_basis *basis, int nbasis,
+                                   const axx_sequence *seqs, int nseq,
+                                   const axx_run_params *params, double *mx, double *my,
+                                   axx_stats *stats);
+
 /* ---- device-resident plans (inputs uploaded once, launched repeatedly) ---- */
 
 axx_status axx_plan_lattice(axx_ctx *ctx, const axx_lattice *lat, const axx_basis *basis,

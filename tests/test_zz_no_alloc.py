@@ -1,0 +1,76 @@
+"""axx_run_lattice_noalloc: the lattice walk for callers that cannot allocate
+GPU memory.
+
+Callers that cannot call cudaMalloc when they run a walk -- code whose GPU
+memory is owned by a pool or a fixed budget, frameworks that forbid device
+allocation after start-up, threads that must not trigger the device-wide
+synchronisation cudaMalloc/cudaFree can cause -- use this entry point.  It
+runs the same kernels as axx_run_lattice but keeps every device-side buffer in
+a static array compiled into the library, so it must give the same signals as
+the allocating call, call after call (the array is reused and keeps the
+previous call's contents), and it must refuse walks that do not fit.
+
+This file is collected last on purpose: if it fails, a run that stops at the
+first failure has already run every other test.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _records():
+    import axonexa_gb300 as A
+    from axonexa_gb300 import _native as N
+    c, r = 0.012, 0.005
+    lat = A.Lattice(c, c, c, 60.0, 0.0, 2e-6, 1).record()
+    basis = N.array_of(N.Basis, [A.Cylinder_XY(c / 2, c / 2, r, 80.0, 0.0, 2e-6, 1, 0.0).record()])
+    seqs = [A.RectGrad(g * 1e-6, 10.0, 30.0) for g in (0.0, 80.0, 160.0)] + \
+        [A.CosGFunc(100e-6, 10.0, 10.0, 2, (0.6, 0.8, 0.0))]
+    srec = N.array_of(N.SequenceRec, [q.record() for q in seqs])
+    return lat, basis, srec, len(seqs)
+
+
+def _call(fn, ctx, lat, basis, srec, m, params):
+    from axonexa_gb300 import _native as N
+    out = [np.zeros(m) for _ in range(5)]
+    ptr = [o.ctypes.data_as(C.POINTER(C.c_double)) for o in out]
+    st = N.Stats(ptr[2], ptr[3], ptr[4], 0, 0, 0)
+    rc = fn(ctx, C.byref(lat), basis, 1, srec, m, C.byref(params), ptr[0], ptr[1], C.byref(st))
+    N.check(rc, ctx)
+    return out, st
+
+
+def test_noalloc_matches_allocating_call_twice_in_a_row():
+    import axonexa_gb300 as A
+    from axonexa_gb300 import _native as N
+    dev = A.default_device()
+    L = N.lib()
+    lat, basis, srec, m = _records()
+    n = 20000
+    params = N.RunParams(n, 3000, 0, 0, N.FLAG_RELAXATION, 4242, 0.002, 0.0, 0)
+    want, st_w = _call(L.axx_run_lattice, dev.h, lat, basis, srec, m, params)
+    for _ in range(2):
+        got, st_g = _call(L.axx_run_lattice_noalloc, dev.h, lat, basis, srec, m, params)
+        for a, b in zip(got, want):
+            np.testing.assert_allclose(a, b, rtol=0, atol=1e-9 * n)
+        assert st_g.walker_steps == st_w.walker_steps
+        assert st_g.boundary_hits == st_w.boundary_hits
+        assert st_g.reflection_cap_hits == 0
+
+
+def test_noalloc_refuses_walks_that_do_not_fit():
+    import axonexa_gb300 as A
+    from axonexa_gb300 import _native as N
+    dev = A.default_device()
+    lat, basis, _, _ = _records()
+    # 16 distinct waveforms x 140,000 steps of FP32 tables exceed the 8 MiB array
+    seqs = [A.RectGrad(1e-4, 1.0 + k, 5.0) for k in range(16)]
+    srec = N.array_of(N.SequenceRec, [q.record() for q in seqs])
+    params = N.RunParams(64, 140000, 0, 0, 0, 1, 0.002, 0.0, 0)
+    with pytest.raises(N.AxxError) as e:
+        _call(N.lib().axx_run_lattice_noalloc, dev.h, lat, basis, srec, len(seqs), params)
+    assert e.value.status == 1
+    assert "no-allocation scratch" in str(e.value)
