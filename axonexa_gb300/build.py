@@ -23,13 +23,15 @@ LIB = os.path.join(HERE, "libaxx.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_SOURCES = [
     "walk_free.cu",
-    "walk_cyl.cu",
-    "walk_sph.cu",
+    "walk_cyl_lat.cu",
+    "walk_cyl_single.cu",
+    "walk_sph_lat.cu",
+    "walk_sph_single.cu",
     "walk_mix.cu",
     "misc_kernels.cu",
     "noalloc.cu",
 ]
-HOST_SOURCES = ["api.cpp", "host_plan.cpp", "substrate.cpp"]
+HOST_SOURCES = ["api.cpp", "host_plan.cpp", "plan_layout.cpp", "substrate.cpp"]
 
 
 def nvcc() -> str:

@@ -20,6 +20,7 @@
 #include "../../include/axx.h"
 #include "ctx_internal.h"
 #include "host_plan.h"
+#include "plan_layout.h"
 #include "walk_launch.h"
 
 using namespace axx;
@@ -28,8 +29,9 @@ using namespace axx;
 struct axx_plan {
   axx_ctx *ctx = nullptr;
   WalkParams P{};
-  int geom = 0, kmax = 1, grid = 0, M = 0, K = 0, n_inst = 0;
+  int geom = 0, km = 0, kmax = 1, grid = 0, M = 0, K = 0, n_inst = 0;
   size_t smem = 0;
+  size_t upload_bytes = 0;
   void *arena = nullptr;
   double *out = nullptr;  // [M*5]
   unsigned long long *counters = nullptr;
@@ -58,22 +60,6 @@ axx_status cuda_fail(axx_ctx *ctx, cudaError_t e, const char *where) {
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
-cudaError_t launch_geom(int geom, int kmax, bool trace, const WalkParams &P, const TraceParams &T,
-                        int grid, size_t smem, cudaStream_t s) {
-  switch (geom) {
-    case AXX_GEOM_FREE: return launch_walk_free(kmax, trace, P, T, grid, smem, s);
-    case AXX_GEOM_CYL: return launch_walk_cyl(kmax, trace, P, T, grid, smem, s);
-    case AXX_GEOM_SPH: return launch_walk_sph(kmax, trace, P, T, grid, smem, s);
-    default: return launch_walk_mix(kmax, trace, P, T, grid, smem, s);
-  }
-}
-
-int kmax_for(int K) {
-  int k = 1;
-  while (k < K) k <<= 1;
-  return k;
-}
-
 axx_status check_params(axx_ctx *ctx, const axx_run_params *p) {
   if (!p) return fail(ctx, AXX_ERR_INVALID_ARG, "params is NULL");
   if (p->num_walkers < 1) return fail(ctx, AXX_ERR_INVALID_ARG, "num_walkers must be >= 1");
@@ -90,141 +76,53 @@ axx_status check_params(axx_ctx *ctx, const axx_run_params *p) {
 
 // Builds the plan's device arena and kernel parameters.
 axx_status build_plan(axx_ctx *ctx, const GeomPlan &g, const SeqPlan &sq, int M,
-                      const axx_run_params *p, int mode, float sspeed, float sstep,
-                      int init_inst, int init_sph, double init_R, double init_cx,
-                      double init_cy, double init_cz, axx_plan **out) {
-  const int K = (int)sq.channels.size();
-  if (K > AXX_KMAX)
+                      const axx_run_params *p, int mode, const axx_basis *basis, int nbasis,
+                      const double cell[3], axx_plan **out) {
+  KernelTables kt;
+  std::string err = make_kernel_tables(g, sq, M, p->steps, mode, p->flags, kt);
+  if (!err.empty()) return fail(ctx, AXX_ERR_UNSUPPORTED, err);
+  InitSpec init;
+  err = init_spec(g, basis, nbasis, mode, p, init);
+  if (!err.empty()) return fail(ctx, AXX_ERR_INVALID_ARG, err);
+  const size_t smem = walk_smem_bytes(g, M);
+  if (smem > AXX_SMEM_MAX)
     return fail(ctx, AXX_ERR_UNSUPPORTED,
-                "more than 16 phase channels (distinct waveform x direction) in one plan");
+                "substrate tables and sequence sums exceed the shared-memory budget (" +
+                    std::to_string(smem) + " bytes)");
+  const int occ = occupancy_walk(g.geom, kt.km, kt.kmax, false, smem);
+  if (occ <= 0) return fail(ctx, AXX_ERR_CUDA, "walk kernel cannot be resident (occupancy 0)");
   auto *pl = new axx_plan();
   pl->ctx = ctx;
   pl->geom = g.geom;
-  pl->K = K;
+  pl->km = kt.km;
+  pl->kmax = kt.kmax;
+  pl->K = kt.K;
   pl->M = M;
-  pl->kmax = kmax_for(std::max(K, 1));
   pl->n_inst = (int)g.geo.size();
-  const int steps = p->steps;
-  const int ncell = (int)g.cstart.size() - 1;
-  // grid: resident capacity of the device, at most one warp per 32 walkers
-  const size_t wsum_bytes = (size_t)(AXX_BLOCK / 32) * M * 5 * sizeof(double);
-  const size_t geo_bytes = (size_t)pl->n_inst * 32 + (size_t)(ncell + 1) * 4 +
-                           ((g.clist.size() * 2 + 15) & ~(size_t)15);
-  const bool smem_geom = g.geom != AXX_GEOM_FREE && geo_bytes <= 96 * 1024;
-  // the geometry staging area starts right after the per-warp sums (160*M
-  // bytes, a multiple of 16)
-  pl->smem = wsum_bytes + (smem_geom ? geo_bytes : 0);
-  const int occ = occupancy_walk(g.geom, pl->kmax, false, pl->smem);
-  if (occ <= 0) {
-    delete pl;
-    return fail(ctx, AXX_ERR_CUDA, "walk kernel cannot be resident (occupancy 0)");
-  }
+  pl->smem = smem;
+  // grid: the device's resident capacity, at most one warp per 32 walkers
   const long long ntask = (p->num_walkers + 31) / 32;
   const long long want = (ntask + AXX_BLOCK / 32 - 1) / (AXX_BLOCK / 32);
   pl->grid = (int)std::min<long long>(want, (long long)occ * ctx->nsm);
-  // arena
-  size_t off = 0;
-  auto take = [&](size_t bytes) {
-    size_t o = off;
-    off = align256(off + std::max<size_t>(bytes, 1));
-    return o;
-  };
-  const size_t o_geo = take(g.geo.size() * sizeof(float4));
-  const size_t o_aux = take(g.aux.size() * sizeof(float4));
-  const size_t o_cs = take(g.cstart.size() * 4);
-  const size_t o_cl = take(g.clist.size() * 2);
-  const size_t o_slot = take(g.slot_tab.size() * sizeof(float4));
-  const size_t o_reg = take(g.slot_region.size() * 4);
-  const size_t o_wave = take(sq.wave.size() * 4);
-  const size_t o_coef = take(sq.coef.size() * 8);
-  const size_t o_part = take((size_t)pl->grid * M * 5 * 8);
-  const size_t o_out = take((size_t)M * 5 * 8);
-  const size_t o_cnt = take(AXX_CNT_N * 8);
-  cudaError_t e = cudaMalloc(&pl->arena, off);
+  const ArenaLayout L = arena_layout(g, kt, M);
+  pl->upload_bytes = L.upload;
+  cudaError_t e = cudaMalloc(&pl->arena, L.fixed + L.per_block * pl->grid);
   if (e != cudaSuccess) {
     delete pl;
     return cuda_fail(ctx, e, "cudaMalloc(plan arena)");
   }
   char *base = (char *)pl->arena;
-  auto up = [&](size_t o, const void *src, size_t bytes) {
-    if (bytes == 0) return cudaSuccess;
-    return cudaMemcpyAsync(base + o, src, bytes, cudaMemcpyHostToDevice, ctx->stream);
-  };
-  cudaError_t es[8] = {
-      up(o_geo, g.geo.data(), g.geo.size() * sizeof(float4)),
-      up(o_aux, g.aux.data(), g.aux.size() * sizeof(float4)),
-      up(o_cs, g.cstart.data(), g.cstart.size() * 4),
-      up(o_cl, g.clist.data(), g.clist.size() * 2),
-      up(o_slot, g.slot_tab.data(), g.slot_tab.size() * sizeof(float4)),
-      up(o_reg, g.slot_region.data(), g.slot_region.size() * 4),
-      up(o_wave, sq.wave.data(), sq.wave.size() * 4),
-      up(o_coef, sq.coef.data(), sq.coef.size() * 8)};
-  for (cudaError_t x : es)
-    if (x != cudaSuccess) {
-      cudaFree(pl->arena);
-      delete pl;
-      return cuda_fail(ctx, x, "cudaMemcpyAsync(plan tables)");
-    }
-  e = cudaStreamSynchronize(ctx->stream);
+  e = upload_tables(base, L, g, kt, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) {
     cudaFree(pl->arena);
     delete pl;
-    return cuda_fail(ctx, e, "cudaStreamSynchronize(plan upload)");
+    return cuda_fail(ctx, e, "uploading the plan tables");
   }
-  WalkParams &P = pl->P;
-  std::memset(&P, 0, sizeof(P));
-  P.mode = mode;
-  P.n_inst = pl->n_inst;
-  P.n_list = (int)g.clist.size();
-  P.ncell = ncell;
-  P.smem_geom = smem_geom ? 1 : 0;
-  P.inst_geo = (const float4 *)(base + o_geo);
-  P.inst_aux = (const float4 *)(base + o_aux);
-  P.cell_start = (const uint32_t *)(base + o_cs);
-  P.cell_list = (const uint16_t *)(base + o_cl);
-  P.gx = g.gx;
-  P.gy = g.gy;
-  P.gz = g.gz;
-  P.inv_hx = g.inv_hx;
-  P.inv_hy = g.inv_hy;
-  P.inv_hz = g.inv_hz;
-  P.slot_tab = (const float4 *)(base + o_slot);
-  P.slot_region = (const int *)(base + o_reg);
-  P.ecs_slot = g.ecs_slot;
-  P.steps = steps;
-  P.n_walkers = p->num_walkers;
-  P.walker_offset = p->walker_offset;
-  P.seed_lo = (uint32_t)p->seed;
-  P.seed_hi = (uint32_t)(p->seed >> 32);
-  P.flags = p->flags;
-  P.init_mode = p->init_mode;
-  P.init_arg = p->init_arg;
-  P.init_quirk = (mode == AXX_MODE_SINGLE) && !(p->flags & AXX_FLAG_FIX_INIT_QUIRK);
-  P.init_inst = init_inst;
-  P.init_sph = init_sph;
-  P.init_R = (float)init_R;
-  P.init_cx = (float)init_cx;
-  P.init_cy = (float)init_cy;
-  P.init_cz = (float)init_cz;
-  P.single_speed = sspeed;
-  P.single_step = sstep;
-  P.K = K;
-  P.wave = (const float *)(base + o_wave);
-  for (int c = 0; c < K; ++c) {
-    P.ch_wave[c] = sq.channels[c].wave;
-    for (int k = 0; k < 3; ++k) P.ch_p[c][k] = sq.channels[c].p[k];
-  }
-  P.M = M;
-  P.coef = (const double *)(base + o_coef);
-  P.partials = (double *)(base + o_part);
-  P.counters = (unsigned long long *)(base + o_cnt);
-  P.abort_flag = ctx->abort_dev;
-  pl->out = (double *)(base + o_out);
-  pl->counters = P.counters;
-  pl->walker_steps = p->num_walkers * (long long)(steps - 1);
-  if (mode == AXX_MODE_LATTICE) {
-    P.a = 0.f;  // set by the caller
-  }
+  fill_walk_params(pl->P, base, L, g, kt, p, mode, M, init, cell, ctx->abort_dev);
+  pl->out = (double *)(base + L.o_out);
+  pl->counters = pl->P.counters;
+  pl->walker_steps = p->num_walkers * (long long)(p->steps - 1);
   *out = pl;
   return AXX_OK;
 }
@@ -241,33 +139,8 @@ axx_status make_lattice_plan(axx_ctx *ctx, const axx_lattice *lat, const axx_bas
   SeqPlan sq;
   e = plan_sequences(seqs, nseq, params->steps, params->timestep, gamma, sq);
   if (!e.empty()) return fail(ctx, AXX_ERR_INVALID_ARG, e);
-  int init_inst = 0, init_sph = 0;
-  double R = 0, cx = 0, cy = 0, cz = 0;
-  if (params->init_mode == AXX_INIT_IN_BASIS) {
-    if (params->init_arg < 0 || params->init_arg >= nbasis)
-      return fail(ctx, AXX_ERR_INVALID_ARG, "init_arg must name a basis for AXX_INIT_IN_BASIS");
-    for (int n = 0; n < (int)g.aux.size(); ++n) {
-      int slot;
-      std::memcpy(&slot, &g.aux[n].z, 4);
-      if (slot == params->init_arg) {
-        init_inst = n;
-        break;
-      }
-    }
-    const axx_basis &b = basis[params->init_arg];
-    init_sph = b.type == AXX_PRIM_SPHERE;
-    R = b.radius;
-    cx = b.cx;
-    cy = b.cy;
-    cz = b.cz;
-  }
-  s = build_plan(ctx, g, sq, nseq, params, AXX_MODE_LATTICE, 0.f, 0.f, init_inst, init_sph, R,
-                 cx, cy, cz, out);
-  if (s != AXX_OK) return s;
-  (*out)->P.a = (float)lat->a;
-  (*out)->P.b = (float)lat->b;
-  (*out)->P.c = (float)lat->c;
-  return AXX_OK;
+  const double cell[3] = {lat->a, lat->b, lat->c};
+  return build_plan(ctx, g, sq, nseq, params, AXX_MODE_LATTICE, basis, nbasis, cell, out);
 }
 
 axx_status make_single_plan(axx_ctx *ctx, const axx_basis *basis, const axx_sequence *seqs,
@@ -285,12 +158,8 @@ axx_status make_single_plan(axx_ctx *ctx, const axx_basis *basis, const axx_sequ
   SeqPlan sq;
   e = plan_sequences(seqs, nseq, params->steps, params->timestep, gamma, sq);
   if (!e.empty()) return fail(ctx, AXX_ERR_INVALID_ARG, e);
-  s = build_plan(ctx, g, sq, nseq, params, AXX_MODE_SINGLE, sp, st, 0,
-                 basis->type == AXX_PRIM_SPHERE, basis->radius, basis->cx, basis->cy, basis->cz,
-                 out);
-  if (s != AXX_OK) return s;
-  (*out)->P.a = (*out)->P.b = (*out)->P.c = 1.0f;
-  return AXX_OK;
+  const double cell[3] = {1.0, 1.0, 1.0};
+  return build_plan(ctx, g, sq, nseq, params, AXX_MODE_SINGLE, basis, 1, cell, out);
 }
 
 axx_status read_results(axx_plan *pl, double *mx, double *my, axx_stats *stats) {
@@ -434,7 +303,8 @@ axx_status axx_plan_launch(axx_plan *pl) {
   *ctx->abort_host = 0;
   AXX_CUDA(ctx, cudaMemsetAsync(pl->counters, 0, AXX_CNT_N * 8, ctx->stream));
   TraceParams T{};
-  AXX_CUDA(ctx, launch_geom(pl->geom, pl->kmax, false, pl->P, T, pl->grid, pl->smem, ctx->stream));
+  AXX_CUDA(ctx, launch_walk(pl->geom, pl->km, pl->kmax, false, pl->P, T, pl->grid, pl->smem,
+                            ctx->stream));
   AXX_CUDA(ctx, launch_reduce_partials(pl->P.partials, pl->grid, pl->M * 5, pl->out, ctx->stream));
   pl->launched = true;
   return AXX_OK;
@@ -574,7 +444,8 @@ static axx_status run_trace(axx_ctx *ctx, axx_plan *pl, int ntrace, float *init_
   T.words = (int32_t *)b;
   cudaError_t e = cudaMemsetAsync(pl->counters, 0, AXX_CNT_N * 8, ctx->stream);
   const int grid = (ntrace + AXX_BLOCK - 1) / AXX_BLOCK;
-  if (e == cudaSuccess) e = launch_geom(pl->geom, 1, true, pl->P, T, grid, pl->smem, ctx->stream);
+  if (e == cudaSuccess)
+    e = launch_walk(pl->geom, pl->km, 1, true, pl->P, T, grid, pl->smem, ctx->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   if (e == cudaSuccess && init_pos) e = cudaMemcpy(init_pos, T.init_pos, ntrace * 12, cudaMemcpyDeviceToHost);
   if (e == cudaSuccess && pos) e = cudaMemcpy(pos, T.pos, nrec * 12, cudaMemcpyDeviceToHost);

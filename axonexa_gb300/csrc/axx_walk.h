@@ -10,9 +10,10 @@
 //                      cell dilated by the longest step, in ascending basis order
 //   slot_tab[nbasis+1] float4 (speed, step length, dt/T2, 4*kappa); the last
 //                      slot is the extracellular space
-//   wave[W*steps]      FP32 unit waveforms s_w(i*dt) of the distinct sequences
-//   coef[M*K]          FP64 gamma*dt*G_m*(g_m . p_c): phase of sequence m from
-//                      the K channel accumulators
+//   wave_il[steps*KMAX] FP32 unit waveform of each phase channel, step-major
+//                      (one row of KMAX values per step; padded channels 0)
+//   coef[M*KMAX]       FP64 gamma*dt*G_m*alpha_mc: phase of sequence m from
+//                      the channel accumulators (0 for padded channels)
 //   partials[grid*M*5] FP64 per-block sums (x, y, x^2, y^2, xy), scratch
 #pragma once
 #include <stdint.h>
@@ -23,7 +24,17 @@
 #define AXX_BLOCK 128        // threads per block of the walk kernels
 #define AXX_INIT_TRIES 100000
 
+#define AXX_MIN_BLOCKS 6      // resident blocks per SM the register budget targets
+#define AXX_SMEM_MAX (200 * 1024)
+
 enum { AXX_MODE_LATTICE = 0, AXX_MODE_SINGLE = 1 };
+// walk modes (template parameter of the kernels)
+enum { AXX_KM_LAT_IMP = 0,     // lattice, specular, impermeable
+       AXX_KM_LAT_PERM = 1,    // lattice, specular, permeable
+       AXX_KM_LAT_REJ = 2,     // lattice, simple rejection
+       AXX_KM_SINGLE = 3,      // single pore, specular
+       AXX_KM_SINGLE_REJ = 4,  // single pore, simple rejection
+       AXX_KM_N = 5 };
 enum { AXX_GEOM_FREE = 0, AXX_GEOM_CYL = 1, AXX_GEOM_SPH = 2, AXX_GEOM_MIX = 3 };
 
 // counters[] slots
@@ -33,10 +44,11 @@ enum { AXX_CNT_CAP = 0, AXX_CNT_INIT_FAIL = 1, AXX_CNT_ABORTED = 2, AXX_CNT_HITS
 struct WalkParams {
   float a, b, c;  // periodic cell
   int mode;       // AXX_MODE_*
+  int km;         // AXX_KM_*
   int n_inst;
+  int n_slot;
   int n_list;
   int ncell;
-  int smem_geom;  // 1: stage instances and cell lists in shared memory
   const float4 *inst_geo;
   const float4 *inst_aux;
   const uint32_t *cell_start;
@@ -44,6 +56,7 @@ struct WalkParams {
   int gx, gy, gz;
   float inv_hx, inv_hy, inv_hz;
   const float4 *slot_tab;
+  const int *slot_region;     // region id of each slot (0 for the extracellular slot)
   int ecs_slot;
   int steps;
   long long n_walkers;
@@ -55,14 +68,11 @@ struct WalkParams {
   int init_inst;              // instance used by AXX_INIT_IN_BASIS and the single pore
   int init_sph;
   float init_R, init_cx, init_cy, init_cz;
-  const int *slot_region;     // region id of each slot (0 for the extracellular slot)
-  float single_speed, single_step;  // single pore: speed and step of basis 0
-  int K;
-  const float *wave;
-  int ch_wave[AXX_KMAX];
-  float ch_p[AXX_KMAX][3];
+  int K, kmax;                // channels in use, channel capacity (padded)
+  const float *wave_il;       // [steps][kmax]
+  float ch_p[AXX_KMAX][3];    // channel projections (0 for padded channels)
   int M;
-  const double *coef;
+  const double *coef;         // [M][kmax]
   double *partials;
   unsigned long long *counters;
   const volatile int *abort_flag;  // host-mapped; checked every 1024 moves

@@ -1,0 +1,25 @@
+// walk_cyl_lat.cu -- walk kernel instantiations: geometry class AXX_GEOM_CYL, walk modes 0 1 2.
+#include "walk_instances.cuh"
+
+namespace axx {
+
+cudaError_t launch_walk_cyl_lat(int km, int kmax, bool trace, const WalkParams &P,
+                           const TraceParams &T, int grid, size_t smem, cudaStream_t s) {
+  switch (km) {
+    case 0: return walk_launch_km<AXX_GEOM_CYL, 0>(kmax, trace, P, T, grid, smem, s);
+    case 1: return walk_launch_km<AXX_GEOM_CYL, 1>(kmax, trace, P, T, grid, smem, s);
+    case 2: return walk_launch_km<AXX_GEOM_CYL, 2>(kmax, trace, P, T, grid, smem, s);
+  }
+  return cudaErrorInvalidValue;
+}
+
+int occupancy_walk_cyl_lat(int km, int kmax, bool trace, size_t smem) {
+  switch (km) {
+    case 0: return walk_occ_km<AXX_GEOM_CYL, 0>(kmax, trace, smem);
+    case 1: return walk_occ_km<AXX_GEOM_CYL, 1>(kmax, trace, smem);
+    case 2: return walk_occ_km<AXX_GEOM_CYL, 2>(kmax, trace, smem);
+  }
+  return 0;
+}
+
+}  // namespace axx

@@ -1,0 +1,63 @@
+// walk_instances.cuh -- launch and occupancy helpers for the instantiations
+// of walk_kernel; each walk_*.cu translation unit instantiates one geometry
+// class and a subset of walk modes, so the variants compile in parallel.
+#pragma once
+#include "walk_kernel.cuh"
+#include "walk_launch.h"
+
+namespace axx {
+
+template <int GEOM, int KMAX, int KM, bool TRACE>
+static cudaError_t walk_go(const WalkParams &P, const TraceParams &T, int grid, size_t smem,
+                           cudaStream_t s) {
+  auto fn = walk_kernel<GEOM, KMAX, KM, TRACE>;
+  if (smem > 48 * 1024) {
+    const cudaError_t e =
+        cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  fn<<<grid, AXX_BLOCK, smem, s>>>(P, T);
+  return cudaGetLastError();
+}
+
+template <int GEOM, int KMAX, int KM, bool TRACE>
+static int walk_occ(size_t smem) {
+  auto fn = walk_kernel<GEOM, KMAX, KM, TRACE>;
+  if (smem > 48 * 1024 &&
+      cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+          cudaSuccess)
+    return 0;
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, AXX_BLOCK, smem) != cudaSuccess)
+    return 0;
+  return n;
+}
+
+template <int GEOM, int KM>
+static cudaError_t walk_launch_km(int kmax, bool trace, const WalkParams &P,
+                                  const TraceParams &T, int grid, size_t smem, cudaStream_t s) {
+  if (trace) return walk_go<GEOM, 1, KM, true>(P, T, grid, smem, s);
+  switch (kmax) {
+    case 1: return walk_go<GEOM, 1, KM, false>(P, T, grid, smem, s);
+    case 2: return walk_go<GEOM, 2, KM, false>(P, T, grid, smem, s);
+    case 4: return walk_go<GEOM, 4, KM, false>(P, T, grid, smem, s);
+    case 8: return walk_go<GEOM, 8, KM, false>(P, T, grid, smem, s);
+    case 16: return walk_go<GEOM, 16, KM, false>(P, T, grid, smem, s);
+  }
+  return cudaErrorInvalidValue;
+}
+
+template <int GEOM, int KM>
+static int walk_occ_km(int kmax, bool trace, size_t smem) {
+  if (trace) return walk_occ<GEOM, 1, KM, true>(smem);
+  switch (kmax) {
+    case 1: return walk_occ<GEOM, 1, KM, false>(smem);
+    case 2: return walk_occ<GEOM, 2, KM, false>(smem);
+    case 4: return walk_occ<GEOM, 4, KM, false>(smem);
+    case 8: return walk_occ<GEOM, 8, KM, false>(smem);
+    case 16: return walk_occ<GEOM, 16, KM, false>(smem);
+  }
+  return 0;
+}
+
+}  // namespace axx

@@ -17,12 +17,12 @@
 //  1. start position from the stream (Lattice::initializeUniformly,
 //     lattice.cuh:31-37; initializeInRegion :46-58; Basis::randUnif;
 //     single pore: Basis::unifRand on a copy of the stream);
-//  2. phase channel c starts at s_w(0) (p_c . r);
+//  2. phase channel c starts at s_c(0) (p_c . r);
 //  3. moves i = 1..steps-1: v, L from the region at r (Lattice::getD,
 //     lattice.cuh:118-132); direction from two uniforms; boundary handling
 //     (boundaryCheckImpermeable / boundaryCheckPermeable / boundaryNormal,
 //     boundaryCheck.cuh:2-113, or simple rejection, kernelLattice.cuh:73-77);
-//     r_unb += r - ri; channel c += s_w(i) (p_c . r_unb) with Kahan
+//     r_unb += r - ri; channel c += s_c(i) (p_c . r_unb) with Kahan
 //     compensation; T2 sum += dt/T2(region) (kernelLattice.cuh:87-96, with
 //     the reference's permeable weighting that always sees accumtime = 0);
 //     periodic wrap (Lattice::correctBoundary, lattice.cuh:60-88).
@@ -39,9 +39,13 @@
 // Periodicity: every basis and each periodic ghost that can be reached from
 // the cell within one step is an instance; all tests of one move use the
 // instance list of the grid cell that holds the move's start.
+//
+// Specialisation: the walk mode (KM: lattice specular impermeable / permeable
+// / rejection, single pore specular / rejection), the geometry class and the
+// channel capacity are template parameters, so a move carries no runtime mode
+// branches; padded channels carry zero waveforms and coefficients.
 #pragma once
 #include <cuda_runtime.h>
-#include <math_constants.h>
 #include "axx_rng.cuh"
 #include "axx_walk.h"
 
@@ -49,20 +53,35 @@ namespace axx {
 
 #define AXX_INF __int_as_float(0x7f800000)
 
-struct GeoView {
+// Geometry, slot tables and cell lists, staged in shared memory.
+struct SmemView {
   const float4 *geo;
   const float4 *aux;
+  const float4 *slot;
   const uint32_t *cstart;
+  const int *region;
   const uint16_t *clist;
 };
 
+// Grid cell of an in-cell point: floor(x*inv) as round-to-nearest of
+// x*inv - 1/2, done by adding 1.5*2^23 (where the FP32 spacing is 1) and
+// reading the integer from the mantissa.  A point within rounding of a grid
+// line may land in either neighbouring cell, which is safe because every
+// cell list covers the cell dilated by one step.
+__device__ __forceinline__ int cell_index(float x, float inv, int n) {
+  const float t = fma_f(x, inv, -0.5f);
+  const float f = t + 12582912.0f;
+  const int i = __float_as_int(f) - 0x4B400000;
+  return min(max(i, 0), n - 1);
+}
+
+template <int GEOM>
 __device__ __forceinline__ int cell_of(const WalkParams &P, float x, float y, float z) {
-  int ix = (int)(x * P.inv_hx);
-  int iy = (int)(y * P.inv_hy);
-  int iz = (int)(z * P.inv_hz);
-  ix = min(max(ix, 0), P.gx - 1);
-  iy = min(max(iy, 0), P.gy - 1);
-  iz = min(max(iz, 0), P.gz - 1);
+  if (P.ncell == 1) return 0;
+  const int ix = cell_index(x, P.inv_hx, P.gx);
+  const int iy = cell_index(y, P.inv_hy, P.gy);
+  if (GEOM == AXX_GEOM_CYL) return iy * P.gx + ix;
+  const int iz = cell_index(z, P.inv_hz, P.gz);
   return (iz * P.gy + iy) * P.gx + ix;
 }
 
@@ -89,22 +108,14 @@ __device__ __forceinline__ float c0_of(const float4 &g, bool sph, float x, float
 // First instance (ascending basis order) of list [b, e) that contains the
 // point; its slot, or the extracellular slot.
 template <int GEOM>
-__device__ __forceinline__ int lookup_list(const GeoView &G, uint32_t b, uint32_t e, int ecs,
+__device__ __forceinline__ int lookup_list(const SmemView &S, uint32_t b, uint32_t e, int ecs,
                                            float x, float y, float z) {
   for (uint32_t j = b; j < e; ++j) {
-    const int k = G.clist[j];
-    const float4 aux = G.aux[k];
-    if (c0_of(G.geo[k], is_sphere<GEOM>(aux), x, y, z) < 0.0f) return aux_slot(aux);
+    const int k = S.clist[j];
+    const float4 aux = S.aux[k];
+    if (c0_of(S.geo[k], is_sphere<GEOM>(aux), x, y, z) < 0.0f) return aux_slot(aux);
   }
   return ecs;
-}
-
-template <int GEOM>
-__device__ __forceinline__ int lookup_slot(const WalkParams &P, const GeoView &G, float x,
-                                           float y, float z) {
-  if (GEOM == AXX_GEOM_FREE) return P.ecs_slot;
-  const int cell = cell_of(P, x, y, z);
-  return lookup_list<GEOM>(G, G.cstart[cell], G.cstart[cell + 1], P.ecs_slot, x, y, z);
 }
 
 // Distance to the first boundary of one instance along the segment
@@ -127,21 +138,20 @@ __device__ __forceinline__ float seg_hit(const float4 &g, float eps, bool sph, b
     c1 = fma_f(ex, ex, fma_f(ey, ey, g.w));
   }
   if (on_surface) c0 = 0.0f;
+  // cheap rejections: both ends inside; outside or on the surface and moving
+  // away; outside with the closest approach beyond the end
+  if (c0 < 0.0f && c1 < 0.0f) return AXX_INF;
+  if (c0 >= 0.0f && (bh >= 0.0f || (c0 > 0.0f && c1 > 0.0f && fma_f(aa, rem, bh) <= 0.0f)))
+    return AXX_INF;
   float s;
   if (c0 < 0.0f) {  // inside: the exit root
-    if (c1 < 0.0f) return AXX_INF;
-    const float disc = fma_f(bh, bh, -(aa * c0));
-    const float sq = sqrt_f(disc);
+    const float sq = sqrt_f(fma_f(bh, bh, -(aa * c0)));
     s = (bh <= 0.0f) ? div_f(sq - bh, aa) : div_f(-c0, bh + sq);
   } else if (c0 > 0.0f) {  // outside: the entry root
-    if (bh >= 0.0f) return AXX_INF;
-    if (c1 > 0.0f && fma_f(aa, rem, bh) <= 0.0f) return AXX_INF;
     const float disc = fma_f(bh, bh, -(aa * c0));
     if (disc <= 0.0f) return AXX_INF;
-    const float sq = sqrt_f(disc);
-    s = div_f(c0, sq - bh);
+    s = div_f(c0, sqrt_f(disc) - bh);
   } else {  // on the surface: the far root
-    if (bh >= 0.0f) return AXX_INF;
     s = div_f(-2.0f * bh, aa);
   }
   if (!(s > 0.0f && s < rem && s >= eps)) return AXX_INF;
@@ -156,11 +166,11 @@ struct MoveOut {
 
 // Specular boundary handling of one move from (sx, sy, sz) with unit
 // direction d and length L, using the instance list [b, e).
-template <int GEOM>
-__device__ __forceinline__ MoveOut boundary_move(const WalkParams &P, const GeoView &G,
-                                                 uint32_t b, uint32_t e, float sx, float sy,
-                                                 float sz, float dx, float dy, float dz, float L,
-                                                 float v, bool perm, Stream &st) {
+template <int GEOM, bool PERM>
+__device__ __forceinline__ MoveOut boundary_move(const SmemView &S, uint32_t b, uint32_t e,
+                                                 int ecs, float sx, float sy, float sz,
+                                                 float dx, float dy, float dz, float L, float v,
+                                                 Stream &st) {
   MoveOut o;
   o.hits = 0;
   o.capped = false;
@@ -172,10 +182,10 @@ __device__ __forceinline__ MoveOut boundary_move(const WalkParams &P, const GeoV
     float best = AXX_INF;
     int bk = -1;
     for (uint32_t j = b; j < e; ++j) {
-      const int k = G.clist[j];
-      const float4 aux = G.aux[k];
+      const int k = S.clist[j];
+      const float4 aux = S.aux[k];
       const bool sph = is_sphere<GEOM>(aux);
-      const float s = seg_hit(G.geo[k], aux.y, sph, k == last, sx, sy, sz, dx, dy, dz,
+      const float s = seg_hit(S.geo[k], aux.y, sph, k == last, sx, sy, sz, dx, dy, dz,
                               sph ? aa_s : aa_c, rem);
       if (s < best) {
         best = s;
@@ -194,15 +204,15 @@ __device__ __forceinline__ MoveOut boundary_move(const WalkParams &P, const GeoV
     const float hx = fma_f(best, dx, sx), hy = fma_f(best, dy, sy), hz = fma_f(best, dz, sz);
     const float rem_before = rem;
     rem = rem - best;
-    const float4 aux = G.aux[bk];
-    if (perm) {
+    const float4 aux = S.aux[bk];
+    if (PERM) {
       const float u = st.next();
-      const float ptr = div_f(P.slot_tab[aux_slot(aux)].w, v);
+      const float ptr = div_f(S.slot[aux_slot(aux)].w, v);
       if (!(u > ptr)) {  // transmitted: continue with the speed of the far side
         const float tx = fma_f(rem_before, dx, sx), ty = fma_f(rem_before, dy, sy),
                     tz = fma_f(rem_before, dz, sz);
-        const int ts = lookup_list<GEOM>(G, b, e, P.ecs_slot, tx, ty, tz);
-        const float vn = P.slot_tab[ts].x;
+        const int ts = lookup_list<GEOM>(S, b, e, ecs, tx, ty, tz);
+        const float vn = S.slot[ts].x;
         const float remt = div_f(rem * vn, v);
         o.fx = fma_f(remt, dx, hx);
         o.fy = fma_f(remt, dy, hy);
@@ -210,7 +220,7 @@ __device__ __forceinline__ MoveOut boundary_move(const WalkParams &P, const GeoV
         return o;
       }
     }
-    const float4 g = G.geo[bk];
+    const float4 g = S.geo[bk];
     const bool sph = is_sphere<GEOM>(aux);
     const float nx = (hx - g.x) * aux.x, ny = (hy - g.y) * aux.x;
     const float nz = sph ? (hz - g.z) * aux.x : 0.0f;
@@ -244,16 +254,17 @@ __device__ __forceinline__ float wrap1(float x, float a) {
 }
 
 // Start position.  Returns false if a rejection loop ran out of tries.
-template <int GEOM>
-__device__ __forceinline__ bool init_position(const WalkParams &P, const GeoView &G,
+template <int GEOM, int KM>
+__device__ __forceinline__ bool init_position(const WalkParams &P, const SmemView &S,
                                               Stream &st, float &x, float &y, float &z) {
-  if (P.mode == AXX_MODE_SINGLE) {
+  constexpr bool single = KM >= AXX_KM_SINGLE;
+  if (single) {
     // Basis::unifRand (cylinderXY.cuh:45-55, Sphere.cuh:55-63).  The sphere's
     // box is centred on the sphere (the reference omits the centre, which
     // only agrees for a sphere at the origin); its retries draw z, y, x, the
     // order in which the compiled reference evaluates the three draws passed
     // as Vector3 constructor arguments.
-    const float4 g = G.geo[P.init_inst];
+    const float4 g = S.geo[P.init_inst];
     const bool sph = P.init_sph != 0;
     x = fma_f(fma_f(2.0f, st.next(), -1.0f), P.init_R, P.init_cx);
     y = fma_f(fma_f(2.0f, st.next(), -1.0f), P.init_R, P.init_cy);
@@ -272,138 +283,136 @@ __device__ __forceinline__ bool init_position(const WalkParams &P, const GeoView
       }
     }
     return false;
-  }
-  if (P.init_mode == 2) {
-    // Basis::randUnif (cylinderXY.cuh:176-183, Sphere.cuh:384-391): the three
-    // draws are Vector3 constructor arguments, consumed z, y, x; a cylinder's
-    // centre has z = 0.
-    const float4 g = G.geo[P.init_inst];
-    const bool sph = P.init_sph != 0;
+  } else {
+    if (P.init_mode == 2) {
+      // Basis::randUnif (cylinderXY.cuh:176-183, Sphere.cuh:384-391): the
+      // three draws are Vector3 constructor arguments, consumed z, y, x; a
+      // cylinder's centre has z = 0.
+      const float4 g = S.geo[P.init_inst];
+      const bool sph = P.init_sph != 0;
+      for (int t = 0; t < AXX_INIT_TRIES; ++t) {
+        const float tz = fma_f(2.0f, st.next(), -1.0f);
+        y = fma_f(fma_f(2.0f, st.next(), -1.0f), P.init_R, P.init_cy);
+        x = fma_f(fma_f(2.0f, st.next(), -1.0f), P.init_R, P.init_cx);
+        z = sph ? fma_f(tz, P.init_R, P.init_cz) : tz * P.init_R;
+        if (c0_of(g, sph, x, y, z) < 0.0f) return true;
+      }
+      return false;
+    }
     for (int t = 0; t < AXX_INIT_TRIES; ++t) {
-      const float tz = fma_f(2.0f, st.next(), -1.0f);
-      y = fma_f(fma_f(2.0f, st.next(), -1.0f), P.init_R, P.init_cy);
-      x = fma_f(fma_f(2.0f, st.next(), -1.0f), P.init_R, P.init_cx);
-      z = sph ? fma_f(tz, P.init_R, P.init_cz) : tz * P.init_R;
-      if (c0_of(g, sph, x, y, z) < 0.0f) return true;
+      x = st.next() * P.a;
+      y = st.next() * P.b;
+      z = st.next() * P.c;
+      if (P.init_mode == 0) return true;
+      // Lattice::initializeInRegion: region id of the first containing basis
+      int slot = P.ecs_slot;
+      if (GEOM != AXX_GEOM_FREE) {
+        const int cell = cell_of<GEOM>(P, x, y, z);
+        slot = lookup_list<GEOM>(S, S.cstart[cell], S.cstart[cell + 1], P.ecs_slot, x, y, z);
+      }
+      if (S.region[slot] == P.init_arg) return true;
     }
     return false;
   }
-  for (int t = 0; t < AXX_INIT_TRIES; ++t) {
-    x = st.next() * P.a;
-    y = st.next() * P.b;
-    z = st.next() * P.c;
-    if (P.init_mode == 0) return true;
-    // Lattice::initializeInRegion: region id of the first containing basis
-    if (P.slot_region[lookup_slot<GEOM>(P, G, x, y, z)] == P.init_arg) return true;
-  }
-  return false;
 }
 
-// One walker: returns the channel sums (value - compensation) in phi[] and
-// the T2 sum.  TRACE records every move of the first ntrace walkers.
-template <int GEOM, int KMAX, bool TRACE>
-__device__ __forceinline__ void walk_one(const WalkParams &P, const GeoView &G,
-                                         const TraceParams &T, long long wid, float *phi,
-                                         float &t2sum, bool &aborted) {
-  const bool single = (P.mode == AXX_MODE_SINGLE);
-  const bool relax = !single && (P.flags & 1u);
-  const bool perm = !single && (P.flags & 2u);
-  const bool reject = (P.flags & 4u) != 0;
+struct WalkResult {
+  unsigned caps, hits;
+  bool init_fail, aborted;
+};
+
+// One walker.  On return acc/cmp hold the channel sums (value, Kahan
+// compensation) and t2s/t2c the T2 sum.  TRACE records every move of the
+// walker when wid < ntrace.
+template <int GEOM, int KMAX, int KM, bool TRACE>
+__device__ __forceinline__ WalkResult walk_one(const WalkParams &P, const SmemView &S,
+                                               const TraceParams &T, long long wid,
+                                               float (&acc)[KMAX], float (&cmp)[KMAX],
+                                               float &t2s, float &t2c) {
+  constexpr bool single = KM >= AXX_KM_SINGLE;
+  constexpr bool perm = KM == AXX_KM_LAT_PERM;
+  constexpr bool reject = KM == AXX_KM_LAT_REJ || KM == AXX_KM_SINGLE_REJ;
+  WalkResult res{0u, 0u, false, false};
   const uint64_t seed = ((uint64_t)P.seed_hi << 32) | P.seed_lo;
-  const uint64_t gwid = (uint64_t)(wid + P.walker_offset);
   Stream st;
-  st.init(seed, gwid, 1u);
+  st.init(seed, (uint64_t)(wid + P.walker_offset), 1u);
   float x = 0.0f, y = 0.0f, z = 0.0f;
   bool ok;
   if (single && P.init_quirk) {
     Stream cp = st;  // the reference passes its curandState by value
-    ok = init_position<GEOM>(P, G, cp, x, y, z);
+    ok = init_position<GEOM, KM>(P, S, cp, x, y, z);
   } else {
-    ok = init_position<GEOM>(P, G, st, x, y, z);
+    ok = init_position<GEOM, KM>(P, S, st, x, y, z);
   }
-  if (!ok) atomicAdd(&P.counters[AXX_CNT_INIT_FAIL], 1ull);
-  const long long tw = wid;  // trace index
-  if (TRACE && tw < T.ntrace) {
-    T.init_pos[tw * 3 + 0] = x;
-    T.init_pos[tw * 3 + 1] = y;
-    T.init_pos[tw * 3 + 2] = z;
+  res.init_fail = !ok;
+  if (TRACE && wid < T.ntrace) {
+    T.init_pos[wid * 3 + 0] = x;
+    T.init_pos[wid * 3 + 1] = y;
+    T.init_pos[wid * 3 + 2] = z;
   }
   float ux = x, uy = y, uz = z;  // unbounded position
-  float acc[KMAX], cmp[KMAX];
+  const float *wave = P.wave_il;
 #pragma unroll
   for (int c = 0; c < KMAX; ++c) {
-    acc[c] = 0.0f;
+    const float d = fma_f(P.ch_p[c][2], z, fma_f(P.ch_p[c][1], y, P.ch_p[c][0] * x));
+    acc[c] = __ldg(&wave[c]) * d;
     cmp[c] = 0.0f;
-    if (c < P.K) {
-      const float sw = __ldg(&P.wave[P.ch_wave[c] * P.steps]);
-      const float d = fma_f(P.ch_p[c][2], z, fma_f(P.ch_p[c][1], y, P.ch_p[c][0] * x));
-      acc[c] = sw * d;
-    }
   }
-  float t2s = 0.0f, t2c = 0.0f;
-  int slot = single ? 0 : lookup_slot<GEOM>(P, G, x, y, z);
-  unsigned long long caps = 0, nhits = 0;
+  t2s = 0.0f;
+  t2c = 0.0f;
+  int slot = single ? 0 : P.ecs_slot;
+  if (!single && GEOM != AXX_GEOM_FREE) {
+    const int cell = cell_of<GEOM>(P, x, y, z);
+    slot = lookup_list<GEOM>(S, S.cstart[cell], S.cstart[cell + 1], P.ecs_slot, x, y, z);
+  }
   for (int i = 1; i < P.steps; ++i) {
-    if ((i & 1023) == 0 && P.abort_flag != nullptr) {
-      int f = 0;
-      if ((threadIdx.x & 31) == 0) f = *P.abort_flag;
-      f = __shfl_sync(__activemask(), f, 0);
-      if (f) {
-        aborted = true;
-        break;
-      }
+    if ((i & 1023) == 0 && P.abort_flag != nullptr && *P.abort_flag) {
+      res.aborted = true;
+      break;
     }
-    float v, L;
-    if (single) {
-      v = P.single_speed;
-      L = P.single_step;
-    } else {
-      const float4 s4 = P.slot_tab[slot];
-      v = s4.x;
-      L = s4.y;
-    }
+    const float4 s4 = S.slot[slot];
+    const float v = s4.x, L = s4.y;
     float u1, u2;
     st.next2(u1, u2);
     float dx, dy, dz;
     direction(u1, u2, dx, dy, dz);
     float fx, fy, fz;
     int hits = 0;
+    uint32_t b = 0, e = 0;
+    if (GEOM != AXX_GEOM_FREE) {
+      const int cell = single ? 0 : cell_of<GEOM>(P, x, y, z);
+      b = S.cstart[cell];
+      e = S.cstart[cell + 1];
+    }
     if (GEOM == AXX_GEOM_FREE) {
       fx = fma_f(L, dx, x);
       fy = fma_f(L, dy, y);
       fz = fma_f(L, dz, z);
-    } else {
-      const int cell = cell_of(P, x, y, z);
-      const uint32_t b = G.cstart[cell], e = G.cstart[cell + 1];
-      if (reject) {
-        fx = fma_f(L, dx, x);
-        fy = fma_f(L, dy, y);
-        fz = fma_f(L, dz, z);
-        int s_new;
-        if (single) {
-          s_new = (c0_of(G.geo[0], is_sphere<GEOM>(G.aux[0]), fx, fy, fz) < 0.0f) ? 0 : -1;
-          if (s_new != 0) {
-            fx = x;
-            fy = y;
-            fz = z;
-          }
-        } else {
-          s_new = lookup_list<GEOM>(G, b, e, P.ecs_slot, fx, fy, fz);
-          if (P.slot_region[s_new] != P.slot_region[slot]) {
-            fx = x;
-            fy = y;
-            fz = z;
-          }
-        }
+    } else if (reject) {
+      fx = fma_f(L, dx, x);
+      fy = fma_f(L, dy, y);
+      fz = fma_f(L, dz, z);
+      bool back;
+      if (single) {
+        back = !(c0_of(S.geo[0], is_sphere<GEOM>(S.aux[0]), fx, fy, fz) < 0.0f);
       } else {
-        const MoveOut o = boundary_move<GEOM>(P, G, b, e, x, y, z, dx, dy, dz, L, v, perm, st);
-        fx = o.fx;
-        fy = o.fy;
-        fz = o.fz;
-        hits = o.hits;
-        nhits += (unsigned long long)o.hits;
-        caps += o.capped ? 1ull : 0ull;
+        const int s_new = lookup_list<GEOM>(S, b, e, P.ecs_slot, fx, fy, fz);
+        back = S.region[s_new] != S.region[slot];
       }
+      if (back) {
+        fx = x;
+        fy = y;
+        fz = z;
+      }
+    } else {
+      const MoveOut o =
+          boundary_move<GEOM, perm>(S, b, e, P.ecs_slot, x, y, z, dx, dy, dz, L, v, st);
+      fx = o.fx;
+      fy = o.fy;
+      fz = o.fz;
+      hits = o.hits;
+      res.hits += (unsigned)o.hits;
+      res.caps += o.capped ? 1u : 0u;
     }
     float px, py, pz;  // position seen by the phase
     if (single) {
@@ -421,40 +430,42 @@ __device__ __forceinline__ void walk_one(const WalkParams &P, const GeoView &G,
       fy = wrap1(fy, P.b);
       fz = wrap1(fz, P.c);
     }
+    // phase channels: s_c(i) is wave_il[i*KMAX + c]; padded channels carry
+    // zero waveforms and zero projections
+    const float *wrow = wave + (size_t)i * KMAX;
 #pragma unroll
     for (int c = 0; c < KMAX; ++c) {
-      if (c < P.K) {
-        const float sw = __ldg(&P.wave[P.ch_wave[c] * P.steps + i]);
-        const float d = fma_f(P.ch_p[c][2], pz, fma_f(P.ch_p[c][1], py, P.ch_p[c][0] * px));
-        kahan_add(acc[c], cmp[c], sw * d);
-      }
+      const float d = fma_f(P.ch_p[c][2], pz, fma_f(P.ch_p[c][1], py, P.ch_p[c][0] * px));
+      kahan_add(acc[c], cmp[c], __ldg(&wrow[c]) * d);
     }
-    int new_slot = slot;
-    if (!single && GEOM != AXX_GEOM_FREE) new_slot = lookup_slot<GEOM>(P, G, fx, fy, fz);
-    if (relax) kahan_add(t2s, t2c, P.slot_tab[perm ? new_slot : slot].z);
+    if (!single) {
+      int new_slot = P.ecs_slot;
+      if (GEOM != AXX_GEOM_FREE) {
+        const int cell = cell_of<GEOM>(P, fx, fy, fz);
+        new_slot =
+            lookup_list<GEOM>(S, S.cstart[cell], S.cstart[cell + 1], P.ecs_slot, fx, fy, fz);
+      }
+      // dt/T2 of the move's region (0 without relaxation); the permeable
+      // walk weights the region after the move (accumtime is always 0)
+      kahan_add(t2s, t2c, perm ? S.slot[new_slot].z : s4.z);
+      slot = new_slot;
+    }
     x = fx;
     y = fy;
     z = fz;
-    slot = new_slot;
-    if (TRACE && tw < T.ntrace) {
-      const long long o = tw * (long long)(P.steps - 1) + (i - 1);
+    if (TRACE && wid < T.ntrace) {
+      const long long o = wid * (long long)(P.steps - 1) + (i - 1);
       T.pos[o * 3 + 0] = x;
       T.pos[o * 3 + 1] = y;
       T.pos[o * 3 + 2] = z;
       int rs = slot;
-      if (single) rs = (c0_of(G.geo[0], is_sphere<GEOM>(G.aux[0]), x, y, z) < 0.0f) ? 0 : -1;
-      T.region[o] = (rs == P.ecs_slot && !single) ? -1 : rs;
+      if (single) rs = (c0_of(S.geo[0], is_sphere<GEOM>(S.aux[0]), x, y, z) < 0.0f) ? 0 : -1;
+      T.region[o] = (!single && rs == P.ecs_slot) ? -1 : rs;
       T.hits[o] = hits;
       T.words[o] = (int32_t)st.words_used();
     }
   }
-  if (caps) atomicAdd(&P.counters[AXX_CNT_CAP], caps);
-  if (nhits) atomicAdd(&P.counters[AXX_CNT_HITS], nhits);
-#pragma unroll
-  for (int c = 0; c < KMAX; ++c) phi[2 * c] = acc[c], phi[2 * c + 1] = cmp[c];
-  t2sum = t2s;
-  (void)t2c;
-  phi[2 * KMAX] = t2c;
+  return res;
 }
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -463,67 +474,71 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
-// The walk kernel.  Dynamic shared memory: [warps][M][5] FP64 sums, then
-// (if smem_geom) the instance arrays and the cell lists.
-template <int GEOM, int KMAX, bool TRACE>
-__global__ void __launch_bounds__(AXX_BLOCK) walk_kernel(const __grid_constant__ WalkParams P,
-                                                         const __grid_constant__ TraceParams T) {
+// The walk kernel.  Dynamic shared memory: [warps][M][5] FP64 sums, then the
+// instances, slot table, cell starts, slot regions and cell lists.
+template <int GEOM, int KMAX, int KM, bool TRACE>
+__global__ void __launch_bounds__(AXX_BLOCK, AXX_MIN_BLOCKS)
+    walk_kernel(const __grid_constant__ WalkParams P, const __grid_constant__ TraceParams T) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const int warps = AXX_BLOCK / 32;
+  constexpr int warps = AXX_BLOCK / 32;
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   double *wsum = reinterpret_cast<double *>(smem);
   const int M = P.M;
   for (int j = threadIdx.x; j < warps * M * 5; j += blockDim.x) wsum[j] = 0.0;
 
-  GeoView G;
-  G.geo = P.inst_geo;
-  G.aux = P.inst_aux;
-  G.cstart = P.cell_start;
-  G.clist = P.cell_list;
-  if (P.smem_geom) {
-    unsigned char *p = smem + (size_t)warps * M * 5 * sizeof(double);
-    float4 *sg = reinterpret_cast<float4 *>(p);
-    float4 *sa = sg + P.n_inst;
-    uint32_t *sc = reinterpret_cast<uint32_t *>(sa + P.n_inst);
-    uint16_t *sl = reinterpret_cast<uint16_t *>(sc + P.ncell + 1);
-    for (int j = threadIdx.x; j < P.n_inst; j += blockDim.x) {
-      sg[j] = P.inst_geo[j];
-      sa[j] = P.inst_aux[j];
-    }
-    for (int j = threadIdx.x; j <= P.ncell; j += blockDim.x) sc[j] = P.cell_start[j];
-    for (int j = threadIdx.x; j < P.n_list; j += blockDim.x) sl[j] = P.cell_list[j];
-    G.geo = sg;
-    G.aux = sa;
-    G.cstart = sc;
-    G.clist = sl;
+  // stage the substrate tables (layout fixed by the host planner)
+  float4 *sg = reinterpret_cast<float4 *>(smem + (size_t)warps * M * 5 * sizeof(double));
+  float4 *sa = sg + P.n_inst;
+  float4 *ss = sa + P.n_inst;
+  uint32_t *sc = reinterpret_cast<uint32_t *>(ss + P.n_slot);
+  int *sr = reinterpret_cast<int *>(sc + P.ncell + 1);
+  uint16_t *sl = reinterpret_cast<uint16_t *>(sr + P.n_slot);
+  for (int j = threadIdx.x; j < P.n_inst; j += blockDim.x) {
+    sg[j] = P.inst_geo[j];
+    sa[j] = P.inst_aux[j];
   }
+  for (int j = threadIdx.x; j < P.n_slot; j += blockDim.x) {
+    ss[j] = P.slot_tab[j];
+    sr[j] = P.slot_region[j];
+  }
+  for (int j = threadIdx.x; j <= P.ncell; j += blockDim.x) sc[j] = P.cell_start[j];
+  for (int j = threadIdx.x; j < P.n_list; j += blockDim.x) sl[j] = P.cell_list[j];
   __syncthreads();
+  SmemView S;
+  S.geo = sg;
+  S.aux = sa;
+  S.slot = ss;
+  S.cstart = sc;
+  S.region = sr;
+  S.clist = sl;
 
   const long long ntask = (P.n_walkers + 31) / 32;
   const long long gwarp = (long long)blockIdx.x * warps + wib;
   const long long nwarp = (long long)gridDim.x * warps;
-  const bool single = (P.mode == AXX_MODE_SINGLE);
-  const bool relax = !single && (P.flags & 1u);
-  bool aborted = false;
+  unsigned caps = 0, hits = 0, init_fail = 0, aborted = 0;
   for (long long task = gwarp; task < ntask; task += nwarp) {
     const long long wid = task * 32 + lane;
     const bool active = wid < P.n_walkers;
-    float phi[2 * KMAX + 1];
-    float t2 = 0.0f;
+    float acc[KMAX], cmp[KMAX], t2s = 0.0f, t2c = 0.0f;
 #pragma unroll
-    for (int c = 0; c < 2 * KMAX + 1; ++c) phi[c] = 0.0f;
-    if (active) walk_one<GEOM, KMAX, TRACE>(P, G, T, wid, phi, t2, aborted);
-    // FP64 epilogue (reference: transformAndSumTwoVectors with COS/SIN_EXP_BINARY,
-    // src/util/cudaVector.cu:165-171, src/util/misc.cuh:29-39)
+    for (int c = 0; c < KMAX; ++c) acc[c] = cmp[c] = 0.0f;
+    if (active) {
+      const WalkResult r = walk_one<GEOM, KMAX, KM, TRACE>(P, S, T, wid, acc, cmp, t2s, t2c);
+      caps += r.caps;
+      hits += r.hits;
+      init_fail += r.init_fail ? 1u : 0u;
+      aborted += r.aborted ? 1u : 0u;
+    }
+    // FP64 epilogue (reference: transformAndSumTwoVectors with
+    // COS/SIN_EXP_BINARY, src/util/cudaVector.cu:165-171, src/util/misc.cuh:29-39)
     double ph[KMAX];
 #pragma unroll
-    for (int c = 0; c < KMAX; ++c) ph[c] = (double)phi[2 * c] - (double)phi[2 * c + 1];
-    const double w = relax ? exp(-((double)t2 - (double)phi[2 * KMAX])) : 1.0;
+    for (int c = 0; c < KMAX; ++c) ph[c] = (double)acc[c] - (double)cmp[c];
+    const double w = exp(-((double)t2s - (double)t2c));
     for (int m = 0; m < M; ++m) {
       double ang = 0.0;
 #pragma unroll
-      for (int c = 0; c < KMAX; ++c)
-        if (c < P.K) ang = fma(__ldg(&P.coef[m * P.K + c]), ph[c], ang);
+      for (int c = 0; c < KMAX; ++c) ang = fma(__ldg(&P.coef[m * KMAX + c]), ph[c], ang);
       double sn, cs;
       sincos(ang, &sn, &cs);
       const double xv = active ? cs * w : 0.0, yv = active ? sn * w : 0.0;
@@ -539,7 +554,10 @@ __global__ void __launch_bounds__(AXX_BLOCK) walk_kernel(const __grid_constant__
       }
     }
   }
-  if (aborted) atomicAdd(&P.counters[AXX_CNT_ABORTED], 1ull);
+  if (caps) atomicAdd(&P.counters[AXX_CNT_CAP], (unsigned long long)caps);
+  if (hits) atomicAdd(&P.counters[AXX_CNT_HITS], (unsigned long long)hits);
+  if (init_fail) atomicAdd(&P.counters[AXX_CNT_INIT_FAIL], (unsigned long long)init_fail);
+  if (aborted) atomicAdd(&P.counters[AXX_CNT_ABORTED], (unsigned long long)aborted);
   __syncthreads();
   for (int j = threadIdx.x; j < M * 5; j += blockDim.x) {
     double s = 0.0;

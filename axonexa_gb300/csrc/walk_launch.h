@@ -5,27 +5,46 @@
 
 namespace axx {
 
-// One function per geometry class, compiled in its own translation unit.
-// kmax in {1, 2, 4, 8, 16}.  Returns the launch error.
-cudaError_t launch_walk_free(int kmax, bool trace, const WalkParams &P, const TraceParams &T,
-                             int grid, size_t smem, cudaStream_t s);
-cudaError_t launch_walk_cyl(int kmax, bool trace, const WalkParams &P, const TraceParams &T,
-                            int grid, size_t smem, cudaStream_t s);
-cudaError_t launch_walk_sph(int kmax, bool trace, const WalkParams &P, const TraceParams &T,
-                            int grid, size_t smem, cudaStream_t s);
-cudaError_t launch_walk_mix(int kmax, bool trace, const WalkParams &P, const TraceParams &T,
-                            int grid, size_t smem, cudaStream_t s);
-// Resident blocks per SM of one instantiation at the given dynamic smem.
-int occupancy_walk_free(int kmax, bool trace, size_t smem);
-int occupancy_walk_cyl(int kmax, bool trace, size_t smem);
-int occupancy_walk_sph(int kmax, bool trace, size_t smem);
-int occupancy_walk_mix(int kmax, bool trace, size_t smem);
-inline int occupancy_walk(int geom, int kmax, bool trace, size_t smem) {
+// One function pair per translation unit (geometry class x walk modes).
+// kmax in {1, 2, 4, 8, 16}; km is AXX_KM_*.  Launches return the launch error.
+#define AXX_DECLARE_WALK(name)                                                              \
+  cudaError_t launch_walk_##name(int km, int kmax, bool trace, const WalkParams &P,         \
+                                 const TraceParams &T, int grid, size_t smem, cudaStream_t s); \
+  int occupancy_walk_##name(int km, int kmax, bool trace, size_t smem);
+AXX_DECLARE_WALK(free)
+AXX_DECLARE_WALK(cyl_lat)
+AXX_DECLARE_WALK(cyl_single)
+AXX_DECLARE_WALK(sph_lat)
+AXX_DECLARE_WALK(sph_single)
+AXX_DECLARE_WALK(mix)
+#undef AXX_DECLARE_WALK
+
+inline cudaError_t launch_walk(int geom, int km, int kmax, bool trace, const WalkParams &P,
+                               const TraceParams &T, int grid, size_t smem, cudaStream_t s) {
+  const bool single = km >= AXX_KM_SINGLE;
   switch (geom) {
-    case AXX_GEOM_FREE: return occupancy_walk_free(kmax, trace, smem);
-    case AXX_GEOM_CYL: return occupancy_walk_cyl(kmax, trace, smem);
-    case AXX_GEOM_SPH: return occupancy_walk_sph(kmax, trace, smem);
-    default: return occupancy_walk_mix(kmax, trace, smem);
+    case AXX_GEOM_FREE: return launch_walk_free(km, kmax, trace, P, T, grid, smem, s);
+    case AXX_GEOM_CYL:
+      return single ? launch_walk_cyl_single(km, kmax, trace, P, T, grid, smem, s)
+                    : launch_walk_cyl_lat(km, kmax, trace, P, T, grid, smem, s);
+    case AXX_GEOM_SPH:
+      return single ? launch_walk_sph_single(km, kmax, trace, P, T, grid, smem, s)
+                    : launch_walk_sph_lat(km, kmax, trace, P, T, grid, smem, s);
+    default: return launch_walk_mix(km, kmax, trace, P, T, grid, smem, s);
+  }
+}
+
+inline int occupancy_walk(int geom, int km, int kmax, bool trace, size_t smem) {
+  const bool single = km >= AXX_KM_SINGLE;
+  switch (geom) {
+    case AXX_GEOM_FREE: return occupancy_walk_free(km, kmax, trace, smem);
+    case AXX_GEOM_CYL:
+      return single ? occupancy_walk_cyl_single(km, kmax, trace, smem)
+                    : occupancy_walk_cyl_lat(km, kmax, trace, smem);
+    case AXX_GEOM_SPH:
+      return single ? occupancy_walk_sph_single(km, kmax, trace, smem)
+                    : occupancy_walk_sph_lat(km, kmax, trace, smem);
+    default: return occupancy_walk_mix(km, kmax, trace, smem);
   }
 }
 
