@@ -32,6 +32,7 @@
 
 #if !defined(__CUDA_ARCH__)
 #include <cmath>
+#include <cstring>
 #endif
 
 namespace axx {
@@ -73,6 +74,16 @@ AXX_HD Words4 philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
   o.z = c2;
   o.w = c3;
   return o;
+}
+
+AXX_HD int float_bits(float f) {
+#if defined(__CUDA_ARCH__)
+  return __float_as_int(f);
+#else
+  int i;
+  std::memcpy(&i, &f, 4);
+  return i;
+#endif
 }
 
 AXX_HD float word_to_uniform(uint32_t x) {
@@ -134,6 +145,89 @@ struct Stream {
   AXX_HD uint32_t words_used() const { return blk * 4u + (uint32_t)pos; }
 };
 
+#if defined(__CUDACC__)
+// Device stream with the key schedule precomputed: rk0[r] = seed_lo + r*W0,
+// rk1[r] = seed_hi + r*W1 (mod 2^32) come from the kernel parameters, the
+// product of the constant counter word (the walker id) with M1 in round 1
+// is computed once per walker, and each 32x32 multiply is one 64-bit
+// product.  Outputs are identical to philox4x32_10 above.
+struct DevStream {
+  uint32_t w_lo, w_hi, r1_hi, r1_lo;  // walker id; M1 * w_lo of round 1
+  uint32_t blk;
+  uint32_t b0, b1, b2, b3;
+  int pos;
+
+  template <class KP>
+  __device__ __forceinline__ void init(const KP &P, uint64_t walker, uint32_t first_word) {
+    w_lo = (uint32_t)walker;
+    w_hi = (uint32_t)(walker >> 32);
+    const uint64_t p1 = (uint64_t)0xCD9E8D57u * w_lo;
+    r1_hi = (uint32_t)(p1 >> 32);
+    r1_lo = (uint32_t)p1;
+    blk = first_word >> 2;
+    load(P);
+    pos = (int)(first_word & 3u);
+  }
+  template <class KP>
+  __device__ __forceinline__ void load(const KP &P) {
+    // round 1 (counter words c1 = 0, c2 = w_lo, c3 = w_hi)
+    const uint64_t p0 = (uint64_t)0xD2511F53u * blk;
+    uint32_t c0 = r1_hi ^ P.rk0[0];
+    uint32_t c1 = r1_lo;
+    uint32_t c2 = (uint32_t)(p0 >> 32) ^ w_hi ^ P.rk1[0];
+    uint32_t c3 = (uint32_t)p0;
+#pragma unroll
+    for (int r = 1; r < 10; ++r) {
+      const uint64_t q0 = (uint64_t)0xD2511F53u * c0;
+      const uint64_t q1 = (uint64_t)0xCD9E8D57u * c2;
+      const uint32_t n0 = (uint32_t)(q1 >> 32) ^ c1 ^ P.rk0[r];
+      const uint32_t n2 = (uint32_t)(q0 >> 32) ^ c3 ^ P.rk1[r];
+      c0 = n0;
+      c1 = (uint32_t)q1;
+      c2 = n2;
+      c3 = (uint32_t)q0;
+    }
+    b0 = c0;
+    b1 = c1;
+    b2 = c2;
+    b3 = c3;
+  }
+  template <class KP>
+  __device__ __forceinline__ uint32_t next_word(const KP &P) {
+    if (pos == 4) {
+      ++blk;
+      load(P);
+      pos = 0;
+    }
+    const uint32_t v = (pos == 0) ? b0 : (pos == 1) ? b1 : (pos == 2) ? b2 : b3;
+    ++pos;
+    return v;
+  }
+  template <class KP>
+  __device__ __forceinline__ float next(const KP &P) {
+    return word_to_uniform(next_word(P));
+  }
+  template <class KP>
+  __device__ __forceinline__ void next2(const KP &P, float &u1, float &u2) {
+    if ((pos & 1) == 0) {
+      if (pos == 4) {
+        ++blk;
+        load(P);
+        pos = 0;
+      }
+      const bool lo = (pos == 0);
+      u1 = word_to_uniform(lo ? b0 : b2);
+      u2 = word_to_uniform(lo ? b1 : b3);
+      pos += 2;
+    } else {
+      u1 = next(P);
+      u2 = next(P);
+    }
+  }
+  __device__ __forceinline__ uint32_t words_used() const { return blk * 4u + (uint32_t)pos; }
+};
+#endif
+
 AXX_HD float fma_f(float a, float b, float c) {
 #if defined(__CUDA_ARCH__)
   return __fmaf_rn(a, b, c);
@@ -182,7 +276,7 @@ AXX_HD void sincos_2pi(float u, float &s, float &c) {
   pc = fma_f(f2, pc, 0x1.03c1f0p+6f);
   pc = fma_f(f2, pc, -0x1.3bd3ccp+4f);
   const float cs = fma_f(f2, pc, 1.0f);
-  const int qi = ((int)q) & 3;
+  const int qi = float_bits(q + 12582912.0f) & 3;  // q in 0..4, exact
   // rotate by qi quarter turns
   const float s1 = (qi & 1) ? cs : sn;
   const float c1 = (qi & 1) ? sn : cs;

@@ -62,6 +62,7 @@ struct WalkParams {
   long long n_walkers;
   long long walker_offset;
   uint32_t seed_lo, seed_hi;
+  uint32_t rk0[10], rk1[10];  // Philox round keys of the seed (key schedule precomputed)
   uint32_t flags;
   int init_mode, init_arg;    // AXX_INIT_*; region id for AXX_INIT_IN_REGION
   int init_quirk;             // single pore: start position drawn on a copy of the stream

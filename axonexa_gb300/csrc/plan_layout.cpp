@@ -151,6 +151,10 @@ void fill_walk_params(WalkParams &P, char *base, const ArenaLayout &L, const Geo
   P.walker_offset = p->walker_offset;
   P.seed_lo = (uint32_t)p->seed;
   P.seed_hi = (uint32_t)(p->seed >> 32);
+  for (int r = 0; r < 10; ++r) {  // Philox4x32 Weyl key schedule
+    P.rk0[r] = P.seed_lo + (uint32_t)r * 0x9E3779B9u;
+    P.rk1[r] = P.seed_hi + (uint32_t)r * 0xBB67AE85u;
+  }
   P.flags = p->flags;
   P.init_mode = p->init_mode;
   P.init_arg = p->init_arg;

@@ -164,82 +164,6 @@ struct MoveOut {
   bool capped;
 };
 
-// Specular boundary handling of one move from (sx, sy, sz) with unit
-// direction d and length L, using the instance list [b, e).
-template <int GEOM, bool PERM>
-__device__ __forceinline__ MoveOut boundary_move(const SmemView &S, uint32_t b, uint32_t e,
-                                                 int ecs, float sx, float sy, float sz,
-                                                 float dx, float dy, float dz, float L, float v,
-                                                 Stream &st) {
-  MoveOut o;
-  o.hits = 0;
-  o.capped = false;
-  float rem = L;
-  int last = -1;
-  while (true) {
-    const float aa_c = fma_f(dx, dx, dy * dy);
-    const float aa_s = fma_f(dx, dx, fma_f(dy, dy, dz * dz));
-    float best = AXX_INF;
-    int bk = -1;
-    for (uint32_t j = b; j < e; ++j) {
-      const int k = S.clist[j];
-      const float4 aux = S.aux[k];
-      const bool sph = is_sphere<GEOM>(aux);
-      const float s = seg_hit(S.geo[k], aux.y, sph, k == last, sx, sy, sz, dx, dy, dz,
-                              sph ? aa_s : aa_c, rem);
-      if (s < best) {
-        best = s;
-        bk = k;
-      }
-    }
-    if (bk < 0) break;
-    if (o.hits == AXX_REFL_CAP) {
-      o.capped = true;
-      o.fx = sx;
-      o.fy = sy;
-      o.fz = sz;
-      return o;
-    }
-    ++o.hits;
-    const float hx = fma_f(best, dx, sx), hy = fma_f(best, dy, sy), hz = fma_f(best, dz, sz);
-    const float rem_before = rem;
-    rem = rem - best;
-    const float4 aux = S.aux[bk];
-    if (PERM) {
-      const float u = st.next();
-      const float ptr = div_f(S.slot[aux_slot(aux)].w, v);
-      if (!(u > ptr)) {  // transmitted: continue with the speed of the far side
-        const float tx = fma_f(rem_before, dx, sx), ty = fma_f(rem_before, dy, sy),
-                    tz = fma_f(rem_before, dz, sz);
-        const int ts = lookup_list<GEOM>(S, b, e, ecs, tx, ty, tz);
-        const float vn = S.slot[ts].x;
-        const float remt = div_f(rem * vn, v);
-        o.fx = fma_f(remt, dx, hx);
-        o.fy = fma_f(remt, dy, hy);
-        o.fz = fma_f(remt, dz, hz);
-        return o;
-      }
-    }
-    const float4 g = S.geo[bk];
-    const bool sph = is_sphere<GEOM>(aux);
-    const float nx = (hx - g.x) * aux.x, ny = (hy - g.y) * aux.x;
-    const float nz = sph ? (hz - g.z) * aux.x : 0.0f;
-    const float dn = sph ? fma_f(dx, nx, fma_f(dy, ny, dz * nz)) : fma_f(dx, nx, dy * ny);
-    const float t = -2.0f * dn;
-    dx = fma_f(t, nx, dx);
-    dy = fma_f(t, ny, dy);
-    if (sph) dz = fma_f(t, nz, dz);
-    sx = hx;
-    sy = hy;
-    sz = hz;
-    last = bk;
-  }
-  o.fx = fma_f(rem, dx, sx);
-  o.fy = fma_f(rem, dy, sy);
-  o.fz = fma_f(rem, dz, sz);
-  return o;
-}
-
 __device__ __forceinline__ void kahan_add(float &s, float &c, float y) {
   const float yy = y - c;
   const float t = s + yy;
@@ -247,16 +171,10 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float y) {
   s = t;
 }
 
-__device__ __forceinline__ float wrap1(float x, float a) {
-  if (x > a) return x - a;
-  if (x < 0.0f) return x + a;
-  return x;
-}
-
 // Start position.  Returns false if a rejection loop ran out of tries.
 template <int GEOM, int KM>
 __device__ __forceinline__ bool init_position(const WalkParams &P, const SmemView &S,
-                                              Stream &st, float &x, float &y, float &z) {
+                                              DevStream &st, float &x, float &y, float &z) {
   constexpr bool single = KM >= AXX_KM_SINGLE;
   if (single) {
     // Basis::unifRand (cylinderXY.cuh:45-55, Sphere.cuh:55-63).  The sphere's
@@ -266,20 +184,20 @@ __device__ __forceinline__ bool init_position(const WalkParams &P, const SmemVie
     // as Vector3 constructor arguments.
     const float4 g = S.geo[P.init_inst];
     const bool sph = P.init_sph != 0;
-    x = fma_f(fma_f(2.0f, st.next(), -1.0f), P.init_R, P.init_cx);
-    y = fma_f(fma_f(2.0f, st.next(), -1.0f), P.init_R, P.init_cy);
-    z = sph ? fma_f(fma_f(2.0f, st.next(), -1.0f), P.init_R, P.init_cz)
-            : (2.0f * P.init_R) * st.next();
+    x = fma_f(fma_f(2.0f, st.next(P), -1.0f), P.init_R, P.init_cx);
+    y = fma_f(fma_f(2.0f, st.next(P), -1.0f), P.init_R, P.init_cy);
+    z = sph ? fma_f(fma_f(2.0f, st.next(P), -1.0f), P.init_R, P.init_cz)
+            : (2.0f * P.init_R) * st.next(P);
     for (int t = 0; t < AXX_INIT_TRIES; ++t) {
       if (c0_of(g, sph, x, y, z) < 0.0f) return true;
       if (sph) {
-        z = fma_f(fma_f(2.0f, st.next(), -1.0f), P.init_R, P.init_cz);
-        y = fma_f(fma_f(2.0f, st.next(), -1.0f), P.init_R, P.init_cy);
-        x = fma_f(fma_f(2.0f, st.next(), -1.0f), P.init_R, P.init_cx);
+        z = fma_f(fma_f(2.0f, st.next(P), -1.0f), P.init_R, P.init_cz);
+        y = fma_f(fma_f(2.0f, st.next(P), -1.0f), P.init_R, P.init_cy);
+        x = fma_f(fma_f(2.0f, st.next(P), -1.0f), P.init_R, P.init_cx);
       } else {
-        x = fma_f(fma_f(2.0f, st.next(), -1.0f), P.init_R, P.init_cx);
-        y = fma_f(fma_f(2.0f, st.next(), -1.0f), P.init_R, P.init_cy);
-        z = (2.0f * P.init_R) * st.next();
+        x = fma_f(fma_f(2.0f, st.next(P), -1.0f), P.init_R, P.init_cx);
+        y = fma_f(fma_f(2.0f, st.next(P), -1.0f), P.init_R, P.init_cy);
+        z = (2.0f * P.init_R) * st.next(P);
       }
     }
     return false;
@@ -291,18 +209,18 @@ __device__ __forceinline__ bool init_position(const WalkParams &P, const SmemVie
       const float4 g = S.geo[P.init_inst];
       const bool sph = P.init_sph != 0;
       for (int t = 0; t < AXX_INIT_TRIES; ++t) {
-        const float tz = fma_f(2.0f, st.next(), -1.0f);
-        y = fma_f(fma_f(2.0f, st.next(), -1.0f), P.init_R, P.init_cy);
-        x = fma_f(fma_f(2.0f, st.next(), -1.0f), P.init_R, P.init_cx);
+        const float tz = fma_f(2.0f, st.next(P), -1.0f);
+        y = fma_f(fma_f(2.0f, st.next(P), -1.0f), P.init_R, P.init_cy);
+        x = fma_f(fma_f(2.0f, st.next(P), -1.0f), P.init_R, P.init_cx);
         z = sph ? fma_f(tz, P.init_R, P.init_cz) : tz * P.init_R;
         if (c0_of(g, sph, x, y, z) < 0.0f) return true;
       }
       return false;
     }
     for (int t = 0; t < AXX_INIT_TRIES; ++t) {
-      x = st.next() * P.a;
-      y = st.next() * P.b;
-      z = st.next() * P.c;
+      x = st.next(P) * P.a;
+      y = st.next(P) * P.b;
+      z = st.next(P) * P.c;
       if (P.init_mode == 0) return true;
       // Lattice::initializeInRegion: region id of the first containing basis
       int slot = P.ecs_slot;
@@ -321,25 +239,289 @@ struct WalkResult {
   bool init_fail, aborted;
 };
 
-// One walker.  On return acc/cmp hold the channel sums (value, Kahan
-// compensation) and t2s/t2c the T2 sum.  TRACE records every move of the
-// walker when wid < ntrace.
-template <int GEOM, int KMAX, int KM, bool TRACE>
-__device__ __forceinline__ WalkResult walk_one(const WalkParams &P, const SmemView &S,
-                                               const TraceParams &T, long long wid,
-                                               float (&acc)[KMAX], float (&cmp)[KMAX],
-                                               float &t2s, float &t2c) {
+// State of one walker between moves.
+template <int KMAX>
+struct Walker {
+  float x, y, z;     // wrapped position (bounded position for the single pore)
+  float ux, uy, uz;  // unbounded position
+  int slot;          // slot of the region at (x, y, z)
+  float acc[KMAX], cmp[KMAX];
+  float t2s, t2c;
+};
+
+// The instances and the list a move may test: either the cell list of the
+// move's start (general substrates) or instance 0 held in registers (ONE:
+// substrates of a single instance -- a one-basis cell without reachable
+// ghosts, or any single pore).
+template <int GEOM, bool ONE>
+struct Cands {
+  const SmemView &S;
+  float4 g0, a0;
+  uint32_t b, e;
+  __device__ __forceinline__ int lookup(int ecs, float x, float y, float z) const {
+    if (ONE) return (c0_of(g0, is_sphere<GEOM>(a0), x, y, z) < 0.0f) ? aux_slot(a0) : ecs;
+    return lookup_list<GEOM>(S, b, e, ecs, x, y, z);
+  }
+};
+
+// Specular boundary handling of one move, general substrates and single
+// instances alike.  A cheap test decides for every candidate whether the
+// segment can meet it at all; the warp votes, and only lanes that may hit
+// run the full nearest-hit loop.
+template <int GEOM, bool PERM, bool ONE>
+__device__ __forceinline__ MoveOut boundary(const WalkParams &P, const Cands<GEOM, ONE> &C,
+                                            float sx, float sy, float sz, float dx, float dy,
+                                            float dz, float L, float v, DevStream &st) {
+  bool maybe = false;
+  {
+    const float aa_c = fma_f(dx, dx, dy * dy);
+    const float aa_s = fma_f(dx, dx, fma_f(dy, dy, dz * dz));
+    auto may = [&](const float4 &g, bool sph) {
+      const float px = sx - g.x, py = sy - g.y;
+      const float pz = sph ? (sz - g.z) : 0.0f;
+      const float ex = fma_f(L, dx, px), ey = fma_f(L, dy, py);
+      float bh, c0, c1;
+      if (sph) {
+        const float ez = fma_f(L, dz, pz);
+        bh = fma_f(px, dx, fma_f(py, dy, pz * dz));
+        c0 = fma_f(px, px, fma_f(py, py, fma_f(pz, pz, g.w)));
+        c1 = fma_f(ex, ex, fma_f(ey, ey, fma_f(ez, ez, g.w)));
+      } else {
+        bh = fma_f(px, dx, py * dy);
+        c0 = fma_f(px, px, fma_f(py, py, g.w));
+        c1 = fma_f(ex, ex, fma_f(ey, ey, g.w));
+      }
+      const float aa = sph ? aa_s : aa_c;
+      // the same rejections seg_hit applies first (c0 is exact here: no
+      // instance has been hit yet in this move)
+      const bool no = (c0 < 0.0f && c1 < 0.0f) ||
+                      (c0 >= 0.0f && (bh >= 0.0f || (c0 > 0.0f && c1 > 0.0f &&
+                                                     fma_f(aa, L, bh) <= 0.0f)));
+      return !no;
+    };
+    if (ONE) {
+      maybe = may(C.g0, is_sphere<GEOM>(C.a0));
+    } else {
+      for (uint32_t j = C.b; j < C.e; ++j) {
+        const int k = C.S.clist[j];
+        maybe |= may(C.S.geo[k], is_sphere<GEOM>(C.S.aux[k]));
+      }
+    }
+  }
+  MoveOut o;
+  o.hits = 0;
+  o.capped = false;
+  if (!__any_sync(__activemask(), maybe) || !maybe) {
+    o.fx = fma_f(L, dx, sx);
+    o.fy = fma_f(L, dy, sy);
+    o.fz = fma_f(L, dz, sz);
+    return o;
+  }
+  float rem = L;
+  int last = -1;
+  while (true) {
+    const float aa_c = fma_f(dx, dx, dy * dy);
+    const float aa_s = fma_f(dx, dx, fma_f(dy, dy, dz * dz));
+    float best = AXX_INF;
+    int bk = -1;
+    float4 bg, ba;
+    if (ONE) {
+      const bool sph = is_sphere<GEOM>(C.a0);
+      best = seg_hit(C.g0, C.a0.y, sph, last == 0, sx, sy, sz, dx, dy, dz, sph ? aa_s : aa_c, rem);
+      if (best < AXX_INF) bk = 0;
+      bg = C.g0;
+      ba = C.a0;
+    } else {
+      for (uint32_t j = C.b; j < C.e; ++j) {
+        const int k = C.S.clist[j];
+        const float4 aux = C.S.aux[k];
+        const bool sph = is_sphere<GEOM>(aux);
+        const float s = seg_hit(C.S.geo[k], aux.y, sph, k == last, sx, sy, sz, dx, dy, dz,
+                                sph ? aa_s : aa_c, rem);
+        if (s < best) {
+          best = s;
+          bk = k;
+        }
+      }
+      if (bk >= 0) {
+        bg = C.S.geo[bk];
+        ba = C.S.aux[bk];
+      }
+    }
+    if (bk < 0) break;
+    if (o.hits == AXX_REFL_CAP) {
+      o.capped = true;
+      o.fx = sx;
+      o.fy = sy;
+      o.fz = sz;
+      return o;
+    }
+    ++o.hits;
+    const float hx = fma_f(best, dx, sx), hy = fma_f(best, dy, sy), hz = fma_f(best, dz, sz);
+    const float rem_before = rem;
+    rem = rem - best;
+    if (PERM) {
+      const float u = st.next(P);
+      const float ptr = div_f(C.S.slot[aux_slot(ba)].w, v);
+      if (!(u > ptr)) {  // transmitted: continue with the speed of the far side
+        const float tx = fma_f(rem_before, dx, sx), ty = fma_f(rem_before, dy, sy),
+                    tz = fma_f(rem_before, dz, sz);
+        const int ts = C.lookup(P.ecs_slot, tx, ty, tz);
+        const float vn = C.S.slot[ts].x;
+        const float remt = div_f(rem * vn, v);
+        o.fx = fma_f(remt, dx, hx);
+        o.fy = fma_f(remt, dy, hy);
+        o.fz = fma_f(remt, dz, hz);
+        return o;
+      }
+    }
+    const bool sph = is_sphere<GEOM>(ba);
+    const float nx = (hx - bg.x) * ba.x, ny = (hy - bg.y) * ba.x;
+    const float nz = sph ? (hz - bg.z) * ba.x : 0.0f;
+    const float dn = sph ? fma_f(dx, nx, fma_f(dy, ny, dz * nz)) : fma_f(dx, nx, dy * ny);
+    const float t = -2.0f * dn;
+    dx = fma_f(t, nx, dx);
+    dy = fma_f(t, ny, dy);
+    if (sph) dz = fma_f(t, nz, dz);
+    sx = hx;
+    sy = hy;
+    sz = hz;
+    last = bk;
+  }
+  o.fx = fma_f(rem, dx, sx);
+  o.fy = fma_f(rem, dy, sy);
+  o.fz = fma_f(rem, dz, sz);
+  return o;
+}
+
+// Branch-free periodic wrap (Lattice::lmod for a displacement below one cell).
+__device__ __forceinline__ float wrap_sel(float x, float a) {
+  const float hi = x - a, lo = x + a;
+  return (x > a) ? hi : ((x < 0.0f) ? lo : x);
+}
+
+// One move i of walker W with the uniforms (u1, u2); `words` is the stream
+// position after the move's draws (for traces).
+template <int GEOM, int KMAX, int KM, bool TRACE, bool ONE>
+__device__ __forceinline__ void do_move(const WalkParams &P, const SmemView &S,
+                                        const TraceParams &T, long long wid, int i, float u1,
+                                        float u2, DevStream &st, Walker<KMAX> &W,
+                                        WalkResult &res, const float4 &g0, const float4 &a0) {
   constexpr bool single = KM >= AXX_KM_SINGLE;
   constexpr bool perm = KM == AXX_KM_LAT_PERM;
   constexpr bool reject = KM == AXX_KM_LAT_REJ || KM == AXX_KM_SINGLE_REJ;
+  const float4 s4 = S.slot[W.slot];
+  const float v = s4.x, L = s4.y;
+  float dx, dy, dz;
+  direction(u1, u2, dx, dy, dz);
+  Cands<GEOM, ONE> C{S, g0, a0, 0u, 0u};
+  if (GEOM != AXX_GEOM_FREE && !ONE) {
+    const int cell = single ? 0 : cell_of<GEOM>(P, W.x, W.y, W.z);
+    C.b = S.cstart[cell];
+    C.e = S.cstart[cell + 1];
+  }
+  float fx, fy, fz;
+  int hits = 0;
+  if (GEOM == AXX_GEOM_FREE) {
+    fx = fma_f(L, dx, W.x);
+    fy = fma_f(L, dy, W.y);
+    fz = fma_f(L, dz, W.z);
+  } else if (reject) {
+    fx = fma_f(L, dx, W.x);
+    fy = fma_f(L, dy, W.y);
+    fz = fma_f(L, dz, W.z);
+    bool back;
+    if (single) {
+      back = !(c0_of(g0, is_sphere<GEOM>(a0), fx, fy, fz) < 0.0f);
+    } else {
+      const int s_new = C.lookup(P.ecs_slot, fx, fy, fz);
+      back = S.region[s_new] != S.region[W.slot];
+    }
+    fx = back ? W.x : fx;
+    fy = back ? W.y : fy;
+    fz = back ? W.z : fz;
+  } else {
+    const MoveOut o = boundary<GEOM, perm, ONE>(P, C, W.x, W.y, W.z, dx, dy, dz, L, v, st);
+    fx = o.fx;
+    fy = o.fy;
+    fz = o.fz;
+    hits = o.hits;
+    res.hits += (unsigned)o.hits;
+    res.caps += o.capped ? 1u : 0u;
+  }
+  float px, py, pz;  // position seen by the phase
+  if (single) {
+    px = fx;
+    py = fy;
+    pz = fz;
+  } else {
+    W.ux = W.ux + (fx - W.x);
+    W.uy = W.uy + (fy - W.y);
+    W.uz = W.uz + (fz - W.z);
+    px = W.ux;
+    py = W.uy;
+    pz = W.uz;
+    fx = wrap_sel(fx, P.a);
+    fy = wrap_sel(fy, P.b);
+    fz = wrap_sel(fz, P.c);
+  }
+  // phase channels: s_c(i) is wave_il[i*KMAX + c]; padded channels carry
+  // zero waveforms and zero projections
+  const float *wrow = P.wave_il + (size_t)i * KMAX;
+#pragma unroll
+  for (int c = 0; c < KMAX; ++c) {
+    const float d = fma_f(P.ch_p[c][2], pz, fma_f(P.ch_p[c][1], py, P.ch_p[c][0] * px));
+    kahan_add(W.acc[c], W.cmp[c], __ldg(&wrow[c]) * d);
+  }
+  if (!single) {
+    int new_slot = P.ecs_slot;
+    if (GEOM != AXX_GEOM_FREE) {
+      if (ONE) {
+        new_slot = C.lookup(P.ecs_slot, fx, fy, fz);
+      } else {
+        const int cell = cell_of<GEOM>(P, fx, fy, fz);
+        new_slot =
+            lookup_list<GEOM>(S, S.cstart[cell], S.cstart[cell + 1], P.ecs_slot, fx, fy, fz);
+      }
+    }
+    // dt/T2 of the move's region (0 without relaxation); the permeable walk
+    // weights the region after the move (accumtime is always 0)
+    kahan_add(W.t2s, W.t2c, perm ? S.slot[new_slot].z : s4.z);
+    W.slot = new_slot;
+  }
+  W.x = fx;
+  W.y = fy;
+  W.z = fz;
+  if (TRACE && wid < T.ntrace) {
+    const long long o = wid * (long long)(P.steps - 1) + (i - 1);
+    T.pos[o * 3 + 0] = W.x;
+    T.pos[o * 3 + 1] = W.y;
+    T.pos[o * 3 + 2] = W.z;
+    int rs = W.slot;
+    if (single) rs = (c0_of(g0, is_sphere<GEOM>(a0), W.x, W.y, W.z) < 0.0f) ? 0 : -1;
+    T.region[o] = (!single && rs == P.ecs_slot) ? -1 : rs;
+    T.hits[o] = hits;
+    T.words[o] = (int32_t)st.words_used();
+  }
+}
+
+// One walker.  On return W holds the channel sums (value, Kahan
+// compensation) and the T2 sum.  TRACE records every move of the walker when
+// wid < ntrace.
+template <int GEOM, int KMAX, int KM, bool TRACE, bool ONE>
+__device__ __forceinline__ WalkResult walk_one(const WalkParams &P, const SmemView &S,
+                                               const TraceParams &T, long long wid,
+                                               Walker<KMAX> &W) {
+  constexpr bool single = KM >= AXX_KM_SINGLE;
+  constexpr bool perm = KM == AXX_KM_LAT_PERM;
   WalkResult res{0u, 0u, false, false};
-  const uint64_t seed = ((uint64_t)P.seed_hi << 32) | P.seed_lo;
-  Stream st;
-  st.init(seed, (uint64_t)(wid + P.walker_offset), 1u);
+  const float4 g0 = S.geo[0], a0 = S.aux[0];
+  DevStream st;
+  st.init(P, (uint64_t)(wid + P.walker_offset), 1u);
   float x = 0.0f, y = 0.0f, z = 0.0f;
   bool ok;
   if (single && P.init_quirk) {
-    Stream cp = st;  // the reference passes its curandState by value
+    DevStream cp = st;  // the reference passes its curandState by value
     ok = init_position<GEOM, KM>(P, S, cp, x, y, z);
   } else {
     ok = init_position<GEOM, KM>(P, S, st, x, y, z);
@@ -350,120 +532,55 @@ __device__ __forceinline__ WalkResult walk_one(const WalkParams &P, const SmemVi
     T.init_pos[wid * 3 + 1] = y;
     T.init_pos[wid * 3 + 2] = z;
   }
-  float ux = x, uy = y, uz = z;  // unbounded position
-  const float *wave = P.wave_il;
+  W.x = W.ux = x;
+  W.y = W.uy = y;
+  W.z = W.uz = z;
 #pragma unroll
   for (int c = 0; c < KMAX; ++c) {
     const float d = fma_f(P.ch_p[c][2], z, fma_f(P.ch_p[c][1], y, P.ch_p[c][0] * x));
-    acc[c] = __ldg(&wave[c]) * d;
-    cmp[c] = 0.0f;
+    W.acc[c] = __ldg(&P.wave_il[c]) * d;
+    W.cmp[c] = 0.0f;
   }
-  t2s = 0.0f;
-  t2c = 0.0f;
-  int slot = single ? 0 : P.ecs_slot;
+  W.t2s = 0.0f;
+  W.t2c = 0.0f;
+  W.slot = single ? 0 : P.ecs_slot;
   if (!single && GEOM != AXX_GEOM_FREE) {
-    const int cell = cell_of<GEOM>(P, x, y, z);
-    slot = lookup_list<GEOM>(S, S.cstart[cell], S.cstart[cell + 1], P.ecs_slot, x, y, z);
+    if (ONE) {
+      W.slot = (c0_of(g0, is_sphere<GEOM>(a0), x, y, z) < 0.0f) ? aux_slot(a0) : P.ecs_slot;
+    } else {
+      const int cell = cell_of<GEOM>(P, x, y, z);
+      W.slot = lookup_list<GEOM>(S, S.cstart[cell], S.cstart[cell + 1], P.ecs_slot, x, y, z);
+    }
   }
-  for (int i = 1; i < P.steps; ++i) {
+  int i = 1;
+  // Two moves per Philox block when every walker of the warp has its stream
+  // at a block boundary and moves draw nothing else (the lattice walk from a
+  // uniform start); otherwise the general stream.
+  if (!perm && __all_sync(__activemask(), st.pos == 4)) {
+    for (; i + 1 < P.steps; i += 2) {
+      if (((i + 1) & 1023) == 0 && P.abort_flag != nullptr && *P.abort_flag) {
+        res.aborted = true;
+        return res;
+      }
+      ++st.blk;
+      st.load(P);
+      const uint32_t w0 = st.b0, w1 = st.b1, w2 = st.b2, w3 = st.b3;
+      st.pos = 2;
+      do_move<GEOM, KMAX, KM, TRACE, ONE>(P, S, T, wid, i, word_to_uniform(w0),
+                                           word_to_uniform(w1), st, W, res, g0, a0);
+      st.pos = 4;
+      do_move<GEOM, KMAX, KM, TRACE, ONE>(P, S, T, wid, i + 1, word_to_uniform(w2),
+                                           word_to_uniform(w3), st, W, res, g0, a0);
+    }
+  }
+  for (; i < P.steps; ++i) {
     if ((i & 1023) == 0 && P.abort_flag != nullptr && *P.abort_flag) {
       res.aborted = true;
       break;
     }
-    const float4 s4 = S.slot[slot];
-    const float v = s4.x, L = s4.y;
     float u1, u2;
-    st.next2(u1, u2);
-    float dx, dy, dz;
-    direction(u1, u2, dx, dy, dz);
-    float fx, fy, fz;
-    int hits = 0;
-    uint32_t b = 0, e = 0;
-    if (GEOM != AXX_GEOM_FREE) {
-      const int cell = single ? 0 : cell_of<GEOM>(P, x, y, z);
-      b = S.cstart[cell];
-      e = S.cstart[cell + 1];
-    }
-    if (GEOM == AXX_GEOM_FREE) {
-      fx = fma_f(L, dx, x);
-      fy = fma_f(L, dy, y);
-      fz = fma_f(L, dz, z);
-    } else if (reject) {
-      fx = fma_f(L, dx, x);
-      fy = fma_f(L, dy, y);
-      fz = fma_f(L, dz, z);
-      bool back;
-      if (single) {
-        back = !(c0_of(S.geo[0], is_sphere<GEOM>(S.aux[0]), fx, fy, fz) < 0.0f);
-      } else {
-        const int s_new = lookup_list<GEOM>(S, b, e, P.ecs_slot, fx, fy, fz);
-        back = S.region[s_new] != S.region[slot];
-      }
-      if (back) {
-        fx = x;
-        fy = y;
-        fz = z;
-      }
-    } else {
-      const MoveOut o =
-          boundary_move<GEOM, perm>(S, b, e, P.ecs_slot, x, y, z, dx, dy, dz, L, v, st);
-      fx = o.fx;
-      fy = o.fy;
-      fz = o.fz;
-      hits = o.hits;
-      res.hits += (unsigned)o.hits;
-      res.caps += o.capped ? 1u : 0u;
-    }
-    float px, py, pz;  // position seen by the phase
-    if (single) {
-      px = fx;
-      py = fy;
-      pz = fz;
-    } else {
-      ux = ux + (fx - x);
-      uy = uy + (fy - y);
-      uz = uz + (fz - z);
-      px = ux;
-      py = uy;
-      pz = uz;
-      fx = wrap1(fx, P.a);
-      fy = wrap1(fy, P.b);
-      fz = wrap1(fz, P.c);
-    }
-    // phase channels: s_c(i) is wave_il[i*KMAX + c]; padded channels carry
-    // zero waveforms and zero projections
-    const float *wrow = wave + (size_t)i * KMAX;
-#pragma unroll
-    for (int c = 0; c < KMAX; ++c) {
-      const float d = fma_f(P.ch_p[c][2], pz, fma_f(P.ch_p[c][1], py, P.ch_p[c][0] * px));
-      kahan_add(acc[c], cmp[c], __ldg(&wrow[c]) * d);
-    }
-    if (!single) {
-      int new_slot = P.ecs_slot;
-      if (GEOM != AXX_GEOM_FREE) {
-        const int cell = cell_of<GEOM>(P, fx, fy, fz);
-        new_slot =
-            lookup_list<GEOM>(S, S.cstart[cell], S.cstart[cell + 1], P.ecs_slot, fx, fy, fz);
-      }
-      // dt/T2 of the move's region (0 without relaxation); the permeable
-      // walk weights the region after the move (accumtime is always 0)
-      kahan_add(t2s, t2c, perm ? S.slot[new_slot].z : s4.z);
-      slot = new_slot;
-    }
-    x = fx;
-    y = fy;
-    z = fz;
-    if (TRACE && wid < T.ntrace) {
-      const long long o = wid * (long long)(P.steps - 1) + (i - 1);
-      T.pos[o * 3 + 0] = x;
-      T.pos[o * 3 + 1] = y;
-      T.pos[o * 3 + 2] = z;
-      int rs = slot;
-      if (single) rs = (c0_of(S.geo[0], is_sphere<GEOM>(S.aux[0]), x, y, z) < 0.0f) ? 0 : -1;
-      T.region[o] = (!single && rs == P.ecs_slot) ? -1 : rs;
-      T.hits[o] = hits;
-      T.words[o] = (int32_t)st.words_used();
-    }
+    st.next2(P, u1, u2);
+    do_move<GEOM, KMAX, KM, TRACE, ONE>(P, S, T, wid, i, u1, u2, st, W, res, g0, a0);
   }
   return res;
 }
@@ -516,14 +633,19 @@ __global__ void __launch_bounds__(AXX_BLOCK, AXX_MIN_BLOCKS)
   const long long gwarp = (long long)blockIdx.x * warps + wib;
   const long long nwarp = (long long)gridDim.x * warps;
   unsigned caps = 0, hits = 0, init_fail = 0, aborted = 0;
+  // a single instance (one basis without reachable ghosts, or a single pore)
+  // is held in registers instead of walking a list
+  const bool one = (GEOM != AXX_GEOM_FREE) && P.n_inst == 1 && P.ncell == 1;
   for (long long task = gwarp; task < ntask; task += nwarp) {
     const long long wid = task * 32 + lane;
     const bool active = wid < P.n_walkers;
-    float acc[KMAX], cmp[KMAX], t2s = 0.0f, t2c = 0.0f;
+    Walker<KMAX> W;
 #pragma unroll
-    for (int c = 0; c < KMAX; ++c) acc[c] = cmp[c] = 0.0f;
+    for (int c = 0; c < KMAX; ++c) W.acc[c] = W.cmp[c] = 0.0f;
+    W.t2s = W.t2c = 0.0f;
     if (active) {
-      const WalkResult r = walk_one<GEOM, KMAX, KM, TRACE>(P, S, T, wid, acc, cmp, t2s, t2c);
+      const WalkResult r = one ? walk_one<GEOM, KMAX, KM, TRACE, true>(P, S, T, wid, W)
+                               : walk_one<GEOM, KMAX, KM, TRACE, false>(P, S, T, wid, W);
       caps += r.caps;
       hits += r.hits;
       init_fail += r.init_fail ? 1u : 0u;
@@ -533,8 +655,8 @@ __global__ void __launch_bounds__(AXX_BLOCK, AXX_MIN_BLOCKS)
     // COS/SIN_EXP_BINARY, src/util/cudaVector.cu:165-171, src/util/misc.cuh:29-39)
     double ph[KMAX];
 #pragma unroll
-    for (int c = 0; c < KMAX; ++c) ph[c] = (double)acc[c] - (double)cmp[c];
-    const double w = exp(-((double)t2s - (double)t2c));
+    for (int c = 0; c < KMAX; ++c) ph[c] = (double)W.acc[c] - (double)W.cmp[c];
+    const double w = exp(-((double)W.t2s - (double)W.t2c));
     for (int m = 0; m < M; ++m) {
       double ang = 0.0;
 #pragma unroll

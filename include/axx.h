@@ -231,6 +231,57 @@ axx_status axx_sync(axx_ctx *ctx);
  * no reference counterpart. */
 axx_status axx_fp32_fma_peak(axx_ctx *ctx, double *fma_per_s);
 
+/* ---- batched acquisitions: many substrates in one persistent launch ------ */
+
+/* One acquisition of a batch (one substrate, its sequences, its run). */
+typedef struct {
+  int32_t mode;                  /* 0: lattice walk, 1: single-pore walk */
+  axx_lattice lattice;           /* lattice mode */
+  const axx_basis *basis;        /* lattice bases, or the single pore in basis[0] */
+  int32_t nbasis;
+  const axx_sequence *seqs;      /* at most 64 per job */
+  int32_t nseq;
+  axx_run_params params;         /* walkers, steps, seed, timestep, flags */
+} axx_job;
+
+typedef struct {
+  int32_t tile;          /* walkers per work item (multiple of 128); 0: autotuned */
+  int32_t blocks_per_sm; /* resident blocks per SM; 0: the occupancy limit */
+  int32_t use_graph;     /* 1: capture the launch in a CUDA graph and replay it */
+} axx_batch_options;
+
+typedef struct axx_batch axx_batch;
+
+/* Plans a batch: uploads every job's tables once and cuts the jobs' walker
+ * ranges into work items (longest first) that one persistent kernel takes
+ * from a shared counter.  Replaces running the acquisitions one by one
+ * (phaseAcquisitionStream::runAcquisitionStreamLattice / runAcquisitionStream,
+ * src/acquisition/phaseAcquisitionStream.cuh:254-613).  Jobs may not use
+ * AXX_FLAG_SIMPLE_REJECTION.  With tile == 0 the tile and blocks per SM come
+ * from axx_autotune_batch's cache (or are tuned on first use). */
+axx_status axx_batch_create(axx_ctx *ctx, const axx_job *jobs, int njobs,
+                            const axx_batch_options *opt, axx_batch **out);
+/* Enqueues one execution of the whole batch (graph replay or launches). */
+axx_status axx_batch_launch(axx_batch *b);
+/* Waits and writes the signals: mx/my hold sum(nseq) entries, job after job;
+ * stats (optional) is an array of njobs records whose sxx/syy/sxy may be NULL. */
+axx_status axx_batch_read(axx_batch *b, double *mx, double *my, axx_stats *stats);
+axx_status axx_batch_info(const axx_batch *b, int *items, int *tile, int *blocks_per_sm,
+                          int *kernel_launches, int64_t *walker_steps);
+axx_status axx_batch_destroy(axx_batch *b);
+/* One-shot batch: create, launch, read, destroy. */
+axx_status axx_run_batch(axx_ctx *ctx, const axx_job *jobs, int njobs,
+                         const axx_batch_options *opt, double *mx, double *my,
+                         axx_stats *stats);
+/* The project's autotuner: times candidate (tile, blocks per SM) pairs on a
+ * shortened copy of the batch (steps capped at `probe_steps`), returns the
+ * fastest in *best and its time in *best_ms, and records it in the tuning
+ * cache (file named by AXX_AUTOTUNE_CACHE, default
+ * $HOME/.cache/axonexa_gb300/autotune.tsv) under the device name and the
+ * batch's shape. */
+axx_status axx_autotune_batch(axx_ctx *ctx, const axx_job *jobs, int njobs, int probe_steps,
+                              axx_batch_options *best, double *best_ms);
+
 /* ---- sequences ----------------------------------------------------------- */
 
 /* b-value of one sequence, as the reference functor's getB(). */
