@@ -10,5 +10,6 @@ from .acquisition import (GAMMA, PI, ApodCosGFunc, CosGFunc, Cylinder_XY, Device
                           phaseAcquisitionStream, philox_words, run_lattice, run_single,
                           trace_lattice, trace_single)
 from .substrate import rps_gamma_pack, hex_cell
+from .batch import Batch, Job, autotune, run_batch
 
 __all__ = [n for n in dir() if not n.startswith("_")]

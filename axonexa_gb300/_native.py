@@ -63,6 +63,16 @@ class Stats(C.Structure):
                 ("walker_steps", C.c_int64), ("boundary_hits", C.c_int64)]
 
 
+class Job(C.Structure):
+    _fields_ = [("mode", C.c_int32), ("lattice", LatticeRec), ("basis", C.POINTER(Basis)),
+                ("nbasis", C.c_int32), ("seqs", C.POINTER(SequenceRec)), ("nseq", C.c_int32),
+                ("params", RunParams)]
+
+
+class BatchOptions(C.Structure):
+    _fields_ = [("tile", C.c_int32), ("blocks_per_sm", C.c_int32), ("use_graph", C.c_int32)]
+
+
 # exported symbols and their argument types
 _SIGS = {
     "axx_abi_version": ([], C.c_int),
@@ -98,6 +108,18 @@ _SIGS = {
     "axx_event_elapsed": ([C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_float)], C.c_int),
     "axx_sync": ([C.c_void_p], C.c_int),
     "axx_fp32_fma_peak": ([C.c_void_p, C.POINTER(C.c_double)], C.c_int),
+    "axx_batch_create": ([C.c_void_p, C.POINTER(Job), C.c_int, C.POINTER(BatchOptions),
+                          C.POINTER(C.c_void_p)], C.c_int),
+    "axx_batch_launch": ([C.c_void_p], C.c_int),
+    "axx_batch_read": ([C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                        C.POINTER(Stats)], C.c_int),
+    "axx_batch_info": ([C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                        C.POINTER(C.c_int), C.POINTER(C.c_int64)], C.c_int),
+    "axx_batch_destroy": ([C.c_void_p], C.c_int),
+    "axx_run_batch": ([C.c_void_p, C.POINTER(Job), C.c_int, C.POINTER(BatchOptions),
+                       C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(Stats)], C.c_int),
+    "axx_autotune_batch": ([C.c_void_p, C.POINTER(Job), C.c_int, C.c_int,
+                            C.POINTER(BatchOptions), C.POINTER(C.c_double)], C.c_int),
     "axx_bvalue": ([C.POINTER(SequenceRec), C.c_double, C.POINTER(C.c_double)], C.c_int),
     "axx_gradient_eval": ([C.POINTER(SequenceRec), C.POINTER(C.c_double), C.c_int,
                            C.POINTER(C.c_double)], C.c_int),

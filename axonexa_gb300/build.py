@@ -30,6 +30,7 @@ CUDA_SOURCES = [
     "walk_mix.cu",
     "misc_kernels.cu",
     "noalloc.cu",
+    "batch.cu",
 ]
 HOST_SOURCES = ["api.cpp", "host_plan.cpp", "plan_layout.cpp", "substrate.cpp"]
 

@@ -1,0 +1,736 @@
+// batch.cu -- many acquisitions (substrates x sequences, uneven walker
+// counts) in one persistent launch, replayed from a captured CUDA graph, with
+// the launch shape chosen by the project's autotuner.
+//
+// The reference runs acquisitions one after another, two streams per device
+// (phaseAcquisitionStream::runAcquisitionStreamLattice / runAcquisitionStream,
+// src/acquisition/phaseAcquisitionStream.cuh:254-613).  Here every job's
+// tables are uploaded once; each job's walker range is cut into work items of
+// `tile` walkers; the items, longest (walkers x steps) first, are taken by
+// resident blocks from one atomic counter.  A block stages the job's walk
+// parameters and substrate in shared memory when its item belongs to a new
+// job, walks the item with the same per-walker code as the single-job kernel
+// (walk_one: identical trajectories), and writes the item's FP64 partial sums
+// to the item's fixed slot; batch_reduce_kernel then adds each job's item
+// partials in item order, so results do not depend on which block ran which
+// item.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <mutex>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include <sys/stat.h>
+
+#include "../../include/axx.h"
+#include "ctx_internal.h"
+#include "host_plan.h"
+#include "plan_layout.h"
+#include "walk_kernel.cuh"
+
+namespace axx {
+
+constexpr int kBatchMaxSeq = 64;  // sequences per job (shared-memory sums)
+
+struct BatchJob {
+  WalkParams P;       // tables point into the batch arena
+  int one;            // single-instance path
+  int M;
+  long long part_off; // first partial (in doubles) of this job's items
+  long long out_off;  // first output (in doubles) of this job
+};
+
+struct BatchItem {
+  int job;
+  int local;          // item index within its job (its partial slot)
+  long long first;    // first walker id of the job
+  int count;          // walkers in the item
+  int pad;
+};
+
+template <int KMAX>
+__global__ void __launch_bounds__(AXX_BLOCK, AXX_MIN_BLOCKS)
+    batch_kernel(const BatchJob *__restrict__ jobs, const BatchItem *__restrict__ items,
+                 int nitems, unsigned *item_counter, double *partials) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  constexpr int warps = AXX_BLOCK / 32;
+  WalkParams &sP = *reinterpret_cast<WalkParams *>(smem);
+  constexpr size_t p_bytes = (sizeof(WalkParams) + 15) & ~(size_t)15;
+  double *wsum = reinterpret_cast<double *>(smem + p_bytes);
+  unsigned char *geo_base = smem + p_bytes + (size_t)warps * kBatchMaxSeq * 5 * sizeof(double);
+  __shared__ int s_item;
+  __shared__ int s_one;
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int cur = -1;
+  TraceParams T{};
+  SmemView S;
+  for (;;) {
+    if (threadIdx.x == 0) s_item = (int)atomicAdd(item_counter, 1u);
+    __syncthreads();
+    const int it = s_item;
+    if (it >= nitems) break;
+    const BatchItem item = items[it];
+    if (item.job != cur) {
+      // stage the job's parameters and substrate tables
+      const int *src = reinterpret_cast<const int *>(&jobs[item.job].P);
+      int *dst = reinterpret_cast<int *>(smem);
+      for (int j = threadIdx.x; j < (int)(sizeof(WalkParams) / 4); j += blockDim.x) dst[j] = src[j];
+      if (threadIdx.x == 0) s_one = jobs[item.job].one;
+      __syncthreads();
+      float4 *sg = reinterpret_cast<float4 *>(geo_base);
+      float4 *sa = sg + sP.n_inst;
+      float4 *ss = sa + sP.n_inst;
+      uint32_t *sc = reinterpret_cast<uint32_t *>(ss + sP.n_slot);
+      int *sr = reinterpret_cast<int *>(sc + sP.ncell + 1);
+      uint16_t *sl = reinterpret_cast<uint16_t *>(sr + sP.n_slot);
+      for (int j = threadIdx.x; j < sP.n_inst; j += blockDim.x) {
+        sg[j] = sP.inst_geo[j];
+        sa[j] = sP.inst_aux[j];
+      }
+      for (int j = threadIdx.x; j < sP.n_slot; j += blockDim.x) {
+        ss[j] = sP.slot_tab[j];
+        sr[j] = sP.slot_region[j];
+      }
+      for (int j = threadIdx.x; j <= sP.ncell; j += blockDim.x) sc[j] = sP.cell_start[j];
+      for (int j = threadIdx.x; j < sP.n_list; j += blockDim.x) sl[j] = sP.cell_list[j];
+      S.geo = sg;
+      S.aux = sa;
+      S.slot = ss;
+      S.cstart = sc;
+      S.region = sr;
+      S.clist = sl;
+      cur = item.job;
+    }
+    const int M = sP.M;
+    for (int j = threadIdx.x; j < warps * M * 5; j += blockDim.x) wsum[j] = 0.0;
+    __syncthreads();
+    const bool one = s_one != 0;
+    const int ntask = (item.count + 31) / 32;
+    unsigned caps = 0, hits = 0, init_fail = 0, aborted = 0;
+    for (int task = wib; task < ntask; task += warps) {
+      const int off = task * 32 + lane;
+      const bool active = off < item.count;
+      const long long wid = item.first + off;
+      Walker<KMAX> W;
+#pragma unroll
+      for (int c = 0; c < KMAX; ++c) W.acc[c] = W.cmp[c] = 0.0f;
+      W.t2s = W.t2c = 0.0f;
+      if (active) {
+        WalkResult r{0u, 0u, false, false};
+        switch (sP.km) {
+          case AXX_KM_LAT_IMP:
+            r = one ? walk_one<AXX_GEOM_MIX, KMAX, AXX_KM_LAT_IMP, false, true>(sP, S, T, wid, W)
+                    : walk_one<AXX_GEOM_MIX, KMAX, AXX_KM_LAT_IMP, false, false>(sP, S, T, wid, W);
+            break;
+          case AXX_KM_LAT_PERM:
+            r = one ? walk_one<AXX_GEOM_MIX, KMAX, AXX_KM_LAT_PERM, false, true>(sP, S, T, wid, W)
+                    : walk_one<AXX_GEOM_MIX, KMAX, AXX_KM_LAT_PERM, false, false>(sP, S, T, wid, W);
+            break;
+          default:
+            r = walk_one<AXX_GEOM_MIX, KMAX, AXX_KM_SINGLE, false, true>(sP, S, T, wid, W);
+            break;
+        }
+        caps += r.caps;
+        hits += r.hits;
+        init_fail += r.init_fail ? 1u : 0u;
+        aborted += r.aborted ? 1u : 0u;
+      }
+      double ph[KMAX];
+#pragma unroll
+      for (int c = 0; c < KMAX; ++c) ph[c] = (double)W.acc[c] - (double)W.cmp[c];
+      const double w = exp(-((double)W.t2s - (double)W.t2c));
+      for (int m = 0; m < M; ++m) {
+        double ang = 0.0;
+#pragma unroll
+        for (int c = 0; c < KMAX; ++c) ang = fma(sP.coef[m * KMAX + c], ph[c], ang);
+        double sn, cs;
+        sincos(ang, &sn, &cs);
+        const double xv = active ? cs * w : 0.0, yv = active ? sn * w : 0.0;
+        const double s0 = warp_sum(xv), s1 = warp_sum(yv), s2 = warp_sum(xv * xv),
+                     s3 = warp_sum(yv * yv), s4 = warp_sum(xv * yv);
+        if (lane == 0) {
+          double *d = wsum + ((size_t)wib * M + m) * 5;
+          d[0] += s0;
+          d[1] += s1;
+          d[2] += s2;
+          d[3] += s3;
+          d[4] += s4;
+        }
+      }
+    }
+    if (caps) atomicAdd(&sP.counters[AXX_CNT_CAP], (unsigned long long)caps);
+    if (hits) atomicAdd(&sP.counters[AXX_CNT_HITS], (unsigned long long)hits);
+    if (init_fail) atomicAdd(&sP.counters[AXX_CNT_INIT_FAIL], (unsigned long long)init_fail);
+    if (aborted) atomicAdd(&sP.counters[AXX_CNT_ABORTED], (unsigned long long)aborted);
+    __syncthreads();
+    double *dst = partials + jobs[item.job].part_off + (long long)item.local * M * 5;
+    for (int j = threadIdx.x; j < M * 5; j += blockDim.x) {
+      double s = 0.0;
+      for (int q = 0; q < warps; ++q) s += wsum[(size_t)q * M * 5 + j];
+      dst[j] = s;
+    }
+    __syncthreads();
+  }
+}
+
+// out[o] for output o = (job j, index within the job) sums the job's item
+// partials in item order.
+__global__ void __launch_bounds__(256)
+    batch_reduce_kernel(const BatchJob *__restrict__ jobs, const int2 *__restrict__ out_map,
+                        const int *__restrict__ job_items, const double *__restrict__ partials,
+                        double *__restrict__ out) {
+  __shared__ double red[256];
+  const int o = blockIdx.x;
+  const int2 jm = out_map[o];
+  const BatchJob &J = jobs[jm.x];
+  const int n = job_items[jm.x];
+  const int stride = J.M * 5;
+  double s = 0.0;
+  for (int t = threadIdx.x; t < n; t += blockDim.x) s += partials[J.part_off + (long long)t * stride + jm.y];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[J.out_off + jm.y] = red[0];
+}
+
+template <int KMAX>
+static cudaError_t batch_prepare(size_t smem) {
+  if (smem > 48 * 1024)
+    return cudaFuncSetAttribute(batch_kernel<KMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)smem);
+  return cudaSuccess;
+}
+
+template <int KMAX>
+static int batch_occ(size_t smem) {
+  if (batch_prepare<KMAX>(smem) != cudaSuccess) return 0;
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_kernel<KMAX>, AXX_BLOCK, smem) !=
+      cudaSuccess)
+    return 0;
+  return n;
+}
+
+static cudaError_t batch_go(int kmax, int grid, size_t smem, cudaStream_t s, const BatchJob *jobs,
+                            const BatchItem *items, int nitems, unsigned *ctr, double *part) {
+  switch (kmax) {
+    case 1: batch_kernel<1><<<grid, AXX_BLOCK, smem, s>>>(jobs, items, nitems, ctr, part); break;
+    case 2: batch_kernel<2><<<grid, AXX_BLOCK, smem, s>>>(jobs, items, nitems, ctr, part); break;
+    case 4: batch_kernel<4><<<grid, AXX_BLOCK, smem, s>>>(jobs, items, nitems, ctr, part); break;
+    case 8: batch_kernel<8><<<grid, AXX_BLOCK, smem, s>>>(jobs, items, nitems, ctr, part); break;
+    default: batch_kernel<16><<<grid, AXX_BLOCK, smem, s>>>(jobs, items, nitems, ctr, part); break;
+  }
+  return cudaGetLastError();
+}
+
+static int batch_occupancy(int kmax, size_t smem) {
+  switch (kmax) {
+    case 1: return batch_occ<1>(smem);
+    case 2: return batch_occ<2>(smem);
+    case 4: return batch_occ<4>(smem);
+    case 8: return batch_occ<8>(smem);
+    default: return batch_occ<16>(smem);
+  }
+}
+
+}  // namespace axx
+
+using namespace axx;
+
+struct axx_batch {
+  axx_ctx *ctx = nullptr;
+  int njobs = 0, nitems = 0, kmax = 1, tile = 0, bps = 0, grid = 0, nout = 0;
+  size_t smem = 0;
+  void *arena = nullptr;
+  BatchJob *d_jobs = nullptr;
+  BatchItem *d_items = nullptr;
+  int2 *d_outmap = nullptr;
+  int *d_jobitems = nullptr;
+  unsigned *d_ctr = nullptr;
+  double *d_part = nullptr, *d_out = nullptr;
+  unsigned long long *d_counters = nullptr;
+  std::vector<int> job_M;
+  std::vector<long long> job_ws;
+  long long walker_steps = 0;
+  bool use_graph = false;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  bool launched = false;
+};
+
+namespace {
+
+axx_status bfail(axx_ctx *ctx, axx_status s, const std::string &m) {
+  if (ctx) ctx->err = m;
+  return s;
+}
+
+axx_status bcuda(axx_ctx *ctx, cudaError_t e, const char *where) {
+  if (ctx) ctx->err = std::string(where) + ": " + cudaGetErrorString(e);
+  return e == cudaErrorMemoryAllocation ? AXX_ERR_OUT_OF_MEMORY : AXX_ERR_CUDA;
+}
+
+size_t up256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+uint64_t fnv(uint64_t h, uint64_t v) {
+  for (int i = 0; i < 8; ++i) {
+    h ^= (v >> (8 * i)) & 0xffu;
+    h *= 1099511628211ull;
+  }
+  return h;
+}
+
+// Shape of a batch for the tuning cache.
+uint64_t batch_shape(const axx_job *jobs, int njobs) {
+  uint64_t h = 1469598103934665603ull;
+  h = fnv(h, (uint64_t)njobs);
+  for (int j = 0; j < njobs; ++j) {
+    const axx_job &J = jobs[j];
+    h = fnv(h, (uint64_t)J.mode);
+    h = fnv(h, (uint64_t)J.params.num_walkers);
+    h = fnv(h, (uint64_t)J.params.steps);
+    h = fnv(h, (uint64_t)J.nbasis);
+    h = fnv(h, (uint64_t)J.nseq);
+    h = fnv(h, (uint64_t)J.params.flags);
+  }
+  return h;
+}
+
+std::string cache_path() {
+  const char *e = std::getenv("AXX_AUTOTUNE_CACHE");
+  if (e && *e) return e;
+  const char *home = std::getenv("HOME");
+  return std::string(home ? home : ".") + "/.cache/axonexa_gb300/autotune.tsv";
+}
+
+std::string device_key(axx_ctx *ctx) {
+  cudaDeviceProp p;
+  if (cudaGetDeviceProperties(&p, ctx->device) != cudaSuccess) return "unknown";
+  std::string n = p.name;
+  for (char &c : n)
+    if (c == ' ' || c == '\t') c = '_';
+  return n + "_sm" + std::to_string(p.major) + std::to_string(p.minor);
+}
+
+std::mutex g_cache_mu;
+
+bool cache_lookup(axx_ctx *ctx, uint64_t shape, axx_batch_options &o) {
+  std::lock_guard<std::mutex> lock(g_cache_mu);
+  std::ifstream f(cache_path());
+  if (!f) return false;
+  const std::string dev = device_key(ctx);
+  std::string line;
+  bool found = false;
+  while (std::getline(f, line)) {
+    std::istringstream ss(line);
+    std::string d;
+    unsigned long long h;
+    int tile, bps;
+    double ms;
+    if (ss >> d >> h >> tile >> bps >> ms && d == dev && h == shape) {
+      o.tile = tile;
+      o.blocks_per_sm = bps;
+      found = true;
+    }
+  }
+  return found;
+}
+
+// mkdir -p of the directory part of `path`
+void make_parent_dirs(const std::string &path) {
+  for (size_t i = 1; i < path.size(); ++i)
+    if (path[i] == '/') ::mkdir(path.substr(0, i).c_str(), 0755);
+}
+
+void cache_store(axx_ctx *ctx, uint64_t shape, const axx_batch_options &o, double ms) {
+  std::lock_guard<std::mutex> lock(g_cache_mu);
+  const std::string path = cache_path();
+  make_parent_dirs(path);
+  std::ofstream f(path, std::ios::app);
+  if (f)
+    f << device_key(ctx) << '\t' << (unsigned long long)shape << '\t' << o.tile << '\t'
+      << o.blocks_per_sm << '\t' << ms << '\n';
+}
+
+}  // namespace
+
+static axx_status batch_build(axx_ctx *ctx, const axx_job *jobs, int njobs,
+                              const axx_batch_options &opt, int steps_cap, axx_batch **out);
+
+extern "C" axx_status axx_autotune_batch(axx_ctx *ctx, const axx_job *jobs, int njobs,
+                                         int probe_steps, axx_batch_options *best,
+                                         double *best_ms) {
+  if (!ctx || !jobs || njobs < 1 || !best) return AXX_ERR_INVALID_ARG;
+  if (probe_steps < 2) probe_steps = 300;
+  const int tiles[] = {256, 512, 1024, 2048, 4096, 8192};
+  double bms = 1e300;
+  axx_batch_options bo{0, 0, 0};
+  for (int tile : tiles) {
+    for (int bsel = 0; bsel < 2; ++bsel) {
+      axx_batch_options o{tile, bsel == 0 ? 0 : -2, 0};
+      axx_batch *b = nullptr;
+      axx_status s = batch_build(ctx, jobs, njobs, o, probe_steps, &b);
+      if (s != AXX_OK) return s;
+      if (bsel == 1 && b->bps <= 1) {
+        axx_batch_destroy(b);
+        continue;
+      }
+      double ms = 1e300;
+      for (int r = 0; r < 3 && s == AXX_OK; ++r) {
+        cudaEventRecord(ctx->ev[6], ctx->stream);
+        s = axx_batch_launch(b);
+        cudaEventRecord(ctx->ev[7], ctx->stream);
+        cudaEventSynchronize(ctx->ev[7]);
+        float t = 0.f;
+        cudaEventElapsedTime(&t, ctx->ev[6], ctx->ev[7]);
+        if (r > 0) ms = std::min(ms, (double)t);
+      }
+      const int bps_used = b->bps;
+      axx_batch_destroy(b);
+      if (s != AXX_OK) return s;
+      if (ms < bms) {
+        bms = ms;
+        bo = axx_batch_options{tile, bps_used, 0};
+      }
+    }
+  }
+  *best = bo;
+  if (best_ms) *best_ms = bms;
+  cache_store(ctx, batch_shape(jobs, njobs), bo, bms);
+  return AXX_OK;
+}
+
+static axx_status batch_build(axx_ctx *ctx, const axx_job *jobs, int njobs,
+                              const axx_batch_options &opt, int steps_cap, axx_batch **out) {
+  *out = nullptr;
+  if (njobs < 1) return bfail(ctx, AXX_ERR_INVALID_ARG, "njobs must be >= 1");
+  cudaError_t e = cudaSetDevice(ctx->device);
+  if (e != cudaSuccess) return bcuda(ctx, e, "cudaSetDevice");
+  struct JobPlan {
+    GeomPlan g;
+    SeqPlan sq;
+    KernelTables kt;
+    InitSpec init;
+    axx_run_params p;
+    int mode;
+    double cell[3];
+  };
+  std::vector<JobPlan> jp(njobs);
+  int kmax = 1;
+  for (int j = 0; j < njobs; ++j) {
+    const axx_job &J = jobs[j];
+    JobPlan &q = jp[j];
+    q.p = J.params;
+    if (steps_cap > 0 && q.p.steps > steps_cap) q.p.steps = steps_cap;
+    q.mode = J.mode;
+    const axx_run_params &p = q.p;
+    if (p.num_walkers < 1 || p.steps < 1 || !(p.timestep > 0.0) || p.walker_offset < 0 ||
+        p.init_mode < 0 || p.init_mode > 2 || !std::isfinite(p.gamma) || p.gamma < 0.0)
+      return bfail(ctx, AXX_ERR_INVALID_ARG, "job " + std::to_string(j) + ": invalid run parameters");
+    if (p.flags & AXX_FLAG_SIMPLE_REJECTION)
+      return bfail(ctx, AXX_ERR_UNSUPPORTED, "batched jobs use specular reflection");
+    if (J.nseq > kBatchMaxSeq)
+      return bfail(ctx, AXX_ERR_INVALID_ARG, "a batched job has at most 64 sequences");
+    const double gamma = p.gamma > 0.0 ? p.gamma : kGammaDefault;
+    std::string err;
+    if (J.mode == AXX_MODE_SINGLE) {
+      if (p.flags & (AXX_FLAG_PERMEABLE | AXX_FLAG_RELAXATION))
+        return bfail(ctx, AXX_ERR_INVALID_ARG, "single-pore jobs have no permeability or relaxation");
+      float sp, st;
+      err = plan_single(J.basis, p.timestep, q.g, sp, st);
+      q.cell[0] = q.cell[1] = q.cell[2] = 1.0;
+    } else {
+      err = plan_lattice(&J.lattice, J.basis, J.nbasis, p.timestep, p.flags, q.g);
+      q.cell[0] = J.lattice.a;
+      q.cell[1] = J.lattice.b;
+      q.cell[2] = J.lattice.c;
+    }
+    if (err.empty()) err = plan_sequences(J.seqs, J.nseq, p.steps, p.timestep, gamma, q.sq);
+    if (!err.empty()) return bfail(ctx, AXX_ERR_INVALID_ARG, "job " + std::to_string(j) + ": " + err);
+    int k = 1;
+    while (k < (int)q.sq.channels.size()) k <<= 1;
+    kmax = std::max(kmax, k);
+  }
+  if (kmax > AXX_KMAX) return bfail(ctx, AXX_ERR_UNSUPPORTED, "more than 16 channels in a job");
+  size_t geo_max = 0;
+  std::vector<size_t> job_off(njobs);
+  size_t off = 0;
+  for (int j = 0; j < njobs; ++j) {
+    JobPlan &q = jp[j];
+    std::string err = make_kernel_tables(q.g, q.sq, jobs[j].nseq, q.p.steps, q.mode, q.p.flags,
+                                         q.kt, kmax);
+    if (err.empty()) err = init_spec(q.g, jobs[j].basis, jobs[j].nbasis, q.mode, &q.p, q.init);
+    if (!err.empty()) return bfail(ctx, AXX_ERR_INVALID_ARG, "job " + std::to_string(j) + ": " + err);
+    geo_max = std::max(geo_max, walk_smem_bytes(q.g, 0));
+    job_off[j] = off;
+    off = up256(off + arena_layout(q.g, q.kt, jobs[j].nseq).fixed);
+  }
+  const size_t p_bytes = (sizeof(WalkParams) + 15) & ~(size_t)15;
+  const size_t smem = p_bytes + (size_t)(AXX_BLOCK / 32) * kBatchMaxSeq * 5 * 8 + geo_max;
+  if (smem > AXX_SMEM_MAX) return bfail(ctx, AXX_ERR_UNSUPPORTED, "a job's substrate exceeds shared memory");
+  // work items, longest first
+  axx_batch_options o = opt;
+  if (o.tile == 0) {
+    const uint64_t shape = batch_shape(jobs, njobs);
+    if (!cache_lookup(ctx, shape, o)) {
+      double ms = 0.0;
+      axx_status s = axx_autotune_batch(ctx, jobs, njobs, 300, &o, &ms);
+      if (s != AXX_OK) return s;
+    }
+  }
+  if (o.tile <= 0 || o.tile % 128 != 0)
+    return bfail(ctx, AXX_ERR_INVALID_ARG, "tile must be a positive multiple of 128");
+  std::vector<BatchItem> items;
+  std::vector<int> job_items(njobs, 0);
+  std::vector<double> cost;
+  for (int j = 0; j < njobs; ++j) {
+    const long long n = jp[j].p.num_walkers;
+    for (long long f = 0; f < n; f += o.tile) {
+      BatchItem it;
+      it.job = j;
+      it.local = job_items[j]++;
+      it.first = f;
+      it.count = (int)std::min<long long>(o.tile, n - f);
+      it.pad = 0;
+      items.push_back(it);
+    }
+  }
+  std::vector<size_t> order(items.size());
+  for (size_t i = 0; i < order.size(); ++i) order[i] = i;
+  auto item_cost = [&](const BatchItem &it) {
+    const JobPlan &q = jp[it.job];
+    return (double)it.count * (double)q.p.steps * (1.0 + 0.05 * (double)q.g.geo.size());
+  };
+  std::stable_sort(order.begin(), order.end(),
+                   [&](size_t a, size_t b) { return item_cost(items[a]) > item_cost(items[b]); });
+  std::vector<BatchItem> sorted(items.size());
+  for (size_t i = 0; i < order.size(); ++i) sorted[i] = items[order[i]];
+  // partials and outputs
+  std::vector<long long> part_off(njobs), out_off(njobs);
+  long long npart = 0, nout = 0;
+  std::vector<int2> outmap;
+  for (int j = 0; j < njobs; ++j) {
+    part_off[j] = npart;
+    npart += (long long)job_items[j] * jobs[j].nseq * 5;
+    out_off[j] = nout;
+    for (int k = 0; k < jobs[j].nseq * 5; ++k) outmap.push_back(make_int2(j, k));
+    nout += jobs[j].nseq * 5;
+  }
+  // arena: job tables | jobs | items | outmap | job_items | counter | partials | out | counters
+  const size_t o_jobs = up256(off);
+  const size_t o_items = up256(o_jobs + sizeof(BatchJob) * njobs);
+  const size_t o_outmap = up256(o_items + sizeof(BatchItem) * sorted.size());
+  const size_t o_jitems = up256(o_outmap + sizeof(int2) * std::max<size_t>(outmap.size(), 1));
+  const size_t o_ctr = up256(o_jitems + 4 * njobs);
+  const size_t o_part = up256(o_ctr + 16);
+  const size_t o_out = up256(o_part + 8 * std::max<long long>(npart, 1));
+  const size_t o_cnt = up256(o_out + 8 * std::max<long long>(nout, 1));
+  const size_t total = up256(o_cnt + 8 * AXX_CNT_N * njobs);
+  auto *b = new axx_batch();
+  b->ctx = ctx;
+  b->njobs = njobs;
+  b->nitems = (int)sorted.size();
+  b->kmax = kmax;
+  b->tile = o.tile;
+  b->smem = smem;
+  b->nout = (int)nout;
+  b->use_graph = opt.use_graph != 0;
+  e = cudaMalloc(&b->arena, total);
+  if (e != cudaSuccess) {
+    delete b;
+    return bcuda(ctx, e, "cudaMalloc(batch arena)");
+  }
+  char *base = (char *)b->arena;
+  b->d_jobs = (BatchJob *)(base + o_jobs);
+  b->d_items = (BatchItem *)(base + o_items);
+  b->d_outmap = (int2 *)(base + o_outmap);
+  b->d_jobitems = (int *)(base + o_jitems);
+  b->d_ctr = (unsigned *)(base + o_ctr);
+  b->d_part = (double *)(base + o_part);
+  b->d_out = (double *)(base + o_out);
+  b->d_counters = (unsigned long long *)(base + o_cnt);
+  std::vector<BatchJob> hj(njobs);
+  for (int j = 0; j < njobs; ++j) {
+    JobPlan &q = jp[j];
+    const ArenaLayout L = arena_layout(q.g, q.kt, jobs[j].nseq);
+    char *jb = base + job_off[j];
+    e = upload_tables(jb, L, q.g, q.kt, ctx->stream);
+    if (e != cudaSuccess) break;
+    fill_walk_params(hj[j].P, jb, L, q.g, q.kt, &q.p, q.mode, jobs[j].nseq, q.init, q.cell,
+                     ctx->abort_dev);
+    hj[j].P.counters = b->d_counters + (size_t)AXX_CNT_N * j;
+    hj[j].one = (q.g.geom != AXX_GEOM_FREE && q.g.geo.size() == 1 && q.g.cstart.size() == 2) ? 1 : 0;
+    hj[j].M = jobs[j].nseq;
+    hj[j].part_off = part_off[j];
+    hj[j].out_off = out_off[j];
+    b->job_M.push_back(jobs[j].nseq);
+    const long long ws = q.p.num_walkers * (long long)(q.p.steps - 1);
+    b->job_ws.push_back(ws);
+    b->walker_steps += ws;
+  }
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(b->d_jobs, hj.data(), sizeof(BatchJob) * njobs, cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess && !sorted.empty())
+    e = cudaMemcpyAsync(b->d_items, sorted.data(), sizeof(BatchItem) * sorted.size(),
+                        cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess && !outmap.empty())
+    e = cudaMemcpyAsync(b->d_outmap, outmap.data(), sizeof(int2) * outmap.size(),
+                        cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(b->d_jobitems, job_items.data(), 4 * njobs, cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) {
+    axx_batch_destroy(b);
+    return bcuda(ctx, e, "uploading the batch tables");
+  }
+  const int occ = batch_occupancy(kmax, smem);
+  if (occ <= 0) {
+    axx_batch_destroy(b);
+    return bfail(ctx, AXX_ERR_CUDA, "batch kernel cannot be resident");
+  }
+  int bps = occ;
+  if (o.blocks_per_sm > 0) bps = std::min(occ, o.blocks_per_sm);
+  if (o.blocks_per_sm < 0) bps = std::max(1, occ + o.blocks_per_sm);
+  b->bps = bps;
+  b->grid = std::max(1, std::min(bps * ctx->nsm, b->nitems));
+  if (b->use_graph) {
+    // capture: reset the counters, the persistent walk, the reduction
+    cudaStream_t s = ctx->stream;
+    e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+      cudaMemsetAsync(b->d_ctr, 0, 16, s);
+      cudaMemsetAsync(b->d_counters, 0, 8 * AXX_CNT_N * njobs, s);
+      batch_go(kmax, b->grid, smem, s, b->d_jobs, b->d_items, b->nitems, b->d_ctr, b->d_part);
+      if (nout > 0)
+        batch_reduce_kernel<<<(int)nout, 256, 0, s>>>(b->d_jobs, b->d_outmap, b->d_jobitems,
+                                                      b->d_part, b->d_out);
+      e = cudaStreamEndCapture(s, &b->graph);
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec, b->graph, 0);
+    if (e != cudaSuccess) {
+      axx_batch_destroy(b);
+      return bcuda(ctx, e, "capturing the batch graph");
+    }
+  }
+  *out = b;
+  return AXX_OK;
+}
+
+extern "C" axx_status axx_batch_create(axx_ctx *ctx, const axx_job *jobs, int njobs,
+                                       const axx_batch_options *opt, axx_batch **out) {
+  if (!ctx || !jobs || !out) return AXX_ERR_INVALID_ARG;
+  axx_batch_options o = opt ? *opt : axx_batch_options{0, 0, 1};
+  return batch_build(ctx, jobs, njobs, o, 0, out);
+}
+
+extern "C" axx_status axx_batch_launch(axx_batch *b) {
+  if (!b) return AXX_ERR_INVALID_ARG;
+  axx_ctx *ctx = b->ctx;
+  *ctx->abort_host = 0;
+  cudaError_t e;
+  if (b->use_graph) {
+    e = cudaGraphLaunch(b->exec, ctx->stream);
+  } else {
+    cudaStream_t s = ctx->stream;
+    e = cudaMemsetAsync(b->d_ctr, 0, 16, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->d_counters, 0, 8 * AXX_CNT_N * b->njobs, s);
+    if (e == cudaSuccess)
+      e = batch_go(b->kmax, b->grid, b->smem, s, b->d_jobs, b->d_items, b->nitems, b->d_ctr,
+                   b->d_part);
+    if (e == cudaSuccess && b->nout > 0) {
+      batch_reduce_kernel<<<b->nout, 256, 0, s>>>(b->d_jobs, b->d_outmap, b->d_jobitems,
+                                                  b->d_part, b->d_out);
+      e = cudaGetLastError();
+    }
+  }
+  if (e != cudaSuccess) return bcuda(ctx, e, "axx_batch_launch");
+  b->launched = true;
+  return AXX_OK;
+}
+
+extern "C" axx_status axx_batch_read(axx_batch *b, double *mx, double *my, axx_stats *stats) {
+  if (!b) return AXX_ERR_INVALID_ARG;
+  axx_ctx *ctx = b->ctx;
+  if (!b->launched) return bfail(ctx, AXX_ERR_INVALID_ARG, "batch was never launched");
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  std::vector<double> h((size_t)b->nout);
+  std::vector<unsigned long long> cnt((size_t)AXX_CNT_N * b->njobs);
+  if (e == cudaSuccess && b->nout > 0)
+    e = cudaMemcpy(h.data(), b->d_out, 8 * h.size(), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(cnt.data(), b->d_counters, 8 * cnt.size(), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return bcuda(ctx, e, "axx_batch_read");
+  size_t o = 0, m0 = 0;
+  bool capped = false, aborted = false, initf = false;
+  for (int j = 0; j < b->njobs; ++j) {
+    const int M = b->job_M[j];
+    for (int m = 0; m < M; ++m) {
+      if (mx) mx[m0 + m] = h[o + m * 5 + 0];
+      if (my) my[m0 + m] = h[o + m * 5 + 1];
+      if (stats) {
+        if (stats[j].sxx) stats[j].sxx[m] = h[o + m * 5 + 2];
+        if (stats[j].syy) stats[j].syy[m] = h[o + m * 5 + 3];
+        if (stats[j].sxy) stats[j].sxy[m] = h[o + m * 5 + 4];
+      }
+    }
+    const unsigned long long *c = &cnt[(size_t)AXX_CNT_N * j];
+    if (stats) {
+      stats[j].reflection_cap_hits = (int64_t)c[AXX_CNT_CAP];
+      stats[j].walker_steps = b->job_ws[j];
+      stats[j].boundary_hits = (int64_t)c[AXX_CNT_HITS];
+    }
+    capped |= c[AXX_CNT_CAP] != 0;
+    aborted |= c[AXX_CNT_ABORTED] != 0;
+    initf |= c[AXX_CNT_INIT_FAIL] != 0;
+    o += (size_t)M * 5;
+    m0 += M;
+  }
+  if (aborted) return bfail(ctx, AXX_ERR_ABORTED, "batch aborted by axx_abort");
+  if (initf) return bfail(ctx, AXX_ERR_INVALID_ARG, "a job's start region is empty");
+  if (capped) return bfail(ctx, AXX_ERR_REFLECTION_CAP, "some moves hit the reflection cap of 1024");
+  return AXX_OK;
+}
+
+extern "C" axx_status axx_batch_info(const axx_batch *b, int *items, int *tile, int *bps,
+                                     int *kernel_launches, int64_t *walker_steps) {
+  if (!b) return AXX_ERR_INVALID_ARG;
+  if (items) *items = b->nitems;
+  if (tile) *tile = b->tile;
+  if (bps) *bps = b->bps;
+  if (kernel_launches) *kernel_launches = b->nout > 0 ? 2 : 1;
+  if (walker_steps) *walker_steps = b->walker_steps;
+  return AXX_OK;
+}
+
+extern "C" axx_status axx_batch_destroy(axx_batch *b) {
+  if (!b) return AXX_OK;
+  if (b->ctx) cudaStreamSynchronize(b->ctx->stream);
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  if (b->arena) cudaFree(b->arena);
+  delete b;
+  return AXX_OK;
+}
+
+extern "C" axx_status axx_run_batch(axx_ctx *ctx, const axx_job *jobs, int njobs,
+                                    const axx_batch_options *opt, double *mx, double *my,
+                                    axx_stats *stats) {
+  axx_batch *b = nullptr;
+  axx_status s = axx_batch_create(ctx, jobs, njobs, opt, &b);
+  if (s != AXX_OK) return s;
+  s = axx_batch_launch(b);
+  if (s == AXX_OK) s = axx_batch_read(b, mx, my, stats);
+  axx_batch_destroy(b);
+  return s;
+}

@@ -16,14 +16,15 @@ int walk_mode(int mode, int geom, uint32_t flags) {
 }
 
 std::string make_kernel_tables(const GeomPlan &g, const SeqPlan &sq, int M, int steps, int mode,
-                               uint32_t flags, KernelTables &kt) {
+                               uint32_t flags, KernelTables &kt, int min_kmax) {
   kt = KernelTables();
   kt.K = (int)sq.channels.size();
   if (kt.K > AXX_KMAX)
     return "more than 16 phase channels (distinct waveform x direction) in one walk";
   kt.km = walk_mode(mode, g.geom, flags);
   kt.kmax = 1;
-  while (kt.kmax < kt.K) kt.kmax <<= 1;
+  while (kt.kmax < kt.K || kt.kmax < min_kmax) kt.kmax <<= 1;
+  if (kt.kmax > AXX_KMAX) return "channel capacity above 16";
   const int km = kt.kmax;
   kt.wave_il.assign((size_t)steps * km, 0.f);
   for (int c = 0; c < kt.K; ++c) {

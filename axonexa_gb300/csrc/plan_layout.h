@@ -34,8 +34,9 @@ struct ArenaLayout {
 // Walk mode for a plan.
 int walk_mode(int mode, int geom, uint32_t flags);
 // Kernel-format tables (interleaved, padded channels) from the plans.
+// min_kmax pads the channel capacity further (a batch shares one capacity).
 std::string make_kernel_tables(const GeomPlan &g, const SeqPlan &sq, int M, int steps, int mode,
-                               uint32_t flags, KernelTables &kt);
+                               uint32_t flags, KernelTables &kt, int min_kmax = 1);
 // Dynamic shared memory of the walk kernel (per-warp sums + staged tables).
 size_t walk_smem_bytes(const GeomPlan &g, int M);
 ArenaLayout arena_layout(const GeomPlan &g, const KernelTables &kt, int M);

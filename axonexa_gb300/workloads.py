@@ -1,0 +1,127 @@
+"""Seeded synthetic workloads with the shapes of the benchmark configurations.
+
+Units are the reference's (mm, ms, T/mm).  No dataset is read: every input is
+drawn from a seeded generator.
+
+* free_box()          -- free diffusion in an empty periodic 50 um box, 65,536
+                         walkers, dt 5 us, 6,000 steps, PGSE delta 5 / Delta
+                         20 ms, 16 G values 0-300 mT/m along x.
+* one_cylinder()      -- one impermeable cylinder r 5 um in a 12 um cell,
+                         1,048,576 walkers, dt 2 us, T2 80/60 ms; PGSE delta
+                         10 / Delta 40 ms (25,000 steps), 32 G 0-200 mT/m, and
+                         cosine OGSE at 50/100/200 Hz (delta 20, Delta 40 ms).
+* gamma_pack()        -- 400 cylinders, gamma radii (k 5, mean 2.5 um) at area
+                         fraction 0.6, permeable kappa 0.02 um/ms, D 1.7/2.0,
+                         T2 80/60, dt 1 us, 64 sequences (PGSE, cosine and
+                         square-wave OGSE, G <= 300 mT/m, directions uniform on
+                         the sphere).
+* batch_256()         -- 256 substrates from a seed: single cylinder (r 1-8 um),
+                         single sphere (r 2-10 um) or hexagonal pack (f 0.4-0.7,
+                         kappa 0-0.05 um/ms); walkers log-uniform 1e4-1e6;
+                         8-64 sequences (PGSE, cosine and square-wave OGSE).
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from .acquisition import CosGFunc, Cylinder_XY, Lattice, RectGrad, Sphere, SWOGSEFunc
+from .batch import Job
+from .substrate import hex_cell, rps_gamma_pack
+
+UM = 1e-3      # mm per um
+D1 = 1e-6      # mm^2/ms per um^2/ms
+MTM = 1e-6     # T/mm per mT/m
+KAPPA = 1e-3   # mm/ms per um/ms
+
+
+def free_box():
+    s = 50 * UM
+    lat = Lattice(s, s, s, 0.0, 0.0, 2.0 * D1, 0)
+    seqs = [RectGrad(g * MTM, 5.0, 15.0) for g in np.linspace(0, 300, 16)]
+    return dict(lattice=lat, basis=[], seqs=seqs, num_walkers=65536, steps=6000,
+                timestep=0.005, seed=1234)
+
+
+def one_cylinder():
+    c, r = 12 * UM, 5 * UM
+    lat = Lattice(c, c, c, 60.0, 0.0, 2.0 * D1, 1)
+    cyl = [Cylinder_XY(c / 2, c / 2, r, 80.0, 0.0, 2.0 * D1, 1, 0.0)]
+    pgse = [RectGrad(g * MTM, 10.0, 30.0) for g in np.linspace(0, 200, 32)]
+    ogse = [CosGFunc(100 * MTM, 20.0, 20.0, n) for n in (1, 2, 4)]
+    return dict(lattice=lat, basis=cyl, acquisitions=[(pgse, 25000), (ogse, 30000)],
+                num_walkers=1 << 20, timestep=0.002, seed=1234)
+
+
+def random_directions(n, rng):
+    v = rng.normal(size=(n, 3))
+    return v / np.linalg.norm(v, axis=1, keepdims=True)
+
+
+def gamma_pack(seed=7, n_cyl=400, walkers=1 << 22):
+    lat, cyl, f = rps_gamma_pack(seed, n_cyl, 5.0, 2.5 * UM, 0.6, D_in=1.7 * D1, T2_in=80.0,
+                                 D_ex=2.0 * D1, T2_ex=60.0, permeability=0.02 * KAPPA)
+    rng = np.random.default_rng(seed)
+    # four waveforms, sixteen (G, direction) pairs each
+    waves = [("pgse", 10.0, 30.0, 0), ("cos", 20.0, 5.0, 2), ("cos", 20.0, 5.0, 4),
+             ("sw", 20.0, 5.0, 2)]
+    seqs = []
+    for kind, d, sp, n in waves:
+        for g, u in zip(rng.uniform(0, 300, 16), random_directions(16, rng)):
+            if kind == "pgse":
+                q = RectGrad(g * MTM, d, sp)
+                q.ghat = tuple(u)
+            elif kind == "cos":
+                q = CosGFunc(g * MTM, d, sp, n, tuple(u))
+            else:
+                q = SWOGSEFunc(g * MTM, d, sp, n, tuple(u))
+            seqs.append(q)
+    te = max(2 * d + sp for _, d, sp, _ in waves)
+    return dict(lattice=lat, basis=cyl, seqs=seqs, num_walkers=walkers,
+                steps=int(round(te / 0.001)), timestep=0.001, seed=seed, fraction=f)
+
+
+def batch_256(seed=2026, n_sub=256, timestep=0.005, walker_scale=1.0, max_steps=None):
+    """Jobs of the uneven 256-substrate batch."""
+    rng = np.random.default_rng(seed)
+    menu = [("pgse", 5.0, 15.0, 0), ("pgse", 10.0, 20.0, 0), ("cos", 20.0, 5.0, 1),
+            ("cos", 20.0, 5.0, 2), ("cos", 20.0, 5.0, 4), ("sw", 20.0, 5.0, 2)]
+    jobs = []
+    for s in range(n_sub):
+        kind = int(rng.integers(3))
+        nw = int(round(10 ** rng.uniform(4, 6) * walker_scale))
+        nseq = int(rng.integers(8, 65))
+        picks = rng.integers(len(menu), size=nseq)
+        G = rng.uniform(0, 300, size=nseq)
+        seqs = []
+        for k, g in zip(picks, G):
+            w, d, sp, n = menu[int(k)]
+            if w == "pgse":
+                seqs.append(RectGrad(g * MTM, d, sp))
+            elif w == "cos":
+                seqs.append(CosGFunc(g * MTM, d, sp, n))
+            else:
+                seqs.append(SWOGSEFunc(g * MTM, d, sp, n))
+        te = max(2 * menu[int(k)][1] + menu[int(k)][2] for k in picks)
+        steps = int(round(te / timestep))
+        if max_steps:
+            steps = min(steps, max_steps)
+        if kind == 0:
+            r = rng.uniform(1, 8) * UM
+            job = Job([Cylinder_XY(0.0, 0.0, r, 0.0, 0.0, 2.0 * D1, 1, 0.0)], seqs, nw, steps,
+                      timestep, seed * 1000 + s)
+        elif kind == 1:
+            r = rng.uniform(2, 10) * UM
+            job = Job([Sphere(0.0, 0.0, 0.0, r, 0.0, 0.0, 2.0 * D1, 1, 0.0)], seqs, nw, steps,
+                      timestep, seed * 1000 + s)
+        else:
+            f = rng.uniform(0.4, 0.7)
+            kappa = rng.uniform(0.0, 0.05) * KAPPA
+            r = rng.uniform(1.5, 4.0) * UM
+            lat, cyl = hex_cell(r, f, D_in=1.7 * D1, T2_in=80.0, D_ex=2.0 * D1, T2_ex=60.0,
+                                permeability=kappa)
+            job = Job(cyl, seqs, nw, steps, timestep, seed * 1000 + s, lattice=lat,
+                      relaxation=True, permeable=kappa > 0)
+        jobs.append(job)
+    return jobs
