@@ -120,6 +120,20 @@ _SIGS = {
                        C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(Stats)], C.c_int),
     "axx_autotune_batch": ([C.c_void_p, C.POINTER(Job), C.c_int, C.c_int,
                             C.POINTER(BatchOptions), C.POINTER(C.c_double)], C.c_int),
+    "axx_mlp_create": ([C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_uint64,
+                        C.POINTER(C.c_void_p)], C.c_int),
+    "axx_mlp_destroy": ([C.c_void_p], C.c_int),
+    "axx_mlp_num_params": ([C.c_void_p, C.POINTER(C.c_int64)], C.c_int),
+    "axx_mlp_get_params": ([C.c_void_p, C.POINTER(C.c_float)], C.c_int),
+    "axx_mlp_set_params": ([C.c_void_p, C.POINTER(C.c_float)], C.c_int),
+    "axx_mlp_gradients": ([C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int,
+                           C.POINTER(C.c_float), C.POINTER(C.c_float)], C.c_int),
+    "axx_mlp_train": ([C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int, C.c_int,
+                       C.c_int, C.c_float, C.c_uint64, C.POINTER(C.c_float)], C.c_int),
+    "axx_mlp_predict": ([C.c_void_p, C.POINTER(C.c_float), C.c_int, C.POINTER(C.c_float)],
+                        C.c_int),
+    "axx_mlp_predict_device": ([C.c_void_p, C.c_void_p, C.c_int, C.c_void_p], C.c_int),
+    "axx_mlp_flops_per_row": ([C.c_void_p, C.POINTER(C.c_double)], C.c_int),
     "axx_bvalue": ([C.POINTER(SequenceRec), C.c_double, C.POINTER(C.c_double)], C.c_int),
     "axx_gradient_eval": ([C.POINTER(SequenceRec), C.POINTER(C.c_double), C.c_int,
                            C.POINTER(C.c_double)], C.c_int),

@@ -31,6 +31,8 @@ CUDA_SOURCES = [
     "misc_kernels.cu",
     "noalloc.cu",
     "batch.cu",
+    "mlp.cu",
+    "mlp_tc.cu",
 ]
 HOST_SOURCES = ["api.cpp", "host_plan.cpp", "plan_layout.cpp", "substrate.cpp"]
 

@@ -1,0 +1,252 @@
+"""Learned surrogate of the walk: an MLP from substrate and sequence
+parameters to the signal, trained on signals the simulator produces.
+
+Inputs (10): mean radius [um], gamma shape, intracellular area fraction,
+kappa [um/ms], D_in, D_ex [um^2/ms], G [mT/m], Delta, delta [ms], omega [Hz]
+(omega = 0: PGSE; otherwise cosine OGSE with omega*delta whole periods).
+Output: the normalised signal |M|/N.
+
+The network (MLP in -> 4 x 256 SiLU -> 1) lives in libaxx.so: BF16 tensor-core
+training (mma.sync GEMMs, FP32 accumulate, Adam) and tcgen05 inference.  Plain
+Monte Carlo stays the fallback: queries outside the training ranges are
+simulated, not predicted.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass
+from typing import Dict, List, Optional, Tuple
+
+import numpy as np
+
+from . import _native as N
+from .acquisition import CosGFunc, Device, Lattice, RectGrad, default_device
+from .batch import Job, run_batch
+from .substrate import rps_gamma_pack
+
+INPUTS = ("mean_radius_um", "gamma_shape", "fraction", "kappa_um_ms", "D_in", "D_ex", "G_mTm",
+          "Delta_ms", "delta_ms", "omega_hz")
+# training ranges around the 400-cylinder permeable substrate (mean radius
+# 2.5 um, shape 5, f 0.6, kappa 0.02, D 1.7 / 2.0) and its sequences
+RANGES = np.array([[1.5, 3.5], [3.0, 8.0], [0.40, 0.65], [0.0, 0.05], [1.2, 2.2], [1.6, 2.6],
+                   [0.0, 300.0], [20.0, 40.0], [5.0, 15.0], [0.0, 400.0]])
+T2_IN, T2_EX = 80.0, 60.0
+
+
+class MLP:
+    """axx_mlp: in_dim -> depth x 256 SiLU -> 1."""
+
+    def __init__(self, in_dim=10, width=256, depth=4, seed=0, device: Device = None):
+        self.dev = device or default_device()
+        h = C.c_void_p()
+        N.check(N.lib().axx_mlp_create(self.dev.h, in_dim, width, depth, seed, C.byref(h)),
+                self.dev.h)
+        self.h = h
+        self.in_dim, self.width, self.depth = in_dim, width, depth
+        n = C.c_int64()
+        N.check(N.lib().axx_mlp_num_params(h, C.byref(n)))
+        self.nparam = n.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            N.lib().axx_mlp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def _f(a):
+        a = np.ascontiguousarray(a, dtype=np.float32)
+        return a, a.ctypes.data_as(C.POINTER(C.c_float))
+
+    def get_params(self) -> np.ndarray:
+        p = np.zeros(self.nparam, np.float32)
+        N.check(N.lib().axx_mlp_get_params(self.h, p.ctypes.data_as(C.POINTER(C.c_float))),
+                self.dev.h)
+        return p
+
+    def set_params(self, p):
+        p, ptr = self._f(p)
+        N.check(N.lib().axx_mlp_set_params(self.h, ptr), self.dev.h)
+
+    def layers(self, p=None):
+        """[(W [out][in], b [out]), ...] views of a parameter vector."""
+        p = self.get_params() if p is None else p
+        out, o = [], 0
+        for l in range(self.depth + 1):
+            i = self.in_dim if l == 0 else self.width
+            od = 1 if l == self.depth else self.width
+            W = p[o:o + od * i].reshape(od, i)
+            o += od * i
+            b = p[o:o + od]
+            o += od
+            out.append((W, b))
+        return out
+
+    def gradients(self, X, y):
+        X, px = self._f(X)
+        y, py = self._f(y)
+        g = np.zeros(self.nparam, np.float32)
+        loss = C.c_float()
+        N.check(N.lib().axx_mlp_gradients(self.h, px, py, len(y),
+                                          g.ctypes.data_as(C.POINTER(C.c_float)),
+                                          C.byref(loss)), self.dev.h)
+        return g, loss.value
+
+    def train(self, X, y, batch=4096, steps=1000, lr=1e-3, seed=0):
+        X, px = self._f(X)
+        y, py = self._f(y)
+        loss = np.zeros(max(steps, 1), np.float32)
+        N.check(N.lib().axx_mlp_train(self.h, px, py, len(y), batch, steps, lr, seed,
+                                      loss.ctypes.data_as(C.POINTER(C.c_float))), self.dev.h)
+        return loss[:steps]
+
+    def predict(self, X) -> np.ndarray:
+        X, px = self._f(X)
+        y = np.zeros(len(X), np.float32)
+        N.check(N.lib().axx_mlp_predict(self.h, px, len(X),
+                                        y.ctypes.data_as(C.POINTER(C.c_float))), self.dev.h)
+        return y
+
+    def predict_device(self, dX_ptr: int, n: int, dy_ptr: int):
+        N.check(N.lib().axx_mlp_predict_device(self.h, C.c_void_p(dX_ptr), n,
+                                               C.c_void_p(dy_ptr)), self.dev.h)
+
+    def flops_per_row(self) -> float:
+        f = C.c_double()
+        N.check(N.lib().axx_mlp_flops_per_row(self.h, C.byref(f)))
+        return f.value
+
+
+def normalise(P: np.ndarray) -> np.ndarray:
+    """Parameters -> [-1, 1] per input."""
+    lo, hi = RANGES[:, 0], RANGES[:, 1]
+    return (2.0 * (np.asarray(P, np.float64) - lo) / (hi - lo) - 1.0).astype(np.float32)
+
+
+def in_range(P: np.ndarray) -> np.ndarray:
+    P = np.asarray(P, np.float64)
+    return np.all((P >= RANGES[:, 0] - 1e-9) & (P <= RANGES[:, 1] + 1e-9), axis=1)
+
+
+def _sequence(G, Delta, delta, omega):
+    """PGSE (omega 0) or cosine OGSE with round(omega*delta) periods; G mT/m."""
+    if omega <= 0.0:
+        return RectGrad(G * 1e-6, delta, Delta - delta)
+    n = max(1, int(round(omega * delta * 1e-3)))
+    return CosGFunc(G * 1e-6, delta, Delta - delta, n)
+
+
+def snap_omega(omega, delta):
+    """The frequency a sequence actually has (whole periods per lobe)."""
+    if omega <= 0.0:
+        return 0.0
+    n = max(1, int(round(omega * delta * 1e-3)))
+    return n / (delta * 1e-3)
+
+
+@dataclass
+class SubstrateDraw:
+    mean_radius: float
+    shape: float
+    fraction: float
+    kappa: float
+    D_in: float
+    D_ex: float
+
+
+def draw_substrates(n, rng) -> List[SubstrateDraw]:
+    out = []
+    for _ in range(n):
+        v = [rng.uniform(lo, hi) for lo, hi in RANGES[:6]]
+        out.append(SubstrateDraw(*v))
+    return out
+
+
+def make_jobs(subs: List[SubstrateDraw], rng, walkers: int, timestep: float,
+              n_cyl: int = 100, waves_per_sub: int = 8, g_per_wave: int = 8):
+    """One batch job per substrate: `waves_per_sub` waveforms (Delta, delta,
+    omega) x `g_per_wave` amplitudes.  Returns (jobs, parameter rows)."""
+    jobs, rows = [], []
+    for k, s in enumerate(subs):
+        lat, cyl, f = rps_gamma_pack(int(rng.integers(1 << 31)), n_cyl, s.shape,
+                                     s.mean_radius * 1e-3, s.fraction, D_in=s.D_in * 1e-6,
+                                     T2_in=T2_IN, D_ex=s.D_ex * 1e-6, T2_ex=T2_EX,
+                                     permeability=s.kappa * 1e-3)
+        seqs, te = [], 0.0
+        for _ in range(waves_per_sub):
+            Delta = rng.uniform(*RANGES[7])
+            delta = min(rng.uniform(*RANGES[8]), Delta - 1.0)
+            omega = 0.0 if rng.uniform() < 0.25 else snap_omega(rng.uniform(20.0, RANGES[9][1]), delta)
+            if omega > RANGES[9][1]:
+                omega = 0.0
+            te = max(te, Delta + delta)
+            for G in rng.uniform(*RANGES[6], size=g_per_wave):
+                seqs.append(_sequence(G, Delta, delta, omega))
+                rows.append([s.mean_radius, s.shape, f, s.kappa, s.D_in, s.D_ex, G, Delta,
+                             delta, omega])
+        steps = int(math.ceil(te / timestep)) + 1
+        jobs.append(Job(cyl, seqs, walkers, steps, timestep, int(rng.integers(1 << 31)),
+                        lattice=lat, relaxation=True, permeable=s.kappa > 0))
+    return jobs, np.array(rows)
+
+
+def simulate(jobs: List[Job], device: Device = None, chunk: int = 64) -> np.ndarray:
+    """Normalised signals |M|/N of every sequence of every job (plain MC)."""
+    out = []
+    for i in range(0, len(jobs), chunk):
+        for r in run_batch(jobs[i:i + chunk], device=device):
+            out.append(r.signal)
+    return np.concatenate(out) if out else np.zeros(0)
+
+
+def generate(n_sub: int, seed: int, walkers: int = 262144, timestep: float = 0.005,
+             n_cyl: int = 100, device: Device = None):
+    """(parameters [n][10], signals [n]) from n_sub substrates x 64 sequences."""
+    rng = np.random.default_rng(seed)
+    subs = draw_substrates(n_sub, rng)
+    jobs, P = make_jobs(subs, rng, walkers, timestep, n_cyl)
+    S = simulate(jobs, device=device)
+    return P, S
+
+
+class Surrogate:
+    """Trained network plus the Monte Carlo fallback for out-of-range queries."""
+
+    def __init__(self, mlp: MLP):
+        self.mlp = mlp
+
+    @classmethod
+    def fit(cls, P, S, steps=4000, batch=4096, lr=1e-3, seed=0, device=None):
+        mlp = MLP(seed=seed, device=device)
+        loss = mlp.train(normalise(P), np.asarray(S, np.float32), batch=batch, steps=steps,
+                         lr=lr, seed=seed)
+        s = cls(mlp)
+        s.loss = loss
+        return s
+
+    def predict(self, P, fallback_walkers: int = 262144, timestep: float = 0.005,
+                device: Device = None) -> Tuple[np.ndarray, np.ndarray]:
+        """Signals for parameter rows; rows outside the training ranges are
+        simulated.  Returns (signals, used_fallback mask)."""
+        P = np.asarray(P, np.float64)
+        ok = in_range(P)
+        out = np.zeros(len(P))
+        if ok.any():
+            out[ok] = self.mlp.predict(normalise(P[ok]))
+        if (~ok).any():
+            rng = np.random.default_rng(0)
+            for i in np.nonzero(~ok)[0]:
+                p = P[i]
+                sub = SubstrateDraw(*p[:6])
+                jobs, _ = make_jobs([sub], rng, fallback_walkers, timestep, waves_per_sub=1,
+                                    g_per_wave=1)
+                jobs[0].seqs = [_sequence(p[6], p[7], p[8], p[9])]
+                jobs[0].steps = int(math.ceil((p[7] + p[8]) / timestep)) + 1
+                out[i] = simulate(jobs, device=device)[0]
+        return out, ~ok

@@ -282,6 +282,38 @@ axx_status axx_run_batch(axx_ctx *ctx, const axx_job *jobs, int njobs,
 axx_status axx_autotune_batch(axx_ctx *ctx, const axx_job *jobs, int njobs, int probe_steps,
                               axx_batch_options *best, double *best_ms);
 
+/* ---- learned surrogate: MLP in -> depth x width (SiLU) -> 1 -------------- */
+
+/* No reference counterpart: the reference has no learned component.  A small
+ * MLP maps substrate and sequence parameters to the signal; it is trained on
+ * signals the walk above produces and runs on the tensor cores in BF16 with
+ * FP32 accumulation.  Inputs are standardised by the caller. */
+typedef struct axx_mlp axx_mlp;
+
+axx_status axx_mlp_create(axx_ctx *ctx, int in_dim, int width, int depth, uint64_t seed,
+                          axx_mlp **out);
+axx_status axx_mlp_destroy(axx_mlp *m);
+/* Number of parameters and FP32 copies of them (weights then biases per
+ * layer, weights row-major [out][in]). */
+axx_status axx_mlp_num_params(const axx_mlp *m, int64_t *n);
+axx_status axx_mlp_get_params(axx_mlp *m, float *params);
+axx_status axx_mlp_set_params(axx_mlp *m, const float *params);
+/* Mean-squared-error gradients of one batch (host X[n][in_dim], y[n]); grads
+ * has axx_mlp_num_params entries; *loss receives the batch loss. */
+axx_status axx_mlp_gradients(axx_mlp *m, const float *X, const float *y, int n, float *grads,
+                             float *loss);
+/* Adam training on the device: `steps` updates with batches of `batch` rows
+ * drawn (seeded) from the n training pairs; loss_out (optional, steps
+ * entries) receives each batch loss. */
+axx_status axx_mlp_train(axx_mlp *m, const float *X, const float *y, int n, int batch, int steps,
+                         float lr, uint64_t seed, float *loss_out);
+/* Predictions for host inputs (X[n][in_dim] -> y[n]) on the tensor cores. */
+axx_status axx_mlp_predict(axx_mlp *m, const float *X, int n, float *y);
+/* Device-resident prediction for timing: X and y are device pointers. */
+axx_status axx_mlp_predict_device(axx_mlp *m, const float *dX, int n, float *dy);
+/* FLOPs of one forward row (2 per multiply-add). */
+axx_status axx_mlp_flops_per_row(const axx_mlp *m, double *flops);
+
 /* ---- sequences ----------------------------------------------------------- */
 
 /* b-value of one sequence, as the reference functor's getB(). */
