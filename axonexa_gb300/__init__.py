@@ -9,7 +9,7 @@ from .acquisition import (GAMMA, PI, ApodCosGFunc, CosGFunc, Cylinder_XY, Device
                           default_device, linear_regression, phaseAcquisition,
                           phaseAcquisitionStream, philox_words, run_lattice, run_single,
                           trace_lattice, trace_single)
-from .substrate import rps_gamma_pack, hex_cell
+from .substrate import gamma_quantile_radii, hex_cell, pack_radii, rps_gamma_pack
 from .batch import Batch, Job, autotune, run_batch
 
 __all__ = [n for n in dir() if not n.startswith("_")]

@@ -12,6 +12,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libaxx.so")
 
 AXX_OK = 0
+AXX_ERR_REFLECTION_CAP = 3
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "reflection cap hit",
           4: "timeout", 5: "no CUDA device", 6: "out of device memory", 7: "aborted",
           8: "unsupported", 9: "non-finite value"}
@@ -150,6 +151,10 @@ _SIGS = {
                                  C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
                                  C.c_int, C.POINTER(Basis), C.POINTER(C.c_int),
                                  C.POINTER(C.c_double), C.POINTER(C.c_double)], C.c_int),
+    "axx_substrate_pack": ([C.c_uint64, C.c_int, C.POINTER(C.c_double), C.c_double, C.c_double,
+                            C.c_double, C.c_double, C.c_int, C.POINTER(Basis),
+                            C.POINTER(C.c_int), C.POINTER(C.c_double),
+                            C.POINTER(C.c_double)], C.c_int),
 }
 
 _lib = None
@@ -182,7 +187,7 @@ def check(status: int, ctx=None) -> None:
     if ctx is not None:
         raw = lib().axx_last_error(ctx)
         msg = raw.decode() if raw else ""
-    if status == 3:
+    if status == AXX_ERR_REFLECTION_CAP:
         raise ReflectionCapError(status, msg)
     raise AxxError(status, msg)
 

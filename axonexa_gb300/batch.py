@@ -75,7 +75,10 @@ class Batch:
         return dict(items=it.value, tile=tile.value, blocks_per_sm=bps.value,
                     kernel_launches=kl.value, walker_steps=ws.value)
 
-    def read(self) -> List[RunResult]:
+    def read(self, max_cap_fraction: float = 0.0) -> List[RunResult]:
+        """Signals of every job.  Moves that hit the reflection cap raise
+        ReflectionCapError unless they are at most `max_cap_fraction` of the
+        batch's walker-steps (each result's `cap_hits` holds its count)."""
         tot = sum(self.rec.nseq)
         mx, my = np.zeros(max(tot, 1)), np.zeros(max(tot, 1))
         bufs = [[np.zeros(max(m, 1)) for _ in range(3)] for m in self.rec.nseq]
@@ -83,8 +86,14 @@ class Batch:
         for j, b in enumerate(bufs):
             p = [x.ctypes.data_as(C.POINTER(C.c_double)) for x in b]
             st[j] = N.Stats(p[0], p[1], p[2], 0, 0, 0)
-        N.check(N.lib().axx_batch_read(self.h, mx.ctypes.data_as(C.POINTER(C.c_double)),
-                                       my.ctypes.data_as(C.POINTER(C.c_double)), st), self.dev.h)
+        status = N.lib().axx_batch_read(self.h, mx.ctypes.data_as(C.POINTER(C.c_double)),
+                                        my.ctypes.data_as(C.POINTER(C.c_double)), st)
+        if status == N.AXX_ERR_REFLECTION_CAP and max_cap_fraction > 0.0:
+            caps = sum(st[j].reflection_cap_hits for j in range(self.rec.n))
+            steps = sum(st[j].walker_steps for j in range(self.rec.n))
+            if caps <= max_cap_fraction * steps:
+                status = 0
+        N.check(status, self.dev.h)
         out, o = [], 0
         for j, m in enumerate(self.rec.nseq):
             b = bufs[j]
@@ -106,11 +115,11 @@ class Batch:
             pass
 
 
-def run_batch(jobs: List[Job], **kw) -> List[RunResult]:
+def run_batch(jobs: List[Job], max_cap_fraction: float = 0.0, **kw) -> List[RunResult]:
     b = Batch(jobs, **kw)
     try:
         b.launch()
-        return b.read()
+        return b.read(max_cap_fraction)
     finally:
         b.close()
 

@@ -9,7 +9,8 @@
 // chosen so that the cylinders' area fraction is the requested one.  When
 // random sequential addition cannot place every cylinder at that density
 // (its jamming limit is near 0.55 for equal discs), the centres are relaxed
-// by pairwise periodic overlap removal until no two cylinders overlap.
+// by pairwise periodic overlap removal until no two cylinders overlap.  Every
+// pair keeps a gap of 1 % of its radius sum (kGap).
 //
 // Randomness: SplitMix64 (Steele, Lea, Flood, OOPSLA 2014) for uniforms,
 // Box-Muller normals, and the Marsaglia-Tsang (ACM TOMS 26(3), 2000) gamma
@@ -58,20 +59,25 @@ struct SplitMix {
 
 double min_image(double d, double L) { return d - L * std::nearbyint(d / L); }
 
+// Minimum separation of two cylinders, relative to the sum of their radii.
+// Touching cylinders form wedges in which a reflected walker never runs out
+// of boundary hits; a 1 % gap keeps every wedge open.
+constexpr double kGap = 1.01;
+
 bool overlaps(const std::vector<double> &x, const std::vector<double> &y,
               const std::vector<double> &r, int i, int upto, double L) {
   for (int j = 0; j < upto; ++j) {
     if (j == i) continue;
     const double dx = min_image(x[i] - x[j], L), dy = min_image(y[i] - y[j], L);
-    const double s = r[i] + r[j];
+    const double s = (r[i] + r[j]) * kGap;
     if (dx * dx + dy * dy < s * s) return true;
   }
   return false;
 }
 
-// Pairwise overlap removal: each overlapping pair moves apart along its
-// centre line by half the overlap (plus 0.1 %).  Returns true when no pair
-// overlaps.
+// Pairwise overlap removal: each pair closer than the minimum separation
+// moves apart along its centre line by half the shortfall (plus 0.1 %).
+// Returns true when every pair is separated.
 bool relax(std::vector<double> &x, std::vector<double> &y, const std::vector<double> &r,
            double L, int iters) {
   const int n = (int)x.size();
@@ -80,7 +86,7 @@ bool relax(std::vector<double> &x, std::vector<double> &y, const std::vector<dou
     for (int i = 0; i < n; ++i)
       for (int j = i + 1; j < n; ++j) {
         double dx = min_image(x[i] - x[j], L), dy = min_image(y[i] - y[j], L);
-        const double s = r[i] + r[j];
+        const double s = (r[i] + r[j]) * kGap;
         double d2 = dx * dx + dy * dy;
         if (d2 >= s * s) continue;
         any = true;
@@ -118,24 +124,18 @@ bool circle_meets_cell(double x, double y, double r, double L) {
 
 }  // namespace
 
-extern "C" axx_status axx_substrate_rps_gamma(uint64_t seed, int n, double shape, double mean,
-                                              double rmin, double rmax, double fraction,
-                                              double D_in, double T2_in, double permeability,
-                                              int max_out, axx_basis *out, int *nout,
-                                              double *side, double *achieved) {
-  if (n < 1 || n > 20000 || !(shape > 0.0) || !(mean > 0.0) || !(rmax > rmin) ||
-      !(fraction > 0.0 && fraction < 0.9) || !out || !nout || !side || !achieved || max_out < n)
+extern "C" axx_status axx_substrate_pack(uint64_t seed, int n, const double *radii,
+                                         double fraction, double D_in, double T2_in,
+                                         double permeability, int max_out, axx_basis *out,
+                                         int *nout, double *side, double *achieved) {
+  if (n < 1 || n > 20000 || !radii || !(fraction > 0.0 && fraction < 0.9) || !out || !nout ||
+      !side || !achieved || max_out < n)
     return AXX_ERR_INVALID_ARG;
-  SplitMix rng{seed * 0x2545F4914F6CDD1Dull + 0x1234567ull};
-  std::vector<double> r(n);
-  for (int i = 0; i < n; ++i) {
-    double d;
-    do {
-      d = rng.gamma(shape, mean / shape);
-    } while (!(d > rmin && d < rmax));
-    r[i] = d;
-  }
+  std::vector<double> r(radii, radii + n);
+  for (double v : r)
+    if (!(v > 0.0) || !std::isfinite(v)) return AXX_ERR_INVALID_ARG;
   std::sort(r.begin(), r.end());
+  SplitMix rng{seed * 0x2545F4914F6CDD1Dull + 0x7654321ull};
   double area = 0.0;
   for (double v : r) area += 3.141592653589793 * v * v;
   const double L = std::sqrt(area / fraction);
@@ -211,4 +211,24 @@ extern "C" axx_status axx_substrate_rps_gamma(uint64_t seed, int n, double shape
   *side = L;
   *achieved = area / (L * L);
   return AXX_OK;
+}
+
+extern "C" axx_status axx_substrate_rps_gamma(uint64_t seed, int n, double shape, double mean,
+                                              double rmin, double rmax, double fraction,
+                                              double D_in, double T2_in, double permeability,
+                                              int max_out, axx_basis *out, int *nout,
+                                              double *side, double *achieved) {
+  if (n < 1 || n > 20000 || !(shape > 0.0) || !(mean > 0.0) || !(rmax > rmin))
+    return AXX_ERR_INVALID_ARG;
+  SplitMix rng{seed * 0x2545F4914F6CDD1Dull + 0x1234567ull};
+  std::vector<double> r(n);
+  for (int i = 0; i < n; ++i) {
+    double d;
+    do {
+      d = rng.gamma(shape, mean / shape);
+    } while (!(d > rmin && d < rmax));
+    r[i] = d;
+  }
+  return axx_substrate_pack(rng.next(), n, r.data(), fraction, D_in, T2_in, permeability,
+                            max_out, out, nout, side, achieved);
 }

@@ -5,6 +5,8 @@ from __future__ import annotations
 import ctypes as C
 import math
 
+import numpy as np
+
 from . import _native as N
 from .acquisition import Cylinder_XY, Lattice
 
@@ -24,6 +26,33 @@ def rps_gamma_pack(seed: int, n: int, shape: float, mean: float, fraction: float
     N.check(N.lib().axx_substrate_rps_gamma(seed, n, shape, mean, rmin, rmax, fraction, D_in,
                                             T2_in, permeability, cap, out, C.byref(nout),
                                             C.byref(side), C.byref(ach)))
+    return _packing(out, nout, side, ach, T2_ex, D_ex)
+
+
+def pack_radii(seed: int, radii, fraction: float, *, D_in: float, T2_in: float, D_ex: float,
+               T2_ex: float, permeability: float = 0.0):
+    """The placement step of rps_gamma_pack for given radii
+    (axx_substrate_pack).  Same return value."""
+    r = np.ascontiguousarray(radii, dtype=np.float64)
+    cap = len(r) * 9
+    out = (N.Basis * cap)()
+    nout, side, ach = C.c_int(), C.c_double(), C.c_double()
+    N.check(N.lib().axx_substrate_pack(seed, len(r), r.ctypes.data_as(C.POINTER(C.c_double)),
+                                       fraction, D_in, T2_in, permeability, cap, out,
+                                       C.byref(nout), C.byref(side), C.byref(ach)))
+    return _packing(out, nout, side, ach, T2_ex, D_ex)
+
+
+def gamma_quantile_radii(n: int, shape: float, mean: float) -> np.ndarray:
+    """n radii at the mid-quantiles (i + 1/2)/n of gamma(shape, mean/shape):
+    a packing whose radius distribution is the gamma law itself rather than a
+    random sample of it."""
+    from scipy.special import gammaincinv
+    q = (np.arange(n) + 0.5) / n
+    return gammaincinv(shape, q) * (mean / shape)
+
+
+def _packing(out, nout, side, ach, T2_ex, D_ex):
     L = side.value
     cyl = []
     for i in range(nout.value):

@@ -23,7 +23,7 @@ import numpy as np
 from . import _native as N
 from .acquisition import CosGFunc, Device, Lattice, RectGrad, default_device
 from .batch import Job, run_batch
-from .substrate import rps_gamma_pack
+from .substrate import gamma_quantile_radii, pack_radii
 
 INPUTS = ("mean_radius_um", "gamma_shape", "fraction", "kappa_um_ms", "D_in", "D_ex", "G_mTm",
           "Delta_ms", "delta_ms", "omega_hz")
@@ -174,10 +174,12 @@ def make_jobs(subs: List[SubstrateDraw], rng, walkers: int, timestep: float,
     omega) x `g_per_wave` amplitudes.  Returns (jobs, parameter rows)."""
     jobs, rows = [], []
     for k, s in enumerate(subs):
-        lat, cyl, f = rps_gamma_pack(int(rng.integers(1 << 31)), n_cyl, s.shape,
-                                     s.mean_radius * 1e-3, s.fraction, D_in=s.D_in * 1e-6,
-                                     T2_in=T2_IN, D_ex=s.D_ex * 1e-6, T2_ex=T2_EX,
-                                     permeability=s.kappa * 1e-3)
+        # radii at the gamma quantiles: the packing's radius distribution is
+        # the one its input row names, not a 100-sample draw from it
+        radii = gamma_quantile_radii(n_cyl, s.shape, s.mean_radius * 1e-3)
+        lat, cyl, f = pack_radii(int(rng.integers(1 << 31)), radii, s.fraction,
+                                 D_in=s.D_in * 1e-6, T2_in=T2_IN, D_ex=s.D_ex * 1e-6,
+                                 T2_ex=T2_EX, permeability=s.kappa * 1e-3)
         seqs, te = [], 0.0
         for _ in range(waves_per_sub):
             Delta = rng.uniform(*RANGES[7])
@@ -196,22 +198,33 @@ def make_jobs(subs: List[SubstrateDraw], rng, walkers: int, timestep: float,
     return jobs, np.array(rows)
 
 
-def simulate(jobs: List[Job], device: Device = None, chunk: int = 64) -> np.ndarray:
-    """Normalised signals |M|/N of every sequence of every job (plain MC)."""
+# Dense packings hold narrow channels between neighbouring cylinders where a
+# rare move reflects more than 1024 times; such moves end at their last
+# reflection.  Training data accepts them up to this fraction of all moves.
+MAX_CAP_FRACTION = 1e-8
+
+
+def simulate(jobs: List[Job], device: Device = None, chunk: int = 64,
+             counts: Optional[Dict[str, int]] = None) -> np.ndarray:
+    """Normalised signals |M|/N of every sequence of every job (plain MC).
+    `counts`, when given, accumulates walker_steps and cap_hits."""
     out = []
     for i in range(0, len(jobs), chunk):
-        for r in run_batch(jobs[i:i + chunk], device=device):
+        for r in run_batch(jobs[i:i + chunk], device=device, max_cap_fraction=MAX_CAP_FRACTION):
             out.append(r.signal)
+            if counts is not None:
+                counts["walker_steps"] = counts.get("walker_steps", 0) + int(r.walker_steps)
+                counts["cap_hits"] = counts.get("cap_hits", 0) + int(r.cap_hits)
     return np.concatenate(out) if out else np.zeros(0)
 
 
 def generate(n_sub: int, seed: int, walkers: int = 262144, timestep: float = 0.005,
-             n_cyl: int = 100, device: Device = None):
+             n_cyl: int = 100, device: Device = None, counts: Optional[Dict[str, int]] = None):
     """(parameters [n][10], signals [n]) from n_sub substrates x 64 sequences."""
     rng = np.random.default_rng(seed)
     subs = draw_substrates(n_sub, rng)
     jobs, P = make_jobs(subs, rng, walkers, timestep, n_cyl)
-    S = simulate(jobs, device=device)
+    S = simulate(jobs, device=device, counts=counts)
     return P, S
 
 
@@ -221,13 +234,24 @@ class Surrogate:
     def __init__(self, mlp: MLP):
         self.mlp = mlp
 
+    # learning-rate schedule: fraction of the steps and lr multiplier
+    SCHEDULE = ((0.5, 1.0), (0.25, 0.3), (0.15, 0.1), (0.1, 0.03))
+
     @classmethod
     def fit(cls, P, S, steps=4000, batch=4096, lr=1e-3, seed=0, device=None):
+        """Adam on the normalised rows, with the learning rate stepped down
+        over the run (SCHEDULE); Adam's moments carry across the stages."""
         mlp = MLP(seed=seed, device=device)
-        loss = mlp.train(normalise(P), np.asarray(S, np.float32), batch=batch, steps=steps,
-                         lr=lr, seed=seed)
+        X, y = normalise(P), np.asarray(S, np.float32)
+        losses, done = [], 0
+        for k, (frac, mult) in enumerate(cls.SCHEDULE):
+            n = steps - done if k == len(cls.SCHEDULE) - 1 else int(round(frac * steps))
+            if n <= 0:
+                continue
+            losses.append(mlp.train(X, y, batch=batch, steps=n, lr=lr * mult, seed=seed + k))
+            done += n
         s = cls(mlp)
-        s.loss = loss
+        s.loss = np.concatenate(losses)
         return s
 
     def predict(self, P, fallback_walkers: int = 262144, timestep: float = 0.005,

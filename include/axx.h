@@ -35,6 +35,8 @@
  *   axx_substrate_rps_gamma <- RPSLatticeInitializer<Basis>::gammaRadialDist +
  *                       uniformCenterDist + correctEdges
  *                       (src/substrate/RPSinitializer.h:76-186).
+ *   axx_substrate_pack <- uniformCenterDist + correctEdges
+ *                       (src/substrate/RPSinitializer.h:103-186) for given radii.
  */
 #ifndef AXX_H_
 #define AXX_H_
@@ -353,12 +355,20 @@ axx_status axx_trace_single(axx_ctx *ctx, const axx_basis *basis,
  * the cell side to *side and up to max_out bases (originals first, then the
  * periodic images of the ones that cross the cell edge) to out, their count to
  * *nout and the achieved area fraction to *achieved.  D_in, T2_in and
- * permeability fill the basis records; region = index+1 as correctEdges sets. */
+ * permeability fill the basis records; region = index+1 as correctEdges sets.
+ * Every pair of cylinders keeps a gap of 1 % of its radius sum. */
 axx_status axx_substrate_rps_gamma(uint64_t seed, int n, double shape, double mean,
                                    double rmin, double rmax, double fraction,
                                    double D_in, double T2_in, double permeability,
                                    int max_out, axx_basis *out, int *nout, double *side,
                                    double *achieved);
+
+/* The placement step of axx_substrate_rps_gamma for caller-chosen radii
+ * (radii[n], any order; they are sorted ascending and region = index+1 in that
+ * order).  Same cell, gap, image and output rules. */
+axx_status axx_substrate_pack(uint64_t seed, int n, const double *radii, double fraction,
+                              double D_in, double T2_in, double permeability, int max_out,
+                              axx_basis *out, int *nout, double *side, double *achieved);
 
 #ifdef __cplusplus
 }

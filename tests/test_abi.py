@@ -84,3 +84,63 @@ def test_bvalue_closed_forms():
     n = 2
     want = A.GAMMA ** 2 * g * g * d ** 3 / (4 * A.PI ** 2 * n * n)
     assert abs(A.CosGFunc(g, d, sp, n).getB() - want) < 1e-9 * want
+
+
+def test_gamma_packing_statistics():
+    """Packing: achieved fraction, periodic minimum gap, radius distribution,
+    images of edge-crossing cylinders (RPSLatticeInitializer semantics)."""
+    import numpy as np
+    import axonexa_gb300 as A
+    lat, cyl, f = A.rps_gamma_pack(3, 400, 5.0, 2.5e-3, 0.6, D_in=1.7e-6, T2_in=80,
+                                   D_ex=2e-6, T2_ex=60, permeability=2e-5)
+    L = lat.a
+    orig = {}
+    for c in cyl:
+        orig.setdefault(c.region, c)
+    assert len(orig) == 400
+    r = np.array([orig[k].radius for k in sorted(orig)])
+    x = np.array([orig[k].centerX for k in sorted(orig)])
+    y = np.array([orig[k].centerY for k in sorted(orig)])
+    assert abs(np.pi * (r ** 2).sum() / L ** 2 - 0.6) < 1e-9 and abs(f - 0.6) < 1e-9
+    # gamma(k=5, mean 2.5 um): mean and coefficient of variation 1/sqrt(5)
+    assert abs(r.mean() - 2.5e-3) < 0.15e-3
+    assert abs(r.std() / r.mean() - 1 / np.sqrt(5)) < 0.06
+    dx = x[:, None] - x[None, :]
+    dy = y[:, None] - y[None, :]
+    dx -= L * np.round(dx / L)
+    dy -= L * np.round(dy / L)
+    d = np.hypot(dx, dy) + np.eye(400) * 1e9
+    assert np.all(d >= (r[:, None] + r[None, :]) * 1.0099)
+    # every extra record is a periodic image of its original
+    for c in cyl[400:]:
+        o = orig[c.region]
+        sx, sy = (c.centerX - o.centerX) / L, (c.centerY - o.centerY) / L
+        assert abs(sx - round(sx)) < 1e-9 and abs(sy - round(sy)) < 1e-9 and (sx, sy) != (0, 0)
+
+
+def test_pack_given_radii():
+    """axx_substrate_pack: caller's radii (gamma mid-quantiles), sorted into
+    regions 1..n, exact area fraction, periodic gap kept."""
+    import numpy as np
+    import axonexa_gb300 as A
+    r = A.gamma_quantile_radii(100, 4.0, 2.0e-3)
+    assert abs(r.mean() - 2.0e-3) < 0.02e-3  # quantile mean -> the law's mean
+    assert np.all(np.diff(r) > 0)
+    lat, cyl, f = A.pack_radii(7, r[::-1], 0.62, D_in=1.7e-6, T2_in=80, D_ex=2e-6, T2_ex=60)
+    L = lat.a
+    orig = {}
+    for c in cyl:
+        orig.setdefault(c.region, c)
+    got = np.array([orig[k].radius for k in range(1, 101)])
+    assert np.array_equal(got, r)
+    assert abs(np.pi * (r ** 2).sum() / L ** 2 - 0.62) < 1e-12 and abs(f - 0.62) < 1e-12
+    x = np.array([orig[k].centerX for k in range(1, 101)])
+    y = np.array([orig[k].centerY for k in range(1, 101)])
+    dx = x[:, None] - x[None, :]
+    dy = y[:, None] - y[None, :]
+    dx -= L * np.round(dx / L)
+    dy -= L * np.round(dy / L)
+    d = np.hypot(dx, dy) + np.eye(100) * 1e9
+    assert np.all(d >= (r[:, None] + r[None, :]) * 1.0099)
+    with pytest.raises(A._native.AxxError):
+        A.pack_radii(7, np.array([1e-3, -1e-3]), 0.5, D_in=1e-6, T2_in=1, D_ex=1e-6, T2_ex=1)

@@ -98,3 +98,39 @@ def test_training_reduces_loss(dev):
     Q = rng.uniform(-1, 1, size=(4000, 10))
     tq = 0.5 + 0.25 * np.sin(2 * Q[:, 0]) * np.cos(Q[:, 1]) + 0.1 * Q[:, 5]
     assert np.sqrt(np.mean((m.predict(Q) - tq) ** 2)) < 0.02
+
+
+def test_surrogate_gain_over_plain_monte_carlo(dev):
+    """Small version of the surrogate workflow: the network is trained on
+    signals the walk produced for random gamma-radius packings; on held-out
+    substrates it answers within the Monte Carlo noise, at far more signals/s
+    than the walk that made its training data; out-of-range queries fall back
+    to the walk."""
+    import axonexa_gb300.surrogate as S
+    walkers, dt = 32768, 0.01
+    t0 = time.perf_counter()
+    P, Y = S.generate(48, seed=1, walkers=walkers, timestep=dt, n_cyl=40, device=dev)
+    t_mc = time.perf_counter() - t0
+    mc_rate = len(Y) / t_mc
+    Ph, Yh = S.generate(8, seed=99, walkers=walkers, timestep=dt, n_cyl=40, device=dev)
+    sur = S.Surrogate.fit(P, Y, steps=1500, batch=2048, lr=1e-3, seed=0, device=dev)
+    pred, fb = sur.predict(Ph)
+    assert not fb.any()
+    err = np.abs(pred - Yh)
+    # Monte Carlo noise of one training signal is about 1/sqrt(walkers) ~ 0.006
+    assert err.mean() < 0.03, err.mean()
+    # versus the method without the network: a constant guess (training mean)
+    assert err.mean() < 0.5 * np.abs(Yh - Y.mean()).mean()
+    # throughput: 1e5 queries through the tensor cores
+    Q = np.tile(Ph, (100000 // len(Ph) + 1, 1))[:100000]
+    sur.mlp.predict(Q[:1000])
+    t0 = time.perf_counter()
+    sur.mlp.predict(Q)
+    t_nn = time.perf_counter() - t0
+    nn_rate = len(Q) / t_nn
+    assert nn_rate > 100 * mc_rate, (nn_rate, mc_rate)
+    # out-of-range queries are simulated instead of predicted
+    out = Ph[:2].copy()
+    out[:, 0] = 6.0  # mean radius beyond the training range
+    val, fb = sur.predict(out, fallback_walkers=4096, timestep=dt)
+    assert fb.all() and np.all((val > 0) & (val <= 1.0))
