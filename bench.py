@@ -15,7 +15,11 @@ Lines printed (rank 0):
                        (value), and through the one-shot C-ABI call with host
                        records in and host sums out (e2e); roofline of the walk
                        kernel against the measured FP32 FMA peak; the CPU oracle
-                       on a bounded sample of the same workload (cpu_baseline).
+                       on a bounded sample of the same workload (cpu_baseline);
+                       "surrogate": tcgen05 inference signals/s on 1e6 queries
+                       (tensor roofline against the measured bf16 peak) beside
+                       the plain walk's signals/s on the surrogate's own
+                       data-generation jobs.
   --impl reference  -- the reference's walker loop on the host cores: the CPU
                        restatement of updateWalkersLatticePhase (oracle, FP64,
                        reference operation order) over all host threads.
@@ -163,6 +167,76 @@ def cpu_sample_baseline(n_walkers: int, threads: int, steps_frac: float = 1.0):
     return total_ws / dt, dt, total_ws
 
 
+def surrogate_section(A, N, L, dev, queries=1000000, reps=10, plain_subs=2):
+    """Learned-surrogate throughput: tcgen05 inference of `queries` rows
+    resident on the GPU (CUDA events on the library stream), the same through
+    the host API (host rows in, host signals out), and the plain walk's
+    signals/s on the surrogate's data-generation jobs (100-cylinder gamma
+    packings, 262,144 walkers, 64 sequences each, dt 5 us)."""
+    import ctypes as C
+
+    import numpy as np
+    import torch
+
+    from axonexa_gb300 import surrogate as S
+    m = S.MLP(seed=0, device=dev)
+    g = torch.Generator(device="cuda")
+    g.manual_seed(SEED)
+    X = torch.rand(queries, 10, device="cuda", generator=g) * 2 - 1
+    y = torch.empty(queries, device="cuda")
+    torch.cuda.synchronize()
+    for _ in range(3):
+        m.predict_device(X.data_ptr(), queries, y.data_ptr())
+    N.check(L.axx_sync(dev.h), dev.h)
+    times = []
+    for _ in range(reps):
+        N.check(L.axx_event_record(dev.h, 0), dev.h)
+        m.predict_device(X.data_ptr(), queries, y.data_ptr())
+        N.check(L.axx_event_record(dev.h, 1), dev.h)
+        ms = C.c_float()
+        N.check(L.axx_event_elapsed(dev.h, 0, 1, C.byref(ms)), dev.h)
+        times.append(ms.value)
+    ms = float(np.median(times))
+    flops = m.flops_per_row() * queries
+    Xh = X.cpu().numpy()
+    m.predict(Xh[:4096])
+    t0 = time.perf_counter()
+    yh = m.predict(Xh)
+    e2e_s = time.perf_counter() - t0
+    assert np.array_equal(yh, y.cpu().numpy()), "host and device inference disagree"
+    peaks = measured_peaks()
+    pk = peaks.get("bf16_tflops")
+    out = {"queries": queries, "signals_per_s": queries / (ms * 1e-3), "ms": ms,
+           "e2e_signals_per_s": queries / e2e_s, "h2d_bytes": int(Xh.nbytes),
+           "d2h_bytes": int(4 * queries), "kernel_launches_per_call": 1,
+           "roofline": {"bound": "tensor", "achieved": flops / (ms * 1e-3) / 1e12,
+                        "peak": pk, "unit": "TFLOP/s",
+                        "frac": (flops / (ms * 1e-3) / 1e12 / pk) if pk else None,
+                        "peak_source": "measured bf16 GEMM burst" if pk else None,
+                        "flops_per_row": m.flops_per_row()}}
+    m.close()
+    if plain_subs > 0:
+        rng = np.random.default_rng(SEED)
+        subs = S.draw_substrates(plain_subs, rng)
+        jobs, P = S.make_jobs(subs, rng, 262144, 0.005, 100)
+        S.simulate(jobs[:1], device=dev)
+        t0 = time.perf_counter()
+        sig = S.simulate(jobs, device=dev)
+        t_mc = time.perf_counter() - t0
+        out["plain_signals_per_s"] = len(sig) / t_mc
+        out["plain_job"] = "%d gamma packings x 64 sequences x 262,144 walkers, dt 5 us" % plain_subs
+        out["speedup_vs_plain"] = out["signals_per_s"] / out["plain_signals_per_s"]
+    return out
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
 def run_reference(args, world, rank):
     if rank != 0:
         return 0
@@ -207,6 +281,9 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the one-shot C-ABI timing")
     ap.add_argument("--walkers", type=int, default=N_WALKERS,
                     help="walkers per acquisition (smaller cases for profiling)")
+    ap.add_argument("--no-surrogate", action="store_true", help="skip the surrogate section")
+    ap.add_argument("--surrogate-only", action="store_true",
+                    help="print only the surrogate section (profiling the inference kernel)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -224,6 +301,10 @@ def main():
     torch.cuda.set_device(local)
     dev = A.Device(local)
     L = N.lib()
+    if args.surrogate_only:
+        if rank == 0:
+            print(json.dumps({"surrogate": surrogate_section(A, N, L, dev, plain_subs=0)}))
+        return 0
     lat, cyl, acqs = workload_records(A)
     nw = args.walkers
     offset = rank * nw  # each rank walks its own walker ids (weak scaling)
@@ -338,6 +419,8 @@ def main():
         "roofline": roof,
         "clocks": clk,
     }
+    if not args.no_surrogate:
+        line["surrogate"] = surrogate_section(A, N, L, dev)
     if not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         n = int(os.environ.get("AXX_CPU_SAMPLE", "4096"))
