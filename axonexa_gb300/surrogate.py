@@ -4,7 +4,10 @@ parameters to the signal, trained on signals the simulator produces.
 Inputs (10): mean radius [um], gamma shape, intracellular area fraction,
 kappa [um/ms], D_in, D_ex [um^2/ms], G [mT/m], Delta, delta [ms], omega [Hz]
 (omega = 0: PGSE; otherwise cosine OGSE with omega*delta whole periods).
-Output: the normalised signal |M|/N.
+Output: the normalised signal |M|/N read at the fixed time TE_READ (55 ms,
+the longest Delta + delta of the ranges) for every sequence: the walk goes on
+past a sequence's own echo with its phase frozen while T2 keeps acting, so a
+common readout time makes the signal a function of the ten inputs alone.
 
 The network (MLP in -> 4 x 256 SiLU -> 1) lives in libaxx.so: BF16 tensor-core
 training (mma.sync GEMMs, FP32 accumulate, Adam) and tcgen05 inference.  Plain
@@ -32,6 +35,7 @@ INPUTS = ("mean_radius_um", "gamma_shape", "fraction", "kappa_um_ms", "D_in", "D
 RANGES = np.array([[1.5, 3.5], [3.0, 8.0], [0.40, 0.65], [0.0, 0.05], [1.2, 2.2], [1.6, 2.6],
                    [0.0, 300.0], [20.0, 40.0], [5.0, 15.0], [0.0, 400.0]])
 T2_IN, T2_EX = 80.0, 60.0
+TE_READ = float(RANGES[7][1] + RANGES[8][1])  # ms
 
 
 class MLP:
@@ -171,7 +175,8 @@ def draw_substrates(n, rng) -> List[SubstrateDraw]:
 def make_jobs(subs: List[SubstrateDraw], rng, walkers: int, timestep: float,
               n_cyl: int = 100, waves_per_sub: int = 8, g_per_wave: int = 8):
     """One batch job per substrate: `waves_per_sub` waveforms (Delta, delta,
-    omega) x `g_per_wave` amplitudes.  Returns (jobs, parameter rows)."""
+    omega) x `g_per_wave` amplitudes, all read at TE_READ.  Returns (jobs,
+    parameter rows)."""
     jobs, rows = [], []
     for k, s in enumerate(subs):
         # radii at the gamma quantiles: the packing's radius distribution is
@@ -180,19 +185,18 @@ def make_jobs(subs: List[SubstrateDraw], rng, walkers: int, timestep: float,
         lat, cyl, f = pack_radii(int(rng.integers(1 << 31)), radii, s.fraction,
                                  D_in=s.D_in * 1e-6, T2_in=T2_IN, D_ex=s.D_ex * 1e-6,
                                  T2_ex=T2_EX, permeability=s.kappa * 1e-3)
-        seqs, te = [], 0.0
+        seqs = []
         for _ in range(waves_per_sub):
             Delta = rng.uniform(*RANGES[7])
             delta = min(rng.uniform(*RANGES[8]), Delta - 1.0)
             omega = 0.0 if rng.uniform() < 0.25 else snap_omega(rng.uniform(20.0, RANGES[9][1]), delta)
             if omega > RANGES[9][1]:
                 omega = 0.0
-            te = max(te, Delta + delta)
             for G in rng.uniform(*RANGES[6], size=g_per_wave):
                 seqs.append(_sequence(G, Delta, delta, omega))
                 rows.append([s.mean_radius, s.shape, f, s.kappa, s.D_in, s.D_ex, G, Delta,
                              delta, omega])
-        steps = int(math.ceil(te / timestep)) + 1
+        steps = int(math.ceil(TE_READ / timestep)) + 1
         jobs.append(Job(cyl, seqs, walkers, steps, timestep, int(rng.integers(1 << 31)),
                         lattice=lat, relaxation=True, permeable=s.kappa > 0))
     return jobs, np.array(rows)
@@ -271,6 +275,5 @@ class Surrogate:
                 jobs, _ = make_jobs([sub], rng, fallback_walkers, timestep, waves_per_sub=1,
                                     g_per_wave=1)
                 jobs[0].seqs = [_sequence(p[6], p[7], p[8], p[9])]
-                jobs[0].steps = int(math.ceil((p[7] + p[8]) / timestep)) + 1
                 out[i] = simulate(jobs, device=device)[0]
         return out, ~ok

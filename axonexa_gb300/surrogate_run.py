@@ -28,6 +28,7 @@ def main(argv=None):
     ap.add_argument("--heldout", type=int, default=2048)
     ap.add_argument("--queries", type=int, default=1000000)
     ap.add_argument("--out", default="")
+    ap.add_argument("--save-data", default="", help="write the pairs (P, Y, Ph, Yh) as .npz")
     a = ap.parse_args(argv)
     import torch
 
@@ -42,6 +43,8 @@ def main(argv=None):
     t_gen = time.perf_counter() - t0
     Ph, Yh = S.generate((a.heldout + 63) // 64, seed=987654, walkers=a.walkers,
                         timestep=a.timestep, n_cyl=a.cylinders, device=dev)
+    if a.save_data:
+        np.savez_compressed(a.save_data, P=P, Y=Y, Ph=Ph, Yh=Yh)
     t0 = time.perf_counter()
     sur = S.Surrogate.fit(P, Y, steps=a.steps, batch=4096, lr=1e-3, seed=0, device=dev)
     t_train = time.perf_counter() - t0
