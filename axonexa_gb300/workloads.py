@@ -125,3 +125,106 @@ def batch_256(seed=2026, n_sub=256, timestep=0.005, walker_scale=1.0, max_steps=
                       relaxation=True, permeable=kappa > 0)
         jobs.append(job)
     return jobs
+
+
+def _plan(dev, lattice, basis, seqs, n, steps, timestep, seed, flags):
+    import ctypes as C
+
+    from . import _native as N
+    from .acquisition import _params
+    L = N.lib()
+    p = _params(n, steps, seed, timestep, flags)
+    b = N.array_of(N.Basis, [x.record() for x in basis])
+    s = N.array_of(N.SequenceRec, [q.record() for q in seqs])
+    h = C.c_void_p()
+    N.check(L.axx_plan_lattice(dev.h, C.byref(lattice.record()), b, len(basis), s, len(seqs),
+                               C.byref(p), C.byref(h)), dev.h)
+    return h
+
+
+def measure(name: str, steps: int = 0, walkers: int = 0, reps: int = 3, device=None) -> dict:
+    """Walker-steps/s of one workload's walks with its tables resident on the
+    GPU (CUDA events on the library stream, best of `reps` after one warm-up).
+    `steps` / `walkers` > 0 shorten the walk / change the walker count."""
+    import ctypes as C
+
+    from . import _native as N
+    from .acquisition import default_device, run_flags
+    dev = device or default_device()
+    L = N.lib()
+    if name == "free_box":
+        w = free_box()
+        acqs = [(w["seqs"], w["steps"])]
+        flags = run_flags()
+    elif name == "one_cylinder":
+        w = one_cylinder()
+        acqs = w["acquisitions"]
+        flags = run_flags(relaxation=True)
+    elif name == "gamma_pack":
+        w = gamma_pack()
+        acqs = [(w["seqs"], w["steps"])]
+        flags = run_flags(relaxation=True, permeable=True)
+    else:
+        raise ValueError("unknown workload " + name)
+    n = walkers or w["num_walkers"]
+    acqs = [(q, min(st, steps) if steps else st) for q, st in acqs]
+    plans = [(_plan(dev, w["lattice"], w["basis"], q, n, st, w["timestep"], w["seed"], flags),
+              len(q), st) for q, st in acqs]
+    ws = sum(n * (st - 1) for _, _, st in plans)
+
+    def launch():
+        for h, _, _ in plans:
+            N.check(L.axx_plan_launch(h), dev.h)
+
+    launch()
+    N.check(L.axx_sync(dev.h), dev.h)
+    best = None
+    for _ in range(reps):
+        N.check(L.axx_event_record(dev.h, 0), dev.h)
+        launch()
+        N.check(L.axx_event_record(dev.h, 1), dev.h)
+        ms = C.c_float()
+        N.check(L.axx_event_elapsed(dev.h, 0, 1, C.byref(ms)), dev.h)
+        best = ms.value if best is None else min(best, ms.value)
+    out = {"workload": name, "walkers": n, "steps": [st for _, _, st in plans],
+           "sequences": [m for _, m, _ in plans], "walker_steps": ws, "ms": best,
+           "walker_steps_per_s": ws / (best * 1e-3),
+           "signals_per_s": sum(m for _, m, _ in plans) / (best * 1e-3)}
+    hits = caps = 0
+    sig = []
+    for h, m, _ in plans:
+        mx, my = (C.c_double * m)(), (C.c_double * m)()
+        st = N.Stats(None, None, None, 0, 0, 0)
+        rc = L.axx_plan_read(h, mx, my, C.byref(st))
+        if rc != N.AXX_ERR_REFLECTION_CAP:
+            N.check(rc, dev.h)
+        hits += st.boundary_hits
+        caps += st.reflection_cap_hits
+        sig += [math.hypot(mx[i], my[i]) / n for i in range(m)]
+        L.axx_plan_destroy(h)
+    out.update(boundary_hits_per_move=hits / ws, reflection_cap_hits=caps,
+               signal_min=min(sig), signal_max=max(sig))
+    if name == "free_box" and not steps:
+        D = w["lattice"].D
+        ref = [math.exp(-q.getB() * D) for q in acqs[0][0]]
+        out["max_abs_vs_exp_bD"] = max(abs(a - b) for a, b in zip(sig, ref))
+        out["standard_error_scale"] = 1.0 / math.sqrt(2.0 * n)
+    if "fraction" in w:
+        out["fraction"] = w["fraction"]
+    return out
+
+
+def main(argv=None):
+    import argparse
+    import json
+    ap = argparse.ArgumentParser(description="time one seeded workload on the GPU")
+    ap.add_argument("workload", choices=["free_box", "one_cylinder", "gamma_pack"])
+    ap.add_argument("--steps", type=int, default=0, help="cut every walk to this many steps")
+    ap.add_argument("--walkers", type=int, default=0)
+    ap.add_argument("--reps", type=int, default=3)
+    a = ap.parse_args(argv)
+    print(json.dumps(measure(a.workload, a.steps, a.walkers, a.reps)))
+
+
+if __name__ == "__main__":
+    main()

@@ -16,6 +16,8 @@ Lines printed (rank 0):
                        records in and host sums out (e2e); roofline of the walk
                        kernel against the measured FP32 FMA peak; the CPU oracle
                        on a bounded sample of the same workload (cpu_baseline);
+                       "batch": the uneven 256-substrate batch in one
+                       persistent graph launch against per-job launches;
                        "surrogate": tcgen05 inference signals/s on 1e6 queries
                        (tensor roofline against the measured bf16 peak) beside
                        the plain walk's signals/s on the surrogate's own
@@ -47,6 +49,10 @@ DT = 0.002
 N_WALKERS = 1 << 20
 SEED = 1234
 PGSE_STEPS, OGSE_STEPS = 25000, 30000
+# from one ncu --set full capture of the PGSE walk launch (262,144 walkers):
+# DRAM bytes read + written per walker, and smsp__issue_active
+WALK_DRAM_BYTES_PER_WALKER = 188928.0 / 262144
+WALK_ISSUE_ACTIVE_NCU = 0.765
 
 
 def workload_records(A):
@@ -219,7 +225,7 @@ def surrogate_section(A, N, L, dev, queries=1000000, reps=10, plain_subs=2):
         rng = np.random.default_rng(SEED)
         subs = S.draw_substrates(plain_subs, rng)
         jobs, P = S.make_jobs(subs, rng, 262144, 0.005, 100)
-        S.simulate(jobs[:1], device=dev)
+        S.simulate(jobs, device=dev)  # same batch shape: tunes (cached) and warms up
         t0 = time.perf_counter()
         sig = S.simulate(jobs, device=dev)
         t_mc = time.perf_counter() - t0
@@ -227,6 +233,73 @@ def surrogate_section(A, N, L, dev, queries=1000000, reps=10, plain_subs=2):
         out["plain_job"] = "%d gamma packings x 64 sequences x 262,144 walkers, dt 5 us" % plain_subs
         out["speedup_vs_plain"] = out["signals_per_s"] / out["plain_signals_per_s"]
     return out
+
+
+def batch_section(A, N, L, dev, reps=3, walker_scale=0.25, max_steps=3000):
+    """The uneven 256-substrate batch (single cylinders, single spheres and
+    hexagonal packs; walkers log-uniform over 1e4-1e6 scaled by
+    `walker_scale`; 8-64 sequences each; walks cut to `max_steps`) as one
+    persistent launch replayed from a CUDA graph with the autotuned tile,
+    against the same jobs as device-resident plans launched one after another."""
+    import ctypes as C
+
+    from axonexa_gb300 import workloads as W
+    from axonexa_gb300.acquisition import _params, run_flags
+    from axonexa_gb300.batch import Batch
+    jobs = W.batch_256(walker_scale=walker_scale, max_steps=max_steps)
+
+    def timed(launch):
+        launch()
+        N.check(L.axx_sync(dev.h), dev.h)
+        best = None
+        for _ in range(reps):
+            N.check(L.axx_event_record(dev.h, 0), dev.h)
+            launch()
+            N.check(L.axx_event_record(dev.h, 1), dev.h)
+            ms = C.c_float()
+            N.check(L.axx_event_elapsed(dev.h, 0, 1, C.byref(ms)), dev.h)
+            best = ms.value if best is None else min(best, ms.value)
+        return best
+
+    b = Batch(jobs, device=dev)
+    info = b.info()
+    ms_batch = timed(b.launch)
+    b.read()
+    b.close()
+    plans, keep = [], []
+    for j in jobs:
+        seqs = N.array_of(N.SequenceRec, [q.record() for q in j.seqs])
+        basis = N.array_of(N.Basis, [x.record() for x in j.basis])
+        h = C.c_void_p()
+        if j.lattice is not None:
+            p = _params(j.num_walkers, j.steps, j.seed, j.timestep,
+                        run_flags(True, j.relaxation, j.permeable))
+            N.check(L.axx_plan_lattice(dev.h, C.byref(j.lattice.record()), basis, len(j.basis),
+                                       seqs, len(j.seqs), C.byref(p), C.byref(h)), dev.h)
+        else:
+            p = _params(j.num_walkers, j.steps, j.seed, j.timestep, run_flags(True))
+            N.check(L.axx_plan_single(dev.h, basis, seqs, len(j.seqs), C.byref(p), C.byref(h)),
+                    dev.h)
+        plans.append(h)
+        keep += [seqs, basis, p]
+
+    def launch_plans():
+        for h in plans:
+            N.check(L.axx_plan_launch(h), dev.h)
+
+    ms_plans = timed(launch_plans)
+    for h in plans:
+        L.axx_plan_destroy(h)
+    ws = info["walker_steps"]
+    return {"workload": "batch_256 (walkers x%.2f, walks cut to %d steps)" % (walker_scale,
+                                                                                max_steps),
+            "jobs": len(jobs), "signals": int(sum(len(j.seqs) for j in jobs)),
+            "walker_steps": ws, "persistent_graph_ms": ms_batch,
+            "persistent_walker_steps_per_s": ws / (ms_batch * 1e-3),
+            "per_job_launches_ms": ms_plans, "per_job_walker_steps_per_s": ws / (ms_plans * 1e-3),
+            "speedup": ms_plans / ms_batch, "tile": info["tile"],
+            "blocks_per_sm": info["blocks_per_sm"], "work_items": info["items"],
+            "kernel_launches_per_batch": info["kernel_launches"]}
 
 
 def measured_peaks():
@@ -282,6 +355,7 @@ def main():
     ap.add_argument("--walkers", type=int, default=N_WALKERS,
                     help="walkers per acquisition (smaller cases for profiling)")
     ap.add_argument("--no-surrogate", action="store_true", help="skip the surrogate section")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-launch section")
     ap.add_argument("--surrogate-only", action="store_true",
                     help="print only the surrogate section (profiling the inference kernel)")
     args = ap.parse_args()
@@ -400,7 +474,11 @@ def main():
     N.check(L.axx_fp32_fma_peak(dev.h, C.byref(peak)), dev.h)
     achieved = ops / (t_step * 1e-3)
     roof = {"bound": "simt", "achieved": achieved / 1e12, "peak": peak.value / 1e12,
-            "unit": "TFLOP/s", "frac": achieved / peak.value, "traffic": None,
+            "unit": "TFLOP/s", "frac": achieved / peak.value,
+            "traffic": WALK_DRAM_BYTES_PER_WALKER * nw,
+            "traffic_source": "ncu dram__bytes_read+write of the PGSE walk launch at 262,144 "
+                              "walkers, scaled by walkers (bytes per launch)",
+            "issue_active_ncu": WALK_ISSUE_ACTIVE_NCU,
             "peak_source": "measured: axx_fp32_fma_peak (register FMA chains on all SMs)",
             "ops_per_move": [round(f, 2) for f in F],
             "hits_per_move": [round(x, 4) for x in hits_per_move]}
@@ -419,6 +497,8 @@ def main():
         "roofline": roof,
         "clocks": clk,
     }
+    if not args.no_batch:
+        line["batch"] = batch_section(A, N, L, dev)
     if not args.no_surrogate:
         line["surrogate"] = surrogate_section(A, N, L, dev)
     if not args.no_cpu_baseline:
