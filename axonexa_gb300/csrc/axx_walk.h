@@ -25,6 +25,10 @@
 #define AXX_INIT_TRIES 100000
 
 #define AXX_MIN_BLOCKS 6      // resident blocks per SM the register budget targets
+// 16 channels (32 accumulator registers) spill under the 80 registers of 6
+// resident blocks; 5 blocks (102 registers) measured 2 % faster than 6 and
+// 10 % faster than 4 on the 400-cylinder pack.
+#define AXX_MIN_BLOCKS_FOR(kmax) ((kmax) >= 16 ? 5 : AXX_MIN_BLOCKS)
 #define AXX_SMEM_MAX (200 * 1024)
 
 enum { AXX_MODE_LATTICE = 0, AXX_MODE_SINGLE = 1 };

@@ -57,7 +57,7 @@ struct BatchItem {
 };
 
 template <int KMAX>
-__global__ void __launch_bounds__(AXX_BLOCK, AXX_MIN_BLOCKS)
+__global__ void __launch_bounds__(AXX_BLOCK, AXX_MIN_BLOCKS_FOR(KMAX))
     batch_kernel(const BatchJob *__restrict__ jobs, const BatchItem *__restrict__ items,
                  int nitems, unsigned *item_counter, double *partials) {
   extern __shared__ __align__(16) unsigned char smem[];

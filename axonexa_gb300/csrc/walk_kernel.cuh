@@ -468,10 +468,25 @@ __device__ __forceinline__ void do_move(const WalkParams &P, const SmemView &S,
   // phase channels: s_c(i) is wave_il[i*KMAX + c]; padded channels carry
   // zero waveforms and zero projections
   const float *wrow = P.wave_il + (size_t)i * KMAX;
+  float wv[KMAX];
+  if (KMAX % 4 == 0) {
+    // rows of 4k floats start on 16-byte boundaries (the table is 256-aligned)
+#pragma unroll
+    for (int q = 0; q < KMAX / 4; ++q) {
+      const float4 w4 = __ldg(reinterpret_cast<const float4 *>(wrow) + q);
+      wv[4 * q] = w4.x;
+      wv[4 * q + 1] = w4.y;
+      wv[4 * q + 2] = w4.z;
+      wv[4 * q + 3] = w4.w;
+    }
+  } else {
+#pragma unroll
+    for (int c = 0; c < KMAX; ++c) wv[c] = __ldg(&wrow[c]);
+  }
 #pragma unroll
   for (int c = 0; c < KMAX; ++c) {
     const float d = fma_f(P.ch_p[c][2], pz, fma_f(P.ch_p[c][1], py, P.ch_p[c][0] * px));
-    kahan_add(W.acc[c], W.cmp[c], __ldg(&wrow[c]) * d);
+    kahan_add(W.acc[c], W.cmp[c], wv[c] * d);
   }
   if (!single) {
     int new_slot = P.ecs_slot;
@@ -594,7 +609,7 @@ __device__ __forceinline__ double warp_sum(double v) {
 // The walk kernel.  Dynamic shared memory: [warps][M][5] FP64 sums, then the
 // instances, slot table, cell starts, slot regions and cell lists.
 template <int GEOM, int KMAX, int KM, bool TRACE>
-__global__ void __launch_bounds__(AXX_BLOCK, AXX_MIN_BLOCKS)
+__global__ void __launch_bounds__(AXX_BLOCK, AXX_MIN_BLOCKS_FOR(KMAX))
     walk_kernel(const __grid_constant__ WalkParams P, const __grid_constant__ TraceParams T) {
   extern __shared__ __align__(16) unsigned char smem[];
   constexpr int warps = AXX_BLOCK / 32;

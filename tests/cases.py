@@ -56,3 +56,15 @@ def seq_mix():
 
 def params(n, steps, seed=1234, dt=0.002, flags=0, init_mode=0, init_arg=0, offset=0):
     return O.Params(n, steps, init_mode, init_arg, flags, seed, dt, 0.0, offset)
+
+
+def gamma_packing(n=100, seed=5, kappa=2e-5):
+    """A dense periodic packing (gamma radii, area fraction 0.6, permeable)
+    from the product's host packer, as oracle records: exercises cell lists
+    with several candidates per move and walkers crossing cell edges."""
+    import axonexa_gb300 as A
+    lat, cyl, _ = A.rps_gamma_pack(seed, n, 5.0, 2.5 * UM, 0.6, D_in=1.7e-6, T2_in=80.0,
+                                   D_ex=D2, T2_ex=60.0, permeability=kappa)
+    L = O.Lattice(lat.a, lat.b, lat.c, lat.T2, 0.0, lat.D)
+    return L, [O.Basis(0, c.region, c.centerX, c.centerY, 0.0, c.radius, c.D, c.T2, 0.0,
+                       c.permeability, c.eps) for c in cyl]

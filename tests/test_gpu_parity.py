@@ -58,6 +58,7 @@ LATTICE_CASES = [
     ("cyl_reject", lambda: cases.one_cylinder(), 5, 0.002),
     ("hex_perm", lambda: cases.hex_cylinders(kappa=2e-5), 3, 0.001),
     ("spheres", lambda: cases.sphere_lattice(), 1, 0.002),
+    ("gamma_perm", lambda: cases.gamma_packing(), 3, 0.001),
 ]
 
 
@@ -130,7 +131,7 @@ def test_per_move_against_reference_fp64(dev, orc, name, make, flags, dt):
     g = A.trace_lattice(L, B, n, steps, dt, seed, device=dev, **flag_kw(flags))
     p = cases.params(n, steps, seed, dt=dt, flags=flags)
     scale = max(lat.a, lat.b, lat.c)
-    worst, ties, moves = 0.0, 0, 0
+    worst, ties, grazing, moves = 0.0, 0, 0, 0
     for w in range(n):
         prev = g["init_pos"][w].astype(np.float64)
         word = 4  # words 1..3 start the walk
@@ -138,12 +139,23 @@ def test_per_move_against_reference_fp64(dev, orc, name, make, flags, dt):
             moves += 1
             r_out, reg, hits, wout = orc.step(lat, bases, p, orc.REF64, w, i, prev, word)
             gpos = g["pos"][w, i - 1].astype(np.float64)
-            if reg != g["region"][w, i - 1] or hits != g["hits"][w, i - 1] or \
-                    wout != g["words"][w, i - 1]:
-                assert _tie(orc, lat, bases, p, w, i, prev, word, g["region"][w, i - 1],
-                            g["hits"][w, i - 1]), (w, i, reg, hits, g["region"][w, i - 1],
-                                                   g["hits"][w, i - 1])
-                ties += 1
+            greg, ghits = g["region"][w, i - 1], g["hits"][w, i - 1]
+            if reg != greg or hits != ghits or wout != g["words"][w, i - 1]:
+                if _tie(orc, lat, bases, p, w, i, prev, word, greg, ghits):
+                    ties += 1
+                else:
+                    # The reference's FP64 quadratic can re-hit the surface a
+                    # walker was just reflected from (a convex surface seen
+                    # from outside, near grazing incidence: the reflected ray
+                    # starts a rounding error inside and finds a root above
+                    # EPSILON).  The kernel formulation tests the last-hit
+                    # instance from its surface, so it has no such hit: its
+                    # FP64 version must reproduce the GPU's events and the
+                    # reference must show the extra hit.
+                    _, kreg, khits, _ = orc.step(lat, bases, p, orc.KERN64, w, i, prev, word)
+                    assert (kreg, khits) == (greg, ghits) and hits > khits, \
+                        (w, i, reg, hits, greg, ghits, kreg, khits)
+                    grazing += 1
             else:
                 d = np.abs(r_out - gpos)
                 d = np.minimum(d, np.array([lat.a, lat.b, lat.c]) - d)
@@ -151,7 +163,11 @@ def test_per_move_against_reference_fp64(dev, orc, name, make, flags, dt):
             prev = gpos
             word = int(g["words"][w, i - 1])
     assert worst < 1e-5, worst
-    assert ties <= max(2, moves // 10000), ties
+    # FP32 start positions flip near-tie moves; a dense packing (area fraction
+    # 0.6) holds many more walkers within a few ulps of a surface
+    rate = 5e-4 if name == "gamma_perm" else 1e-4
+    assert ties <= max(2, int(moves * rate)), ties
+    assert grazing <= max(2, moves // 10000), grazing
 
 
 SIGNAL_CASES = [
