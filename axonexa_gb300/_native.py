@@ -75,6 +75,23 @@ class BatchOptions(C.Structure):
 
 
 # exported symbols and their argument types
+class Field(C.Structure):
+    """axx_field"""
+    _fields_ = [("kind", C.c_int32), ("num_periods", C.c_int32), ("B0", C.c_double),
+                ("G", C.c_double), ("gx", C.c_double), ("gy", C.c_double), ("gz", C.c_double),
+                ("duration", C.c_double), ("spacing", C.c_double), ("period", C.c_double),
+                ("ramp", C.c_double), ("rf_duration", C.c_double), ("dtmin", C.c_double),
+                ("dtmax", C.c_double), ("TE", C.c_double)]
+
+
+class MagParams(C.Structure):
+    """axx_mag_params"""
+    _fields_ = [("num_walkers", C.c_int64), ("steps", C.c_int32), ("integrator", C.c_int32),
+                ("flags", C.c_uint32), ("pad", C.c_uint32), ("seed", C.c_uint64),
+                ("timestep", C.c_double), ("gamma", C.c_double), ("m0", C.c_double * 3),
+                ("walker_offset", C.c_int64)]
+
+
 _SIGS = {
     "axx_abi_version": ([], C.c_int),
     "axx_status_string": ([C.c_int], C.c_char_p),
@@ -155,6 +172,13 @@ _SIGS = {
                             C.c_double, C.c_double, C.c_int, C.POINTER(Basis),
                             C.POINTER(C.c_int), C.POINTER(C.c_double),
                             C.POINTER(C.c_double)], C.c_int),
+    "axx_run_mag": ([C.c_void_p, C.POINTER(Basis), C.POINTER(Field), C.c_int,
+                     C.POINTER(MagParams), C.POINTER(C.c_double), C.POINTER(C.c_double),
+                     C.POINTER(C.c_double)], C.c_int),
+    "axx_trace_mag": ([C.c_void_p, C.POINTER(Basis), C.POINTER(Field), C.c_int,
+                       C.POINTER(MagParams), C.c_int, C.POINTER(C.c_float),
+                       C.POINTER(C.c_float), C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                       C.POINTER(C.c_float)], C.c_int),
 }
 
 _lib = None

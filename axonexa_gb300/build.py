@@ -33,6 +33,7 @@ CUDA_SOURCES = [
     "batch.cu",
     "mlp.cu",
     "mlp_tc.cu",
+    "mag.cu",
 ]
 HOST_SOURCES = ["api.cpp", "host_plan.cpp", "plan_layout.cpp", "substrate.cpp"]
 

@@ -37,6 +37,12 @@
  *                       (src/substrate/RPSinitializer.h:76-186).
  *   axx_substrate_pack <- uniformCenterDist + correctEdges
  *                       (src/substrate/RPSinitializer.h:103-186) for given radii.
+ *   axx_run_mag      <- magAcquisitionStream<F>::runAcquisition
+ *                       (src/acquisition/magAcquisitionStream.cuh:37-90) with
+ *                       the device work of updateWalkersMag
+ *                       (src/kernels/kernelMag.cuh:1-141), the B-field
+ *                       functors (src/functors/bfunctors.cuh) and the Bloch
+ *                       updates (src/bloch/blochdiff.cuh:29-172).
  */
 #ifndef AXX_H_
 #define AXX_H_
@@ -362,6 +368,64 @@ axx_status axx_substrate_rps_gamma(uint64_t seed, int n, double shape, double me
                                    double D_in, double T2_in, double permeability,
                                    int max_out, axx_basis *out, int *nout, double *side,
                                    double *achieved);
+
+/* ---- magnetisation (Bloch) walk of a single pore ------------------------- */
+
+/* B-field functor kinds (src/functors/bfunctors.cuh). */
+enum {
+  AXX_FIELD_QSC_GRE = 0,      /* QSC_GRE(B0, G, duration, spacing) */
+  AXX_FIELD_QSC_PGSE = 1,     /* QSC_PGSE(B0, G, duration, spacing, rf_duration,
+                                 dtmin, dtmax, TE) */
+  AXX_FIELD_QSC_COS_GRE = 2,  /* QSC_COS_GRE(B0, G, duration, spacing, num_periods) */
+  AXX_FIELD_QSC_GRE_TRAP = 3, /* QSC_GRE_TRAP(B0, G, duration, spacing, ramp) */
+  AXX_FIELD_SIN_GRE = 4,      /* SIN_GRE(B0, (gx,gy,gz), duration, spacing, period) */
+  AXX_FIELD_COS_GRE = 5,      /* COS_GRE(B0, (gx,gy,gz), duration, spacing, num_periods) */
+  AXX_FIELD_RECT_GRE = 6,     /* RECT_GRE(B0, (gx,gy,gz), duration, spacing) */
+  AXX_FIELD_UCN_LOWFIELD = 7  /* UCN_lowfield(B0, G, rf_duration, dtmin, dtmax) */
+};
+
+/* One field functor; unused members are ignored.  B in T, G in T/mm,
+ * times in ms (the reference's units). */
+typedef struct {
+  int32_t kind, num_periods;
+  double B0, G, gx, gy, gz;
+  double duration, spacing, period, ramp, rf_duration, dtmin, dtmax, TE;
+} axx_field;
+
+/* Integrators of updateWalkersMag's compile-time switches.  ROTATE: the
+ * default exact rotation (updateMag_noT2_rotate).  RK4 (RK4_NORELAXATION):
+ * fourth-order Runge-Kutta for the t = 0 update only -- the reference's step
+ * loop has no RK4 branch and rotates.  ROTATE_MULTISTEP: rotations of the
+ * functor's getStepTimeMin (QSC_PGSE and UCN_lowfield only). */
+enum { AXX_MAG_ROTATE = 0, AXX_MAG_RK4 = 1, AXX_MAG_ROTATE_MULTISTEP = 2 };
+
+typedef struct {
+  int64_t num_walkers;
+  int32_t steps;       /* time points 0..steps-1, steps-1 moves */
+  int32_t integrator;  /* AXX_MAG_* */
+  uint32_t flags;      /* AXX_FLAG_SIMPLE_REJECTION, AXX_FLAG_FIX_INIT_QUIRK */
+  uint32_t pad;
+  uint64_t seed;
+  double timestep;     /* ms */
+  double gamma;        /* rad/(ms T); the reference's GAMMA macro (0: 267500) */
+  double m0[3];        /* initial magnetisation (SimuParams mx/my/mz_initial) */
+  int64_t walker_offset;
+} axx_mag_params;
+
+#define AXX_MAG_MAX_FIELDS 16
+
+/* Walkers in one pore (Cylinder_XY or Sphere, as updateWalkersMag's
+ * basis[0]); per field functor j the sums over walkers of the final
+ * magnetisation: mx[j], my[j], mz[j] (FP64; magAcquisition::getMx/My/Mz).
+ * 1 <= nfield <= AXX_MAG_MAX_FIELDS. */
+axx_status axx_run_mag(axx_ctx *ctx, const axx_basis *pore, const axx_field *fields, int nfield,
+                       const axx_mag_params *params, double *mx, double *my, double *mz);
+/* The first ntrace walkers of the same walk: start position init_pos[3],
+ * position after every move pos[(steps-1)*3], boundary hits and next stream
+ * word per move, final magnetisation m_final[nfield*3] (all per walker). */
+axx_status axx_trace_mag(axx_ctx *ctx, const axx_basis *pore, const axx_field *fields, int nfield,
+                         const axx_mag_params *params, int ntrace, float *init_pos, float *pos,
+                         int32_t *hits, int32_t *words, float *m_final);
 
 /* The placement step of axx_substrate_rps_gamma for caller-chosen radii
  * (radii[n], any order; they are sorted ascending and region = index+1 in that

@@ -10,6 +10,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <functional>
 #include <limits>
 #include <thread>
 #include <type_traits>
@@ -543,7 +544,10 @@ struct TraceRow {
 
 // Reference-order FP64 walk: updateWalkersLatticePhase
 // (kernelLattice.cuh:1-104) or updateWalkersPhase (kernelPhase.cuh:4-66).
-void walk_ref(const WalkIn &in, const RefLattice &L, int64_t w, WalkOut &out, TraceRow *tr) {
+// on_move (optional) sees the start (i = 0) and the position after every
+// move i (bounded for the single pore, wrapped for lattices).
+void walk_ref(const WalkIn &in, const RefLattice &L, int64_t w, WalkOut &out, TraceRow *tr,
+              const std::function<void(int, const V3 &)> *on_move = nullptr) {
   const orc_params &p = *in.p;
   const double dt = p.timestep;
   Stream st{p.seed, (uint64_t)(w + p.walker_offset), 1u};
@@ -605,6 +609,7 @@ void walk_ref(const WalkIn &in, const RefLattice &L, int64_t w, WalkOut &out, Tr
     tr->init_pos[2] = r.z;
   }
   V3 ru = r;
+  if (on_move) (*on_move)(0, r);
   for (int j = 0; j < in.nseq; ++j) out.phase[j] = in.gamma * dot(gfunc(in.seqs[j], 0.0), r) * dt;
   double T2f = 0.0;
   const orc_basis *b0 = in.single ? &in.basis[0] : nullptr;
@@ -681,6 +686,7 @@ void walk_ref(const WalkIn &in, const RefLattice &L, int64_t w, WalkOut &out, Tr
       else T2f += dt / L.getT2(ri);
     }
     if (!in.single) L.correct(r);
+    if (on_move) (*on_move)(i, r);
     if (tr) {
       const size_t o = (size_t)(i - 1);
       tr->pos[o * 3 + 0] = r.x;
@@ -832,6 +838,146 @@ void walk_kern(const WalkIn &in, const KGeom<T> &G, int64_t w, WalkOut &out, Tra
     }
   }
   out.t2factor = in.relax ? ((double)t2s - (double)t2c) : 0.0;
+}
+
+// ------------------------------------------------------ Bloch (mag) path ---
+// B-field functors (src/functors/bfunctors.cuh) in FP64 with the reference's
+// expressions; `gamma` stands for the GAMMA macro their constructors and
+// operator() use (QSC_PGSE, UCN_lowfield).
+V3 cross(const V3 &a, const V3 &b) {  // Vector3::operator% (vector3.cuh:179-183)
+  return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+
+V3 bfield(const orc_field &f, double gamma, const V3 &r, double time) {
+  const double B0 = f.B0, G = f.G, gd = f.duration, gs = f.spacing;
+  const V3 gv{f.gx, f.gy, f.gz};
+  switch (f.kind) {
+    case 0:  // QSC_GRE::operator() (:29-50)
+      if (time < gd) return {0.0, G * r.z, B0 + G * r.y};
+      if (time >= gs + gd && time < 2.0 * gd + gs) return {0.0, -G * r.z, B0 - G * r.y};
+      return {0.0, 0.0, B0};
+    case 1: {  // QSC_PGSE (:72-118): B1 = PI / |GAMMA rfDuration|, w = GAMMA B0
+      const double B1 = kPI / std::fabs(gamma * f.rf_duration);
+      if (time < gd) return {0.0, G * r.z, B0 + G * r.y};
+      if (time >= f.TE / 2.0 && time < f.TE / 2.0 + f.rf_duration) {
+        const double w = gamma * B0;
+        return {B1 * std::cos(w * time), -B1 * std::sin(w * time), B0};
+      }
+      if (time >= gs + gd && time < 2.0 * gd + gs) return {0.0, G * r.z, B0 + G * r.y};
+      return {0.0, 0.0, B0};
+    }
+    case 2: {  // QSC_COS_GRE (:144-191): period = duration / periods
+      const double period = gd / (double)f.num_periods;
+      auto amp = [&](double t) { return std::cos(2.0 * kPI * t / period); };
+      if (time < gd) return {0.0, G * amp(time) * r.z, B0 + G * amp(time) * r.y};
+      if (time >= gs + gd && time < 2.0 * gd + gs) {
+        const double te = time - gs - gd;
+        return {0.0, -G * amp(te) * r.z, B0 - G * amp(te) * r.y};
+      }
+      return {0.0, 0.0, B0};
+    }
+    case 3: {  // QSC_GRE_TRAP (:224-271), ramps ampMod1/ampMod2 as written
+      const double ramp = f.ramp;
+      const double t1 = ramp, t2 = ramp + gd, t3 = 2.0 * t1 + t2, t4 = gs, t5 = t4 + t3;
+      auto m1 = [&](double t) { return (G / ramp) * t; };
+      auto m2 = [&](double t) { return G - (G / ramp) * t; };
+      if (time < t1) {
+        const double m = m1(time);
+        return {0.0, (G * r.z) * m, B0 + (G * r.y) * m};
+      } else if (time >= t1 && time < t2) {
+        return {0.0, G * r.z, B0 + G * r.y};
+      } else if (time >= t2 && time < t3) {
+        const double m = m2(time - t2);
+        return {0.0, G * r.z * m, B0 + G * r.y * m};
+      } else if (time >= t5 && time < t5 + t1) {
+        const double m = m1(time - t5);
+        return {0.0, (G * r.z) * m, B0 + (G * r.y) * m};
+      } else if (time >= t5 + t1 && time < t5 + t2) {
+        return {0.0, G * r.z, B0 + G * r.y};
+      } else if (time >= t5 + t2 && time < t5 + t3) {
+        const double m = m2(time - t5 - t2);
+        return {0.0, G * r.z * m, B0 + G * r.y * m};
+      }
+      return {0.0, 0.0, B0};
+    }
+    case 4:    // SIN_GRE (:310-328)
+    case 5: {  // COS_GRE (:376-392): period = duration / periods
+      const double period = f.kind == 4 ? f.period : gd / ((double)f.num_periods);
+      auto amp = [&](double t) {
+        return f.kind == 4 ? std::sin(2.0 * kPI * t / period) : std::cos(2.0 * kPI * t / period);
+      };
+      const double gr = gv.x * r.x + gv.y * r.y + gv.z * r.z;  // Vector3 * Vector3
+      if (time < gd) return {0.0, 0.0, B0 + gr * amp(time)};
+      if (time >= gs + gd && time < 2.0 * gd + gs) return {0.0, 0.0, B0 - gr * amp(time - gs - gd)};
+      return {0.0, 0.0, B0};
+    }
+    case 6: {  // RECT_GRE (:417-425)
+      const double gr = gv.x * r.x + gv.y * r.y + gv.z * r.z;
+      if (time < gd) return {0.0, 0.0, B0 + gr};
+      if (time >= gs + gd && time < 2.0 * gd + gs) return {0.0, 0.0, B0 - gr};
+      return {0.0, 0.0, B0};
+    }
+    default: {  // UCN_lowfield (:444-466): B1 = PI / (2 |GAMMA rfDuration|), w = GAMMA B0
+      const double B1 = kPI / (2.0 * std::fabs(gamma * f.rf_duration));
+      const double w = gamma * B0;
+      if (time < f.rf_duration)
+        return {B1 * std::cos(w * time) - .5 * G * r.x, -B1 * std::sin(w * time) - .5 * G * r.y,
+                G * r.z + B0};
+      return {-.5 * G * r.x, -.5 * G * r.y, G * r.z + B0};
+    }
+  }
+}
+
+// getStepTimeMin (QSC_PGSE :121-127, UCN_lowfield :469-475)
+double step_time_min(const orc_field &f, double time) {
+  if (f.kind == 1) return (time >= f.TE / 2.0 && time < f.TE / 2.0 + f.rf_duration) ? f.dtmin : f.dtmax;
+  return (time <= f.rf_duration) ? f.dtmin : f.dtmax;
+}
+
+// updateMag_noT2_rotate (blochdiff.cuh:147-172): rotation of M about B by
+// -GAMMA |B| h.  |B| = 0 leaves M unchanged (the reference divides by 0).
+V3 mag_rotate(const V3 &M, const V3 &B, double h, double gamma) {
+  const double Bmag = std::sqrt(B.x * B.x + B.y * B.y + B.z * B.z);
+  if (!(Bmag > 0.0)) return M;
+  const V3 bh = B * (1.0 / Bmag);
+  const V3 C = bh * (M.x * bh.x + M.y * bh.y + M.z * bh.z);
+  const V3 u = M - C;
+  const double ang = -gamma * Bmag * h;
+  return (C + u * std::cos(ang)) + cross(bh, u) * std::sin(ang);
+}
+
+// updateMagRK4 without relaxation (blochdiff.cuh:29-44); bloch() = (M % B) GAMMA
+V3 mag_rk4(const orc_field &f, double gamma, const V3 &r, const V3 &M, double i, double h) {
+  auto bl = [&](const V3 &m, const V3 &B) { return cross(m, B) * gamma; };
+  const double tn = i * h;
+  const V3 k1 = bl(M, bfield(f, gamma, r, tn)) * h;
+  const V3 k2 = bl(M + k1 * .5, bfield(f, gamma, r, tn + .5 * h)) * h;
+  const V3 k3 = bl(M + k2 * .5, bfield(f, gamma, r, tn + .5 * h)) * h;
+  const V3 k4 = bl(M + k3, bfield(f, gamma, r, tn + h)) * h;
+  const V3 d = (((k1 + k2 * 2.0) + k3 * 2.0) + k4) * (1.0 / 6.0);
+  return {M.x + d.x, M.y + d.y, M.z + d.z};
+}
+
+// updateMag_rotate_noT2_multistep (blochdiff.cuh:118-140)
+V3 mag_multistep(const orc_field &f, double gamma, const V3 &r, V3 M, int i, double dt) {
+  double acc = 0.0, tk = i * dt;
+  const double hmin = step_time_min(f, tk);
+  do {
+    M = mag_rotate(M, bfield(f, gamma, r, tk), hmin, gamma);
+    acc += hmin;
+    tk += hmin;
+  } while (acc < dt);
+  return M;
+}
+
+// The update updateWalkersMag applies for field f at step i (kernelMag.cuh:
+// 32-72 for i = 0, :96-134 for i >= 1).  With RK4_NORELAXATION only the i = 0
+// update is RK4: the step loop has no branch for it and rotates.
+V3 mag_update(const orc_field &f, const orc_mag_params &p, const V3 &r, const V3 &M, int i) {
+  const double dt = p.timestep;
+  if (p.integrator == 2) return mag_multistep(f, p.gamma, r, M, i, dt);
+  if (p.integrator == 1 && i == 0) return mag_rk4(f, p.gamma, r, M, 0.0, dt);
+  return mag_rotate(M, bfield(f, p.gamma, r, i * dt), dt, p.gamma);
 }
 
 }  // namespace
@@ -1058,4 +1204,85 @@ int orc_step(const orc_lattice *lat, const orc_basis *basis, int nbasis, const o
   return 0;
 }
 
-}  // extern "C"
+void orc_bfield(const orc_field *f, double gamma, const double r[3], double t, double out[3]) {
+  const V3 b = bfield(*f, gamma, V3{r[0], r[1], r[2]}, t);
+  out[0] = b.x;
+  out[1] = b.y;
+  out[2] = b.z;
+}
+
+void orc_mag_along(const orc_field *f, int nf, const orc_mag_params *p, const double *pos,
+                   double *m_out) {
+  for (int j = 0; j < nf; ++j) {
+    V3 M{p->m0[0], p->m0[1], p->m0[2]};
+    for (int i = 0; i < p->steps; ++i)
+      M = mag_update(f[j], *p, V3{pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]}, M, i);
+    m_out[3 * j] = M.x;
+    m_out[3 * j + 1] = M.y;
+    m_out[3 * j + 2] = M.z;
+  }
+}
+
+int orc_mag_walk(const orc_basis *pore, const orc_field *f, int nf, const orc_mag_params *p,
+                 int nthreads, double *sums, double *m_walk, orc_trace *trace) {
+  if (!pore || !p || p->num_walkers < 1 || p->steps < 1 || !(p->timestep > 0.0)) return -1;
+  if (nf < 1 || !f || !sums || p->integrator < 0 || p->integrator > 2) return -1;
+  for (int j = 0; j < nf; ++j) {
+    if (f[j].kind < 0 || f[j].kind > 7) return -1;
+    if (p->integrator == 2 && f[j].kind != 1 && f[j].kind != 7) return -2;  // no getStepTimeMin
+  }
+  orc_params wp{p->num_walkers, p->steps, 0, 0, p->flags & 4u, p->seed, p->timestep, p->gamma,
+                p->walker_offset};
+  WalkIn in{nullptr, pore, 1, nullptr, 0, &wp, p->gamma, true, false, false, (p->flags & 4u) != 0};
+  RefLattice L{};
+  const int64_t N = p->num_walkers;
+  if (nthreads < 1) nthreads = 1;
+  if ((int64_t)nthreads > N) nthreads = (int)N;
+  std::vector<std::vector<double>> part(nthreads, std::vector<double>((size_t)nf * 3, 0.0));
+  auto work = [&](int t) {
+    const int64_t w0 = N * t / nthreads, w1 = N * (t + 1) / nthreads;
+    WalkOut out;
+    std::vector<V3> M(nf);
+    const std::function<void(int, const V3 &)> cb = [&](int i, const V3 &r) {
+      for (int j = 0; j < nf; ++j) M[j] = mag_update(f[j], *p, r, M[j], i);
+    };
+    for (int64_t w = w0; w < w1; ++w) {
+      TraceRow row, *tr = nullptr;
+      if (trace && w < trace->ntrace) {
+        const size_t o = (size_t)w * (size_t)(p->steps - 1);
+        row = {trace->init_pos + w * 3, trace->pos + o * 3, trace->region + o, trace->hits + o,
+               trace->words + o};
+        tr = &row;
+      }
+      for (int j = 0; j < nf; ++j) M[j] = V3{p->m0[0], p->m0[1], p->m0[2]};
+      walk_ref(in, L, w, out, tr, &cb);
+      for (int j = 0; j < nf; ++j) {
+        double *s = &part[t][(size_t)j * 3];
+        s[0] += M[j].x;
+        s[1] += M[j].y;
+        s[2] += M[j].z;
+        if (m_walk && trace && w < trace->ntrace) {
+          double *o = m_walk + ((size_t)w * nf + j) * 3;
+          o[0] = M[j].x;
+          o[1] = M[j].y;
+          o[2] = M[j].z;
+        }
+      }
+    }
+  };
+  if (nthreads == 1) {
+    work(0);
+  } else {
+    std::vector<std::thread> th;
+    for (int t = 0; t < nthreads; ++t) th.emplace_back(work, t);
+    for (auto &x : th) x.join();
+  }
+  for (int j = 0; j < nf * 3; ++j) {
+    double s = 0.0;
+    for (int t = 0; t < nthreads; ++t) s += part[t][j];
+    sums[j] = s;
+  }
+  return 0;
+}
+
+}  // extern "C\"

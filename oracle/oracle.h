@@ -97,6 +97,44 @@ int orc_step(const orc_lattice *lat, const orc_basis *basis, int nbasis, const o
 double orc_bvalue(const orc_sequence *q, double gamma);
 void orc_gradient(const orc_sequence *q, double t, double out[3]);
 
+/* ---- magnetisation (Bloch) path ------------------------------------------
+ * The records have the layout of the product's axx_field / axx_mag_params.
+ * Field kinds: 0 QSC_GRE, 1 QSC_PGSE, 2 QSC_COS_GRE, 3 QSC_GRE_TRAP,
+ * 4 SIN_GRE, 5 COS_GRE, 6 RECT_GRE, 7 UCN_lowfield (src/functors/bfunctors.cuh).
+ * Integrators: 0 rotation (the reference's default), 1 RK4 (RK4_NORELAXATION),
+ * 2 multi-step rotation (ROTATE_MULTISTEP). */
+typedef struct {
+  int32_t kind, num_periods;
+  double B0, G, gx, gy, gz, duration, spacing, period, ramp, rf_duration, dtmin, dtmax, TE;
+} orc_field;
+
+typedef struct {
+  int64_t num_walkers;
+  int32_t steps, integrator;
+  uint32_t flags; /* 4: simple rejection instead of specular reflection */
+  uint32_t pad;
+  uint64_t seed;
+  double timestep, gamma, m0[3];
+  int64_t walker_offset;
+} orc_mag_params;
+
+/* B(r, t) of one field functor (FP64, the reference's expressions). */
+void orc_bfield(const orc_field *f, double gamma, const double r[3], double t, double out[3]);
+
+/* Magnetisation of one walker along a given trajectory: pos[0] is the start,
+ * pos[i] the position after move i (i = 1..steps-1); m_out[3*j..] for field j.
+ * The integrator and time points are updateWalkersMag's (kernelMag.cuh). */
+void orc_mag_along(const orc_field *f, int nf, const orc_mag_params *p, const double *pos,
+                   double *m_out);
+
+/* updateWalkersMag restated in FP64 (reference order) for a single pore:
+ * sums[3*j..3*j+2] = (sum Mx, sum My, sum Mz) of field j over the walkers;
+ * m_walk (optional) = the first `trace->ntrace` walkers' final M
+ * [ntrace][nf][3]; trace (optional) = their trajectories as orc_walk
+ * records them.  Returns 0 or a negative code. */
+int orc_mag_walk(const orc_basis *pore, const orc_field *f, int nf, const orc_mag_params *p,
+                 int nthreads, double *sums, double *m_walk, orc_trace *trace);
+
 #ifdef __cplusplus
 }
 #endif

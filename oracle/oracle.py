@@ -199,3 +199,95 @@ def gradient(seq, t: float):
     out = (C.c_double * 3)()
     lib().orc_gradient(C.byref(seq), C.c_double(t), out)
     return np.array(list(out))
+
+
+# ---- magnetisation (Bloch) path --------------------------------------------
+MAG_VARIANTS = ("mag_rot_spec", "mag_rot_rej", "mag_rk4_spec", "mag_ms_spec")
+ROTATE, RK4, MULTISTEP = 0, 1, 2
+
+
+class Field(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("num_periods", C.c_int32), ("B0", C.c_double),
+                ("G", C.c_double), ("gx", C.c_double), ("gy", C.c_double), ("gz", C.c_double),
+                ("duration", C.c_double), ("spacing", C.c_double), ("period", C.c_double),
+                ("ramp", C.c_double), ("rf_duration", C.c_double), ("dtmin", C.c_double),
+                ("dtmax", C.c_double), ("TE", C.c_double)]
+
+
+class MagParams(C.Structure):
+    _fields_ = [("num_walkers", C.c_int64), ("steps", C.c_int32), ("integrator", C.c_int32),
+                ("flags", C.c_uint32), ("pad", C.c_uint32), ("seed", C.c_uint64),
+                ("timestep", C.c_double), ("gamma", C.c_double), ("m0", C.c_double * 3),
+                ("walker_offset", C.c_int64)]
+
+
+def mag_params(n, steps, seed, dt, integrator=ROTATE, reject=False, gamma=267500.0,
+               m0=(1.0, 0.0, 0.0), offset=0):
+    return MagParams(n, steps, integrator, 4 if reject else 0, 0, seed, dt, gamma,
+                     (C.c_double * 3)(*m0), offset)
+
+
+def mag_variant(integrator: int, reject: bool) -> str:
+    if reject:
+        return "mag_rot_rej" if integrator == ROTATE else None
+    return ("mag_rot_spec", "mag_rk4_spec", "mag_ms_spec")[integrator]
+
+
+def _mag_out(sums, mw, bufs, nf, ntrace, steps):
+    return (sums.reshape(nf, 3), mw.reshape(ntrace, nf, 3) if ntrace else None,
+            _shape_trace(bufs, ntrace, steps) if ntrace else None)
+
+
+def mag_walk(pore, fields, params, nthreads=1, ntrace=0):
+    """updateWalkersMag restated (FP64, reference order).  Returns
+    (sums[nf,3], final M of the first ntrace walkers [ntrace,nf,3] | None,
+    their traces | None)."""
+    L = lib()
+    nf = len(fields)
+    f = _arr(fields, Field)
+    sums = np.zeros(nf * 3)
+    mw = np.zeros(max(ntrace, 1) * nf * 3)
+    tr, bufs = (make_trace(ntrace, params.steps) if ntrace else (None, None))
+    rc = L.orc_mag_walk(C.byref(pore), f, nf, C.byref(params), nthreads,
+                        sums.ctypes.data_as(C.POINTER(C.c_double)),
+                        mw.ctypes.data_as(C.POINTER(C.c_double)) if ntrace else None,
+                        C.byref(tr) if tr is not None else None)
+    if rc != 0:
+        raise ValueError("orc_mag_walk failed: %d" % rc)
+    return _mag_out(sums, mw, bufs, nf, ntrace, params.steps)
+
+
+def ref_mag(variant, pore, fields, params, ntrace=0):
+    """The reference's updateWalkersMag compiled here; None if unavailable."""
+    R = reflib()
+    if R is None:
+        return None
+    fn = getattr(R, "ref_mag_" + variant)
+    nf = len(fields)
+    f = _arr(fields, Field)
+    sums = np.zeros(nf * 3)
+    mw = np.zeros(max(ntrace, 1) * nf * 3)
+    tr, bufs = (make_trace(ntrace, params.steps) if ntrace else (None, None))
+    rc = fn(C.byref(pore), f, nf, C.byref(params), sums.ctypes.data_as(C.POINTER(C.c_double)),
+            mw.ctypes.data_as(C.POINTER(C.c_double)) if ntrace else None,
+            C.byref(tr) if tr is not None else None)
+    if rc != 0:
+        raise ValueError("ref_mag_%s failed: %d" % (variant, rc))
+    return _mag_out(sums, mw, bufs, nf, ntrace, params.steps)
+
+
+def mag_along(fields, params, pos) -> np.ndarray:
+    """Final M [nf,3] of one walker along the trajectory pos[steps,3] (FP64)."""
+    nf = len(fields)
+    f = _arr(fields, Field)
+    p = np.ascontiguousarray(pos, dtype=np.float64)
+    out = np.zeros(nf * 3)
+    lib().orc_mag_along(f, nf, C.byref(params), p.ctypes.data_as(C.POINTER(C.c_double)),
+                        out.ctypes.data_as(C.POINTER(C.c_double)))
+    return out.reshape(nf, 3)
+
+
+def bfield(field, gamma, r, t) -> np.ndarray:
+    out = (C.c_double * 3)()
+    lib().orc_bfield(C.byref(field), C.c_double(gamma), (C.c_double * 3)(*r), C.c_double(t), out)
+    return np.array(list(out))

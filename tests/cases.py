@@ -68,3 +68,31 @@ def gamma_packing(n=100, seed=5, kappa=2e-5):
     L = O.Lattice(lat.a, lat.b, lat.c, lat.T2, 0.0, lat.D)
     return L, [O.Basis(0, c.region, c.centerX, c.centerY, 0.0, c.radius, c.D, c.T2, 0.0,
                        c.permeability, c.eps) for c in cyl]
+
+
+# ---- magnetisation (Bloch) path: field functors and pores ------------------
+def mag_fields():
+    """One field functor of each kind (B in T, G in T/mm, times in ms)."""
+    F = O.Field
+    return [
+        F(0, 0, 1e-3, 1e-3, 0, 0, 0, 0.5, 0.6, 0, 0, 0, 0, 0, 0),                # QSC_GRE
+        F(1, 0, 1e-3, 1e-3, 0, 0, 0, 0.4, 0.8, 0, 0, 0.2, 0.0005, 0.002, 1.6),   # QSC_PGSE
+        F(2, 2, 1e-3, 1e-3, 0, 0, 0, 0.6, 0.4, 0, 0, 0, 0, 0, 0),                # QSC_COS_GRE
+        F(3, 0, 1e-3, 1e-3, 0, 0, 0, 0.3, 0.4, 0, 0.1, 0, 0, 0, 0),              # QSC_GRE_TRAP
+        F(4, 0, 1e-3, 0, 1e-3, 5e-4, 0, 0.5, 0.4, 0.25, 0, 0, 0, 0, 0),          # SIN_GRE
+        F(5, 2, 1e-3, 0, 0, 1e-3, 5e-4, 0.5, 0.4, 0, 0, 0, 0, 0, 0),             # COS_GRE
+        F(6, 0, 1e-3, 0, 1e-3, 0, 0, 0.5, 0.4, 0, 0, 0, 0, 0, 0),                # RECT_GRE
+        F(7, 0, 1e-4, 2e-4, 0, 0, 0, 0, 0, 0, 0, 0.3, 0.0005, 0.002, 0),         # UCN_lowfield
+    ]
+
+
+def mag_multistep_fields():
+    """The functors that define getStepTimeMin (QSC_PGSE, UCN_lowfield)."""
+    f = mag_fields()
+    return [f[1], f[7]]
+
+
+def mag_pore(sph=False):
+    if sph:
+        return O.Basis(1, 1, 0.0, 0.0, 0.0, 6 * UM, D2, 0.0, 0.0, 0.0, 1e-14)
+    return O.Basis(0, 1, 0.0, 0.0, 0.0, 5 * UM, D2, 0.0, 0.0, 0.0, 1e-14)

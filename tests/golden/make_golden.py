@@ -48,6 +48,22 @@ def golden_cases():
     return out
 
 
+def mag_golden_cases():
+    """(name, variant, pore, fields, params) of the magnetisation walker."""
+    MP = O.mag_params
+    fa, fm = cases.mag_fields(), cases.mag_multistep_fields()
+    cyl, sph = cases.mag_pore(False), cases.mag_pore(True)
+    return [
+        ("mag_rot_cyl", "mag_rot_spec", cyl, fa, MP(48, 800, 21, 0.002)),
+        ("mag_rot_sph", "mag_rot_spec", sph, fa, MP(48, 800, 22, 0.002)),
+        ("mag_rej_cyl", "mag_rot_rej", cyl, fa, MP(48, 800, 23, 0.002, reject=True)),
+        ("mag_rk4_cyl", "mag_rk4_spec", cyl, fa, MP(48, 800, 24, 0.002, integrator=O.RK4)),
+        ("mag_ms_cyl", "mag_ms_spec", cyl, fm, MP(48, 800, 25, 0.002, integrator=O.MULTISTEP,
+                                                  m0=(0.0, 0.0, 1.0))),
+        ("mag_ms_sph", "mag_ms_spec", sph, fm, MP(48, 800, 26, 0.002, integrator=O.MULTISTEP)),
+    ]
+
+
 def main():
     if O.reflib() is None:
         O.build(ref=True)
@@ -61,6 +77,16 @@ def main():
             data[name + "/" + k] = v if k == "init_pos" else v[:, :TRACE_MOVES]
     np.savez_compressed(os.path.join(HERE, "ref_walks.npz"), **data)
     print("wrote", len(data), "arrays")
+    mag = {}
+    for name, var, pore, fields, p in mag_golden_cases():
+        sums, mw, tr = O.ref_mag(var, pore, fields, p, ntrace=NTRACE)
+        mag[name + "/sums"] = sums
+        mag[name + "/m_walk"] = mw
+        if tr is not None and "rej" not in var:  # boundaryNormal is hooked in specular builds
+            for k, v in tr.items():
+                mag[name + "/" + k] = v if k == "init_pos" else v[:, :TRACE_MOVES]
+    np.savez_compressed(os.path.join(HERE, "ref_mag.npz"), **mag)
+    print("wrote", len(mag), "arrays")
 
 
 if __name__ == "__main__":
