@@ -456,11 +456,13 @@ axx_status mag_run(axx_ctx *ctx, const axx_basis *pore, const axx_field *fields,
     return mfail2(ctx, AXX_ERR_INVALID_ARG, "num_walkers, steps, timestep or walker_offset out of range");
   if (mp->integrator < 0 || mp->integrator > 2)
     return mfail2(ctx, AXX_ERR_INVALID_ARG, "unknown integrator");
-  if (!std::isfinite(mp->gamma) || mp->gamma < 0.0)
-    return mfail2(ctx, AXX_ERR_INVALID_ARG, "gamma must be finite and >= 0");
+  // negative ratios are physical here (helium-3: the reference's magLF
+  // examples use GAMMA = -203789): they reverse the precession
+  if (!std::isfinite(mp->gamma))
+    return mfail2(ctx, AXX_ERR_INVALID_ARG, "gamma must be finite");
   if (mp->flags & ~(uint32_t)(AXX_FLAG_SIMPLE_REJECTION | AXX_FLAG_FIX_INIT_QUIRK))
     return mfail2(ctx, AXX_ERR_INVALID_ARG, "the magnetisation walk takes only the rejection and init-quirk flags");
-  const double gamma = mp->gamma > 0.0 ? mp->gamma : kGammaDefault;
+  const double gamma = mp->gamma != 0.0 ? mp->gamma : kGammaDefault;
   const double dt = mp->timestep;
   const int steps = mp->steps;
   for (int j = 0; j < nf; ++j) {

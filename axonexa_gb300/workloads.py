@@ -218,12 +218,73 @@ def main(argv=None):
     import argparse
     import json
     ap = argparse.ArgumentParser(description="time one seeded workload on the GPU")
-    ap.add_argument("workload", choices=["free_box", "one_cylinder", "gamma_pack"])
+    ap.add_argument("workload", choices=["free_box", "one_cylinder", "gamma_pack", "mag_lowfield"])
     ap.add_argument("--steps", type=int, default=0, help="cut every walk to this many steps")
     ap.add_argument("--walkers", type=int, default=0)
     ap.add_argument("--reps", type=int, default=3)
+    ap.add_argument("--cpu-sample", type=int, default=0,
+                    help="mag_lowfield: also time the CPU oracle on this many walkers")
     a = ap.parse_args(argv)
-    print(json.dumps(measure(a.workload, a.steps, a.walkers, a.reps)))
+    if a.workload == "mag_lowfield":
+        print(json.dumps(measure_mag(a.walkers, a.steps, a.reps, a.cpu_sample)))
+    else:
+        print(json.dumps(measure(a.workload, a.steps, a.walkers, a.reps)))
+
+
+
+def mag_lowfield(n_fields=16, walkers=57344, gd=1.0, gs=1.0):
+    """The low-field helium-3 cell of the reference's magLF example, in its
+    units: cylinder radius 24.2, D 20, dt 0.001, GAMMA -203789, B0 6e-4,
+    QSC_GRE gradient-echo fields with G = i * 6e-6 / n_fields, duration and
+    spacing gd, gs; one walk, n_fields field functors."""
+    from .acquisition import Cylinder_XY
+    from .magnetization import QSC_GRE
+    pore = Cylinder_XY(0.0, 0.0, 24.2, 0.0, 0.0, 20.0, 0, 0.0)
+    fields = [QSC_GRE(6e-4, i * 6e-6 / n_fields, gd, gs) for i in range(n_fields)]
+    te = 2.0 * gd + gs
+    return dict(pore=pore, fields=fields, num_walkers=walkers, steps=int(te / 0.001),
+                timestep=0.001, gamma=-203789.0, seed=1234)
+
+
+def measure_mag(walkers: int = 0, steps: int = 0, reps: int = 3, cpu_sample: int = 0,
+                device=None) -> dict:
+    """Walker-steps/s of the magnetisation walk (axx_run_mag, host records in,
+    host sums out, best of reps after one warm-up), and optionally the CPU
+    oracle's reference-order walk on a bounded walker sample."""
+    import os
+    import time
+
+    from .magnetization import run_mag
+    w = mag_lowfield()
+    n = walkers or w["num_walkers"]
+    st = steps or w["steps"]
+    kw = dict(gamma=w["gamma"], device=device)
+    run_mag(w["pore"], w["fields"], n, st, w["timestep"], w["seed"], **kw)
+    best, r = None, None
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        r = run_mag(w["pore"], w["fields"], n, st, w["timestep"], w["seed"], **kw)
+        dtw = time.perf_counter() - t0
+        best = dtw if best is None else min(best, dtw)
+    ws = n * (st - 1)
+    out = {"workload": "mag_lowfield", "walkers": n, "steps": st, "fields": len(w["fields"]),
+           "seconds": best, "walker_steps_per_s": ws / best,
+           "field_updates_per_s": n * st * len(w["fields"]) / best,
+           "signal": [float(x) for x in r.signal]}
+    if cpu_sample:
+        from oracle import oracle as O
+        O.lib()
+        pore = O.Basis(0, 0, 0.0, 0.0, 0.0, 24.2, 20.0, 0.0, 0.0, 0.0, 1e-14)
+        F = [O.Field(0, 0, f.B0, f.G, 0, 0, 0, f.gradientDuration, f.gradientSpacing, 0, 0, 0, 0,
+                     0, 0) for f in w["fields"]]
+        p = O.mag_params(cpu_sample, st, w["seed"], w["timestep"], gamma=w["gamma"])
+        th = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        O.mag_walk(pore, F, p, nthreads=th)
+        tc = time.perf_counter() - t0
+        out["cpu_oracle"] = {"walker_steps_per_s": cpu_sample * (st - 1) / tc, "cores": th,
+                             "sample_walkers": cpu_sample, "seconds": tc}
+    return out
 
 
 if __name__ == "__main__":

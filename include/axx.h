@@ -407,7 +407,8 @@ typedef struct {
   uint32_t pad;
   uint64_t seed;
   double timestep;     /* ms */
-  double gamma;        /* rad/(ms T); the reference's GAMMA macro (0: 267500) */
+  double gamma;        /* rad/(ms T); the reference's GAMMA macro (0: 267500;
+                          negative for helium-3, -203789, as its magLF examples) */
   double m0[3];        /* initial magnetisation (SimuParams mx/my/mz_initial) */
   int64_t walker_offset;
 } axx_mag_params;

@@ -164,3 +164,23 @@ def test_mag_acquisition_stream_api(dev):
     s = [math.hypot(pas.getAcquisition(i).getMx()[0], pas.getAcquisition(i).getMy()[0])
          for i in range(3)]
     assert s[0] > s[1] > s[2]
+
+
+def test_mag_negative_gamma_helium3(dev, orc):
+    """GAMMA = -203789 (helium-3, the reference's magLF examples) reverses the
+    precession; per-walker M against FP64 along the same paths."""
+    import axonexa_gb300 as A
+    f = orc.Field(0, 0, 1e-3, 1e-3, 0, 0, 0, 0.5, 0.6, 0, 0, 0, 0, 0, 0)
+    pore = cases.mag_pore()
+    P, F = to_product(pore, [f])
+    n, steps, dt, gam = 32, 800, 0.002, -203789.0
+    g = A.trace_mag(P, F, n, steps, dt, 17, gamma=gam, device=dev)
+    mp = orc.mag_params(n, steps, 17, dt, gamma=gam)
+    worst = 0.0
+    for w in range(n):
+        pos = np.vstack([g["init_pos"][w][None], g["pos"][w]]).astype(np.float64)
+        worst = max(worst, float(np.abs(g["m"][w] - orc.mag_along([f], mp, pos)).max()))
+    assert worst < 2e-4, worst
+    # free precession sense: after one step My = -sin(-|gamma| B0 dt) > 0 for gamma < 0
+    one = A.trace_mag(P, [A.QSC_GRE(1e-3, 0.0, 0.5, 0.6)], 1, 1, dt, 1, gamma=gam, device=dev)
+    assert one["m"][0, 0, 1] > 0
