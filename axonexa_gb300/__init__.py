@@ -9,10 +9,11 @@ from .acquisition import (GAMMA, PI, ApodCosGFunc, CosGFunc, Cylinder_XY, Device
                           default_device, linear_regression, phaseAcquisition,
                           phaseAcquisitionStream, philox_words, run_lattice, run_single,
                           trace_lattice, trace_single)
-from .substrate import gamma_quantile_radii, hex_cell, pack_radii, rps_gamma_pack
+from .substrate import gamma_quantile_radii, hex_cell, pack_radii, rps_gamma_pack, volume_fraction
 from .batch import Batch, Job, autotune, run_batch
 from .magnetization import (COS_GRE, QSC_COS_GRE, QSC_GRE, QSC_GRE_TRAP, QSC_PGSE, RECT_GRE,
                             SIN_GRE, UCN_lowfield, magAcquisition, magAcquisitionStream,
                             run_mag, trace_mag)
+from .acquisition import run_wc, wc_start
 
 __all__ = [n for n in dir() if not n.startswith("_")]

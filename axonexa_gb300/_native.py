@@ -172,6 +172,13 @@ _SIGS = {
                             C.c_double, C.c_double, C.c_int, C.POINTER(Basis),
                             C.POINTER(C.c_int), C.POINTER(C.c_double),
                             C.POINTER(C.c_double)], C.c_int),
+    "axx_volume_fraction": ([C.c_void_p, C.POINTER(LatticeRec), C.POINTER(Basis), C.c_int,
+                             C.c_int64, C.c_uint64, C.POINTER(C.c_double),
+                             C.POINTER(C.c_int64)], C.c_int),
+    "axx_run_wc": ([C.c_void_p, C.POINTER(Basis), C.c_int64, C.c_int32, C.c_double, C.c_double,
+                    C.POINTER(C.c_uint32), C.POINTER(C.c_double), C.POINTER(C.c_double),
+                    C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double)],
+                   C.c_int),
     "axx_run_mag": ([C.c_void_p, C.POINTER(Basis), C.POINTER(Field), C.c_int,
                      C.POINTER(MagParams), C.POINTER(C.c_double), C.POINTER(C.c_double),
                      C.POINTER(C.c_double)], C.c_int),

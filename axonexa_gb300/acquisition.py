@@ -391,6 +391,47 @@ def philox_words(seed: int, walker: int, n: int, device: Device = None) -> np.nd
 
 
 # ------------------------------------------------------------- acquisition ---
+def wc_start(basis, n: int, seed: int):
+    """Per-walker non-zero 32-bit xorshift states and start points uniform
+    in the pore (the host side of runAcquisitionWC, seeded generator)."""
+    rng = np.random.default_rng(int(seed) & 0xFFFFFFFFFFFFFFFF)
+    state = rng.integers(1, 1 << 32, size=n, dtype=np.uint64).astype(np.uint32)
+    R = basis.radius if hasattr(basis, "radius") else basis.getRadius()
+    sph = isinstance(basis, Sphere)
+    c = np.array([basis.centerX, basis.centerY, basis.centerZ if sph else 0.0])
+    out = np.zeros((n, 3))
+    filled = 0
+    while filled < n:
+        p = rng.uniform(-1.0, 1.0, size=(2 * (n - filled) + 16, 3)) * R
+        if not sph:
+            p[:, 2] = (p[:, 2] + R)  # z in [0, 2R) as Cylinder_XY::unifRandCPU
+        q = p[:, 0] ** 2 + p[:, 1] ** 2 + (p[:, 2] ** 2 if sph else 0.0)
+        p = p[q < R * R][: n - filled]
+        out[filled:filled + len(p)] = p + np.array([c[0], c[1], c[2] if sph else 0.0])
+        filled += len(p)
+    return state, out
+
+
+def run_wc(basis, rng_state, start, grad, timestep: float, *, gamma: float = GAMMA,
+           return_phase: bool = False, device: Device = None):
+    """The WCDMC comparison walker (axx_run_wc).  Returns (phases | None,
+    sum cos(phase), sum sin(phase))."""
+    dev = device or default_device()
+    st = np.ascontiguousarray(rng_state, np.uint32)
+    p0 = np.ascontiguousarray(start, np.float64)
+    g = np.ascontiguousarray(grad, np.float64)
+    n = len(st)
+    ph = np.zeros(n) if return_phase else None
+    sc, ss = C.c_double(), C.c_double()
+    N.check(N.lib().axx_run_wc(dev.h, C.byref(basis.record()), n, len(g), float(timestep),
+                               float(gamma), st.ctypes.data_as(C.POINTER(C.c_uint32)),
+                               p0.ctypes.data_as(C.POINTER(C.c_double)),
+                               g.ctypes.data_as(C.POINTER(C.c_double)),
+                               ph.ctypes.data_as(C.POINTER(C.c_double)) if return_phase else None,
+                               C.byref(sc), C.byref(ss)), dev.h)
+    return ph, sc.value, ss.value
+
+
 def linear_regression(y, x) -> float:
     """Slope of y on x (misc.cuh:41-59)."""
     if len(y) != len(x):
@@ -503,6 +544,20 @@ class phaseAcquisitionStream:
         res = run_single(basis, acq.gradientFunctors, self.number_of_particles, acq.numOfSteps,
                          timestep, acq.seed, specular=specular, device=self.device)
         self._store(acq, res)
+
+    def runAcquisitionWC(self, num, basis, timestep, blocks=None, threads=None):
+        """runAcquisitionWC (phaseAcquisitionStream.cuh:193-252): per
+        measurement the WCDMC walker (axx_run_wc) with the functor's G(j dt)
+        table.  The driver's host draws (per-walker xorshift states and
+        start points in the pore) come from a generator seeded with the
+        acquisition's seed instead of srand/rand."""
+        acq = self.acqSet[num]
+        n, steps = self.number_of_particles, acq.numOfSteps
+        for i, g in enumerate(acq.gradientFunctors):
+            grad = np.array([tuple(g(j * timestep)) for j in range(steps)], dtype=np.float64)
+            state, start = wc_start(basis, n, acq.seed)
+            r = run_wc(basis, state, start, grad, timestep, device=self.device)
+            acq.mx[i], acq.my[i] = r[1], r[2]
 
     def runAcquisitionStreamLattice(self, basis, lat, timestep, blocks=None, threads=None,
                                     numOfDevices=1, plan=None, numOfSMPerDevice=None, **kw):

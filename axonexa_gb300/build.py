@@ -34,6 +34,8 @@ CUDA_SOURCES = [
     "mlp.cu",
     "mlp_tc.cu",
     "mag.cu",
+    "calcf.cu",
+    "wc.cu",
 ]
 HOST_SOURCES = ["api.cpp", "host_plan.cpp", "plan_layout.cpp", "substrate.cpp"]
 

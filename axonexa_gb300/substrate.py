@@ -73,3 +73,16 @@ def hex_cell(radius: float, fraction: float, *, D_in, T2_in, D_ex, T2_ex, permea
            Cylinder_XY(d / 2.0, 2.0 * h, radius, T2_in, 0.0, D_in, 3, permeability),
            Cylinder_XY(d, h, radius, T2_in, 0.0, D_in, 4, permeability)]
     return Lattice(d, 2.0 * h, d, T2_ex, 0.0, D_ex, 4), cyl
+
+
+def volume_fraction(lattice, basis, points: int = 1 << 22, seed: int = 1234, device=None):
+    """Monte Carlo intracellular volume fraction of a lattice substrate
+    (axx_volume_fraction; the reference's calcf, src/util/calcf.cuh).
+    Returns (fraction, count)."""
+    from .acquisition import default_device
+    dev = device or default_device()
+    b = N.array_of(N.Basis, [x.record() for x in basis])
+    f, n = C.c_double(), C.c_int64()
+    N.check(N.lib().axx_volume_fraction(dev.h, C.byref(lattice.record()), b, len(basis),
+                                        int(points), int(seed), C.byref(f), C.byref(n)), dev.h)
+    return f.value, n.value

@@ -218,7 +218,8 @@ def main(argv=None):
     import argparse
     import json
     ap = argparse.ArgumentParser(description="time one seeded workload on the GPU")
-    ap.add_argument("workload", choices=["free_box", "one_cylinder", "gamma_pack", "mag_lowfield"])
+    ap.add_argument("workload", choices=["free_box", "one_cylinder", "gamma_pack", "mag_lowfield",
+                                         "wc_sphere"])
     ap.add_argument("--steps", type=int, default=0, help="cut every walk to this many steps")
     ap.add_argument("--walkers", type=int, default=0)
     ap.add_argument("--reps", type=int, default=3)
@@ -227,6 +228,8 @@ def main(argv=None):
     a = ap.parse_args(argv)
     if a.workload == "mag_lowfield":
         print(json.dumps(measure_mag(a.walkers, a.steps, a.reps, a.cpu_sample)))
+    elif a.workload == "wc_sphere":
+        print(json.dumps(measure_wc(a.walkers or 32768, a.steps or 22000, a.reps)))
     else:
         print(json.dumps(measure(a.workload, a.steps, a.walkers, a.reps)))
 
@@ -285,6 +288,37 @@ def measure_mag(walkers: int = 0, steps: int = 0, reps: int = 3, cpu_sample: int
         out["cpu_oracle"] = {"walker_steps_per_s": cpu_sample * (st - 1) / tc, "cores": th,
                              "sample_walkers": cpu_sample, "seconds": tc}
     return out
+
+
+
+def measure_wc(walkers: int = 32768, steps: int = 22000, reps: int = 3, device=None) -> dict:
+    """The WCDMC walker (axx_run_wc) against the main single-pore walker
+    (axx_run_single, specular) on WCcompare's sphere: radius 2.5 um, D
+    2.5 um^2/ms, dt 1 us, a cosine OGSE gradient (delta 10, spacing 2 ms)."""
+    import time
+
+    from .acquisition import CosGFunc, Sphere, run_single, run_wc, wc_start
+    pore = Sphere(0.0, 0.0, 0.0, 2.5 * UM, 0.0, 0.0, 2.5 * D1, 1, 0.0)
+    seq = CosGFunc(50 * MTM, 10.0, 2.0, 5)
+    dt = 0.001
+    grad = np.array([tuple(seq(j * dt)) for j in range(steps)], dtype=np.float64)
+    state, start = wc_start(pore, walkers, 7)
+    run_wc(pore, state, start, grad, dt, device=device)
+    t_wc = min(_timed(lambda: run_wc(pore, state, start, grad, dt, device=device))
+               for _ in range(reps))
+    run_single(pore, [seq], walkers, steps, dt, 7, device=device)
+    t_sp = min(_timed(lambda: run_single(pore, [seq], walkers, steps, dt, 7, device=device))
+               for _ in range(reps))
+    return {"workload": "wc_sphere", "walkers": walkers, "steps": steps,
+            "wc_walker_steps_per_s": walkers * steps / t_wc, "wc_seconds": t_wc,
+            "specular_walker_steps_per_s": walkers * (steps - 1) / t_sp, "specular_seconds": t_sp}
+
+
+def _timed(fn):
+    import time
+    t0 = time.perf_counter()
+    fn()
+    return time.perf_counter() - t0
 
 
 if __name__ == "__main__":

@@ -37,6 +37,10 @@
  *                       (src/substrate/RPSinitializer.h:76-186).
  *   axx_substrate_pack <- uniformCenterDist + correctEdges
  *                       (src/substrate/RPSinitializer.h:103-186) for given radii.
+ *   axx_volume_fraction <- calcf + kernelCalcf (src/util/calcf.cuh:1-38).
+ *   axx_run_wc       <- phaseAcquisitionStream<F>::runAcquisitionWC
+ *                       (src/acquisition/phaseAcquisitionStream.cuh:193-252)
+ *                       with kernelWC (src/kernels/kernelWC.cuh:13-89).
  *   axx_run_mag      <- magAcquisitionStream<F>::runAcquisition
  *                       (src/acquisition/magAcquisitionStream.cuh:37-90) with
  *                       the device work of updateWalkersMag
@@ -368,6 +372,27 @@ axx_status axx_substrate_rps_gamma(uint64_t seed, int n, double shape, double me
                                    double D_in, double T2_in, double permeability,
                                    int max_out, axx_basis *out, int *nout, double *side,
                                    double *achieved);
+
+/* Monte Carlo intracellular volume fraction (calcf / kernelCalcf,
+ * src/util/calcf.cuh:1-38): `points` uniform points in the cell (point i uses
+ * words 1..3 of stream (seed, i), as a walker's start), counted when the first
+ * basis containing them has region > 0.  Writes count / points and the count. */
+axx_status axx_volume_fraction(axx_ctx *ctx, const axx_lattice *lat, const axx_basis *basis,
+                               int nbasis, int64_t points, uint64_t seed, double *fraction,
+                               int64_t *inside);
+
+/* The WCDMC comparison walker (kernelWC, src/kernels/kernelWC.cuh:13-89, as
+ * phaseAcquisitionStream::runAcquisitionWC drives it, :193-252): walkers in
+ * one pore, per step Gaussian displacements of sigma = sqrt(2 D dt) per axis
+ * from four uniforms of a per-walker 32-bit xorshift state (Box-Muller), a
+ * move leaving the pore rejected, the Kahan-summed phase gamma dt sum_t
+ * G[t] . r.  rng_state[n], start[n*3] and grad[steps*3] (T/mm) come from the
+ * caller as the reference's driver makes them on the host; writes the phases
+ * (optional, phase[n]) and sum_cos / sum_sin of the phases (FP64). */
+axx_status axx_run_wc(axx_ctx *ctx, const axx_basis *pore, int64_t num_walkers, int32_t steps,
+                      double timestep, double gamma, const uint32_t *rng_state,
+                      const double *start, const double *grad, double *phase, double *sum_cos,
+                      double *sum_sin);
 
 /* ---- magnetisation (Bloch) walk of a single pore ------------------------- */
 

@@ -1204,6 +1204,98 @@ int orc_step(const orc_lattice *lat, const orc_basis *basis, int nbasis, const o
   return 0;
 }
 
+int orc_wc(const orc_basis *pore, int64_t n, int steps, double timestep, double gamma,
+           const uint32_t *rng_state, const double *start, const double *grad, double *phase,
+           double *sum_cos, double *sum_sin) {
+  if (!pore || n < 1 || steps < 0 || !rng_state || !start || !grad || !phase) return -1;
+  const bool sph = pore->type == 1;
+  // d_sigma = sqrt(2.0f * basis->getD() * pars->timestep)
+  const double sigma = std::sqrt(2.0f * pore->D * timestep);
+  double sc = 0.0, ss = 0.0;
+  for (int64_t i = 0; i < n; ++i) {
+    uint32_t st = rng_state[i];
+    auto uni = [&]() {  // rng_uni (:13-23)
+      uint32_t x = st;
+      x = x ^ (x >> 13);
+      x = x ^ (x << 17);
+      x = x ^ (x >> 5);
+      st = x;
+      return ((double)x + 1.0) / 4294967296.0f;
+    };
+    double x1 = start[3 * i], y1 = start[3 * i + 1], z1 = start[3 * i + 2];
+    double ph = 0.0, kc = 0.0;
+    for (int t = 0; t < steps; ++t) {
+      double r = std::sqrt(-2.0f * std::log(uni()));
+      double phi = 2.0f * kPI * (-0.5f + uni());
+      const double dx = r * std::cos(phi), dy = r * std::sin(phi);
+      r = std::sqrt(-2.0f * std::log(uni()));
+      phi = 2.0f * kPI * (-0.5f + uni());
+      const double dz = r * std::cos(phi);
+      double x2 = x1 + dx * sigma, y2 = y1 + dy * sigma, z2 = z1 + dz * sigma;
+      // Cylinder_XY / Sphere::inside(x, y, z) (cylinderXY.cuh:76-80, Sphere.cuh:96-100)
+      double q = (x2 - pore->cx) * (x2 - pore->cx) + (y2 - pore->cy) * (y2 - pore->cy);
+      if (sph) q = q + (z2 - pore->cz) * (z2 - pore->cz);
+      if (!(q < pore->radius * pore->radius)) {
+        x2 = x1;
+        y2 = y1;
+        z2 = z1;
+      }
+      const double ky = grad[3 * t] * x2 + grad[3 * t + 1] * y2 + grad[3 * t + 2] * z2 - kc;
+      const double kt = ph + ky;
+      kc = (kt - ph) - ky;
+      ph = kt;
+      x1 = x2;
+      y1 = y2;
+      z1 = z2;
+    }
+    phase[i] = ph * gamma * timestep;
+    sc += (double)std::cos((float)phase[i]);
+    ss += (double)std::sin((float)phase[i]);
+  }
+  if (sum_cos) *sum_cos = sc;
+  if (sum_sin) *sum_sin = ss;
+  return 0;
+}
+
+int orc_volume_fraction(const orc_lattice *lat, const orc_basis *basis, int nbasis,
+                        int64_t points, uint64_t seed, int mode, int nthreads, int64_t *inside) {
+  if (!lat || nbasis < 0 || (nbasis > 0 && !basis) || points < 1 || !inside) return -1;
+  if (mode != ORC_REF64 && mode != ORC_KERN32) return -1;
+  RefLattice L{};
+  L.a = lat->a;
+  L.b = lat->b;
+  L.c = lat->c;
+  for (int k = 0; k < nbasis; ++k) L.B.push_back(RefBasis{&basis[k]});
+  KGeom<float> G;
+  if (mode == ORC_KERN32) k_build(lat, basis, nbasis, 1e-12, false, false, G);
+  if (nthreads < 1) nthreads = 1;
+  if ((int64_t)nthreads > points) nthreads = (int)points;
+  std::vector<int64_t> cnt(nthreads, 0);
+  auto work = [&](int t) {
+    for (int64_t i = points * t / nthreads; i < points * (t + 1) / nthreads; ++i) {
+      Stream st{seed, (uint64_t)i, 1u};
+      if (mode == ORC_REF64) {
+        V3 r;
+        r.x = st.uniform() * L.a;
+        r.y = st.uniform() * L.b;
+        r.z = st.uniform() * L.c;
+        cnt[t] += L.region(r) > 0 ? 1 : 0;
+      } else {
+        const float x = (float)st.uniform() * G.a, y = (float)st.uniform() * G.b,
+                    z = (float)st.uniform() * G.c;
+        cnt[t] += G.region[k_lookup(G, x, y, z)] > 0 ? 1 : 0;
+      }
+    }
+  };
+  std::vector<std::thread> th;
+  for (int t = 0; t < nthreads; ++t) th.emplace_back(work, t);
+  for (auto &x : th) x.join();
+  int64_t c = 0;
+  for (auto v : cnt) c += v;
+  *inside = c;
+  return 0;
+}
+
 void orc_bfield(const orc_field *f, double gamma, const double r[3], double t, double out[3]) {
   const V3 b = bfield(*f, gamma, V3{r[0], r[1], r[2]}, t);
   out[0] = b.x;

@@ -97,6 +97,24 @@ int orc_step(const orc_lattice *lat, const orc_basis *basis, int nbasis, const o
 double orc_bvalue(const orc_sequence *q, double gamma);
 void orc_gradient(const orc_sequence *q, double t, double out[3]);
 
+/* Monte Carlo intracellular volume fraction (the algorithm of calcf /
+ * kernelCalcf, src/util/calcf.cuh:1-38): point i draws words 1..3 of stream
+ * (seed, i) as Lattice::initializeUniformly does and counts when the first
+ * basis containing it has region > 0.  REF64: FP64 positions and the
+ * reference lookup over the listed bases; KERN32: the kernel's FP32
+ * positions and instance lookup.  *inside = the count. */
+int orc_volume_fraction(const orc_lattice *lat, const orc_basis *basis, int nbasis,
+                        int64_t points, uint64_t seed, int mode, int nthreads, int64_t *inside);
+
+/* kernelWC (src/kernels/kernelWC.cuh:13-89) restated in FP64 (the reference
+ * example builds it with real = double): per walker the xorshift uniforms,
+ * Box-Muller displacements, rejection at the pore wall and the Kahan phase;
+ * phase[n] (required) and sums of cosf/sinf of each phase (the reduction
+ * evaluates cosf/sinf of the phase narrowed to float). */
+int orc_wc(const orc_basis *pore, int64_t n, int steps, double timestep, double gamma,
+           const uint32_t *rng_state, const double *start, const double *grad, double *phase,
+           double *sum_cos, double *sum_sin);
+
 /* ---- magnetisation (Bloch) path ------------------------------------------
  * The records have the layout of the product's axx_field / axx_mag_params.
  * Field kinds: 0 QSC_GRE, 1 QSC_PGSE, 2 QSC_COS_GRE, 3 QSC_GRE_TRAP,

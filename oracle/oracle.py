@@ -291,3 +291,32 @@ def bfield(field, gamma, r, t) -> np.ndarray:
     out = (C.c_double * 3)()
     lib().orc_bfield(C.byref(field), C.c_double(gamma), (C.c_double * 3)(*r), C.c_double(t), out)
     return np.array(list(out))
+
+
+def volume_fraction(lat, bases, points, seed, mode=REF64, nthreads=1) -> int:
+    """Count of the calcf points inside a basis of region > 0."""
+    b = _arr(bases, Basis)
+    n = C.c_int64()
+    rc = lib().orc_volume_fraction(C.byref(lat), b, len(bases), C.c_int64(points),
+                                   C.c_uint64(seed), mode, nthreads, C.byref(n))
+    if rc != 0:
+        raise ValueError("orc_volume_fraction failed")
+    return n.value
+
+
+def wc(pore, rng_state, start, grad, timestep, gamma=267500.0):
+    """kernelWC restated (FP64).  Returns (phase[n], sum_cos, sum_sin)."""
+    st = np.ascontiguousarray(rng_state, np.uint32)
+    p0 = np.ascontiguousarray(start, np.float64)
+    g = np.ascontiguousarray(grad, np.float64)
+    n, steps = len(st), len(g)
+    ph = np.zeros(n)
+    sc, ss = C.c_double(), C.c_double()
+    rc = lib().orc_wc(C.byref(pore), C.c_int64(n), steps, C.c_double(timestep),
+                      C.c_double(gamma), st.ctypes.data_as(C.POINTER(C.c_uint32)),
+                      p0.ctypes.data_as(C.POINTER(C.c_double)),
+                      g.ctypes.data_as(C.POINTER(C.c_double)),
+                      ph.ctypes.data_as(C.POINTER(C.c_double)), C.byref(sc), C.byref(ss))
+    if rc != 0:
+        raise ValueError("orc_wc failed")
+    return ph, sc.value, ss.value

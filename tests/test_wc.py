@@ -1,0 +1,72 @@
+"""The WCDMC comparison walker (kernelWC, src/kernels/kernelWC.cuh:13-89).
+
+The reference's kernelWC.cuh cannot be compiled for the host (the same file
+holds the reduction launchers written in CUDA launch syntax), so this
+restatement is not pinned to a reference build; it is checked against free
+diffusion (exp(-bD)) instead, and the GPU walker against it for identical
+xorshift streams and starts."""
+import math
+
+import numpy as np
+import pytest
+
+import cases
+
+
+def pgse_table(G, delta, Delta, dt, steps):
+    t = np.arange(steps) * dt
+    g = np.where(t < delta, G, np.where((t >= Delta) & (t < Delta + delta), -G, 0.0))
+    return np.stack([g, np.zeros(steps), np.zeros(steps)], axis=1)
+
+
+def big_pore_case(n):
+    from oracle import oracle as O
+    pore = O.Basis(1, 1, 0.0, 0.0, 0.0, 1.0, 2.0e-6, 0.0, 0.0, 0.0, 1e-14)  # 1 mm sphere
+    rng = np.random.default_rng(3)
+    state = rng.integers(1, 1 << 32, size=n, dtype=np.uint64).astype(np.uint32)
+    start = np.zeros((n, 3))
+    return pore, state, start
+
+
+def test_wc_oracle_free_diffusion(orc):
+    """In a pore far larger than the diffusion length the PGSE signal is
+    exp(-b D), b = gamma^2 G^2 delta^2 (Delta - delta/3)."""
+    n, dt, delta, Delta = 20000, 0.002, 4.0, 10.0
+    steps = int((Delta + delta) / dt) + 1
+    pore, state, start = big_pore_case(n)
+    G = 4e-5  # T/mm
+    ph, sc, ss = orc.wc(pore, state, start, pgse_table(G, delta, Delta, dt, steps), dt)
+    b = (267500.0 * G * delta) ** 2 * (Delta - delta / 3.0)
+    want = math.exp(-b * 2.0e-6)
+    se = math.sqrt(max(np.var(np.cos(ph)), 1e-12) / n)
+    assert abs(sc / n - want) < 4 * se + 2e-3, (sc / n, want)
+    # zero gradient: zero phase
+    ph0, sc0, _ = orc.wc(pore, state[:100], start[:100], np.zeros((50, 3)), dt)
+    assert np.all(ph0 == 0.0) and sc0 == 100.0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("sph", [False, True])
+def test_gpu_wc_against_oracle(dev, orc, sph):
+    import axonexa_gb300 as A
+    from oracle import oracle as O
+    R, D, dt = 2.5e-3, 2.5e-6, 0.001
+    n, steps = 8192, 2000
+    if sph:
+        pore_o = O.Basis(1, 1, 0.0, 0.0, 0.0, R, D, 0.0, 0.0, 0.0, 1e-14)
+        pore = A.Sphere(0.0, 0.0, 0.0, R, 0.0, 0.0, D, 1, 0.0)
+    else:
+        pore_o = O.Basis(0, 1, 0.0, 0.0, 0.0, R, D, 0.0, 0.0, 0.0, 1e-14)
+        pore = A.Cylinder_XY(0.0, 0.0, R, 0.0, 0.0, D, 1, 0.0)
+    state, start = A.wc_start(pore, n, 99)
+    grad = pgse_table(6e-5, 0.8, 1.2, dt, steps)
+    ph, sc, ss = A.run_wc(pore, state, start, grad, dt, return_phase=True, device=dev)
+    ref, rsc, rss = orc.wc(pore_o, state, start, grad, dt)
+    close = np.abs(ph - ref) <= 1e-3 * np.maximum(1.0, np.abs(ref))
+    # identical streams: FP32 and FP64 walks part only where a rejection
+    # decision sits on a rounding tie
+    assert close.mean() > 0.995, close.mean()
+    se = math.sqrt(np.var(np.cos(ref)) / n)
+    assert abs(sc - rsc) / n < 4 * se + 1e-4
+    assert abs(ss - rss) / n < 4 * math.sqrt(np.var(np.sin(ref)) / n) + 1e-4
+    assert np.all(np.isfinite(ph))
