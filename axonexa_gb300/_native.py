@@ -21,6 +21,7 @@ PRIM_CYLINDER_Z, PRIM_SPHERE = 0, 1
 SEQ_PGSE, SEQ_COS, SEQ_SIN, SEQ_APODCOS, SEQ_SQUARE = 0, 1, 2, 3, 4
 FLAG_RELAXATION, FLAG_PERMEABLE, FLAG_SIMPLE_REJECTION = 1, 2, 4
 FLAG_KEEP_INIT_QUIRK, FLAG_FIX_INIT_QUIRK = 8, 16
+FLAG_LATTICE_PICKING = 32
 INIT_UNIFORM, INIT_IN_REGION, INIT_IN_BASIS = 0, 1, 2
 
 

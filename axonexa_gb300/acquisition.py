@@ -324,14 +324,16 @@ def run_lattice(lattice: Lattice, basis: Sequence, seqs: Sequence, num_walkers: 
 
 
 def run_single(basis, seqs: Sequence, num_walkers: int, steps: int, timestep: float, seed: int,
-               *, specular=True, gamma=GAMMA, fix_init_quirk=False, device: Device = None,
-               walker_offset=0) -> RunResult:
-    """One single-pore walk (axx_run_single)."""
+               *, specular=True, gamma=GAMMA, fix_init_quirk=False, lattice_picking=False,
+               device: Device = None, walker_offset=0) -> RunResult:
+    """One single-pore walk (axx_run_single); lattice_picking: the
+    LATTICE_PICKING moves of kernelPhase.cuh:31-35."""
     dev = device or default_device()
     L = N.lib()
     M = len(seqs)
     s = N.array_of(N.SequenceRec, [q.record() for q in seqs])
-    flags = run_flags(specular) | (N.FLAG_FIX_INIT_QUIRK if fix_init_quirk else 0)
+    flags = (run_flags(specular) | (N.FLAG_FIX_INIT_QUIRK if fix_init_quirk else 0) |
+             (N.FLAG_LATTICE_PICKING if lattice_picking else 0))
     p = _params(num_walkers, steps, seed, timestep, flags, gamma=gamma, offset=walker_offset)
     out = [np.zeros(max(M, 1)) for _ in range(5)]
     ptr = [o.ctypes.data_as(C.POINTER(C.c_double)) for o in out]
@@ -358,9 +360,11 @@ def trace_lattice(lattice: Lattice, basis: Sequence, num_trace: int, steps: int,
 
 
 def trace_single(basis, num_trace: int, steps: int, timestep: float, seed: int, *,
-                 specular=True, fix_init_quirk=False, device: Device = None):
+                 specular=True, fix_init_quirk=False, lattice_picking=False,
+                 device: Device = None):
     dev = device or default_device()
-    flags = run_flags(specular) | (N.FLAG_FIX_INIT_QUIRK if fix_init_quirk else 0)
+    flags = (run_flags(specular) | (N.FLAG_FIX_INIT_QUIRK if fix_init_quirk else 0) |
+             (N.FLAG_LATTICE_PICKING if lattice_picking else 0))
     p = _params(num_trace, steps, seed, timestep, flags)
     return _trace(dev, p, num_trace, steps,
                   lambda ip, pos, reg, hit, wd: N.lib().axx_trace_single(

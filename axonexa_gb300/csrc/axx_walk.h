@@ -70,6 +70,7 @@ struct WalkParams {
   uint32_t flags;
   int init_mode, init_arg;    // AXX_INIT_*; region id for AXX_INIT_IN_REGION
   int init_quirk;             // single pore: start position drawn on a copy of the stream
+  int picking;                // single pore: LATTICE_PICKING moves
   int init_inst;              // instance used by AXX_INIT_IN_BASIS and the single pore
   int init_sph;
   float init_R, init_cx, init_cy, init_cz;

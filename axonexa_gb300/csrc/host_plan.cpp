@@ -228,6 +228,8 @@ std::string plan_lattice(const axx_lattice *lat, const axx_basis *basis, int nba
   if (!(lat->D >= 0.0) || !finite(lat->D)) return "lattice D must be >= 0";
   if (nbasis < 0 || nbasis > 60000) return "nbasis must be in [0, 60000]";
   if (nbasis > 0 && !basis) return "basis is NULL";
+  if (flags & AXX_FLAG_LATTICE_PICKING)
+    return "lattice picking exists only in the single-pore walk (kernelPhase.cuh:31-35)";
   const bool relax = flags & AXX_FLAG_RELAXATION;
   bool any_cyl = false, any_sph = false;
   for (int k = 0; k < nbasis; ++k) {

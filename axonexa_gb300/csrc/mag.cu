@@ -226,7 +226,7 @@ __global__ void __launch_bounds__(AXX_BLOCK)
             z = ez;
           }
         } else {
-          const MoveOut o = boundary<GEOM, false, true>(P, C, x, y, z, dx, dy, dz, L, v, st);
+          const MoveOut o = boundary<GEOM, false, true>(P, C, x, y, z, dx, dy, dz, L, v, st, L);
           x = o.fx;
           y = o.fy;
           z = o.fz;

@@ -160,6 +160,7 @@ void fill_walk_params(WalkParams &P, char *base, const ArenaLayout &L, const Geo
   P.init_mode = p->init_mode;
   P.init_arg = p->init_arg;
   P.init_quirk = (mode == AXX_MODE_SINGLE) && !(p->flags & AXX_FLAG_FIX_INIT_QUIRK);
+  P.picking = (mode == AXX_MODE_SINGLE) && (p->flags & AXX_FLAG_LATTICE_PICKING);
   P.init_inst = init.inst;
   P.init_sph = init.sph;
   P.init_R = (float)init.R;

@@ -268,10 +268,13 @@ struct Cands {
 // instances alike.  A cheap test decides for every candidate whether the
 // segment can meet it at all; the warp votes, and only lanes that may hit
 // run the full nearest-hit loop.
+// L is the move's segment length, Lb its path budget, which replaces L at the
+// first hit (lattice picking: a sqrt(3) L diagonal segment, budget L).
 template <int GEOM, bool PERM, bool ONE>
 __device__ __forceinline__ MoveOut boundary(const WalkParams &P, const Cands<GEOM, ONE> &C,
                                             float sx, float sy, float sz, float dx, float dy,
-                                            float dz, float L, float v, DevStream &st) {
+                                            float dz, float L, float v, DevStream &st,
+                                            float Lb) {
   bool maybe = false;
   {
     const float aa_c = fma_f(dx, dx, dy * dy);
@@ -356,10 +359,10 @@ __device__ __forceinline__ MoveOut boundary(const WalkParams &P, const Cands<GEO
       o.fz = sz;
       return o;
     }
-    ++o.hits;
     const float hx = fma_f(best, dx, sx), hy = fma_f(best, dy, sy), hz = fma_f(best, dz, sz);
     const float rem_before = rem;
-    rem = rem - best;
+    rem = (o.hits == 0 ? Lb : rem) - best;
+    ++o.hits;
     if (PERM) {
       const float u = st.next(P);
       const float ptr = div_f(C.S.slot[aux_slot(ba)].w, v);
@@ -402,18 +405,30 @@ __device__ __forceinline__ float wrap_sel(float x, float a) {
 
 // One move i of walker W with the uniforms (u1, u2); `words` is the stream
 // position after the move's draws (for traces).
-template <int GEOM, int KMAX, int KM, bool TRACE, bool ONE>
+// PICK (single pore, LATTICE_PICKING, kernelPhase.cuh:31-35): the move is
+// +-L along every axis, the signs in bits 0..2 of `signs` (x, y, z): a
+// sqrt(3) L segment along a cube diagonal with path budget L.
+template <int GEOM, int KMAX, int KM, bool TRACE, bool ONE, bool PICK = false>
 __device__ __forceinline__ void do_move(const WalkParams &P, const SmemView &S,
                                         const TraceParams &T, long long wid, int i, float u1,
                                         float u2, DevStream &st, Walker<KMAX> &W,
-                                        WalkResult &res, const float4 &g0, const float4 &a0) {
+                                        WalkResult &res, const float4 &g0, const float4 &a0,
+                                        uint32_t signs = 0u) {
   constexpr bool single = KM >= AXX_KM_SINGLE;
   constexpr bool perm = KM == AXX_KM_LAT_PERM;
   constexpr bool reject = KM == AXX_KM_LAT_REJ || KM == AXX_KM_SINGLE_REJ;
   const float4 s4 = S.slot[W.slot];
-  const float v = s4.x, L = s4.y;
-  float dx, dy, dz;
-  direction(u1, u2, dx, dy, dz);
+  const float v = s4.x, Lb = s4.y;
+  float dx, dy, dz, L = Lb;
+  if (PICK) {
+    const float k = 0.57735026918962576451f;
+    dx = (signs & 1u) ? k : -k;
+    dy = (signs & 2u) ? k : -k;
+    dz = (signs & 4u) ? k : -k;
+    L = Lb * 1.7320508075688772935f;
+  } else {
+    direction(u1, u2, dx, dy, dz);
+  }
   Cands<GEOM, ONE> C{S, g0, a0, 0u, 0u};
   if (GEOM != AXX_GEOM_FREE && !ONE) {
     const int cell = single ? 0 : cell_of<GEOM>(P, W.x, W.y, W.z);
@@ -441,7 +456,7 @@ __device__ __forceinline__ void do_move(const WalkParams &P, const SmemView &S,
     fy = back ? W.y : fy;
     fz = back ? W.z : fz;
   } else {
-    const MoveOut o = boundary<GEOM, perm, ONE>(P, C, W.x, W.y, W.z, dx, dy, dz, L, v, st);
+    const MoveOut o = boundary<GEOM, perm, ONE>(P, C, W.x, W.y, W.z, dx, dy, dz, L, v, st, Lb);
     fx = o.fx;
     fy = o.fy;
     fz = o.fz;
@@ -568,6 +583,24 @@ __device__ __forceinline__ WalkResult walk_one(const WalkParams &P, const SmemVi
     }
   }
   int i = 1;
+  if constexpr (single) {
+    if (P.picking) {
+      // LATTICE_PICKING: three raw words per move, their low bits the signs
+      // (randomSign, kernelSetup.cuh:13-15), drawn z, y, x as the compiled
+      // reference evaluates the three Vector3 constructor arguments
+      for (; i < P.steps; ++i) {
+        if ((i & 1023) == 0 && P.abort_flag != nullptr && *P.abort_flag) {
+          res.aborted = true;
+          break;
+        }
+        const uint32_t wz = st.next_word(P), wy = st.next_word(P), wx = st.next_word(P);
+        const uint32_t signs = (wx & 1u) | ((wy & 1u) << 1) | ((wz & 1u) << 2);
+        do_move<GEOM, KMAX, KM, TRACE, ONE, true>(P, S, T, wid, i, 0.f, 0.f, st, W, res, g0, a0,
+                                                  signs);
+      }
+      return res;
+    }
+  }
   // Two moves per Philox block when every walker of the warp has its stream
   // at a block boundary and moves draw nothing else (the lattice walk from a
   // uniform start); otherwise the general stream.

@@ -130,7 +130,10 @@ enum {
                                            copy of the stream, as unifRand(curandState)
                                            by value does (Sphere.cuh:55); default on in
                                            axx_run_single unless AXX_FLAG_FIX_INIT_QUIRK */
-  AXX_FLAG_FIX_INIT_QUIRK = 1u << 4
+  AXX_FLAG_FIX_INIT_QUIRK = 1u << 4,
+  AXX_FLAG_LATTICE_PICKING = 1u << 5    /* single pore, LATTICE_PICKING (kernelPhase.cuh:31-35):
+                                           every move is +-stepLength along each axis, the
+                                           signs from three stream words */
 };
 
 enum { AXX_INIT_UNIFORM = 0,     /* Lattice::initializeUniformly (lattice.cuh:31-37) */

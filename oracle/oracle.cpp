@@ -324,8 +324,12 @@ struct KMove {
 };
 
 template <typename T>
+// L: length of the move's segment; Lb: its path budget, which replaces the
+// segment length at the first hit (they differ for lattice picking, whose
+// diagonal segment is sqrt(3) L long while boundaryNormal budgets
+// speed * (dt - t_hit)).
 KMove<T> k_boundary(const KGeom<T> &G, T sx, T sy, T sz, T dx, T dy, T dz, T L, T v, bool perm,
-                    Stream &st) {
+                    Stream &st, T Lb) {
   KMove<T> o{T(0), T(0), T(0), 0, false};
   T rem = L;
   int last = -1;
@@ -350,10 +354,10 @@ KMove<T> k_boundary(const KGeom<T> &G, T sx, T sy, T sz, T dx, T dy, T dz, T L, 
       o.fz = sz;
       return o;
     }
-    ++o.hits;
     const T hx = fmaT(best, dx, sx), hy = fmaT(best, dy, sy), hz = fmaT(best, dz, sz);
     const T rem_before = rem;
-    rem = rem - best;
+    rem = (o.hits == 0 ? Lb : rem) - best;
+    ++o.hits;
     const KInst<T> &g = G.inst[bk];
     if (perm) {
       const T u = (T)st.uniform();
@@ -529,6 +533,7 @@ struct WalkIn {
   const orc_params *p;
   double gamma;
   bool single, relax, perm, reject;
+  bool pick = false;  // LATTICE_PICKING (single pore): +-L steps along each axis
 };
 
 struct WalkOut {
@@ -617,10 +622,21 @@ void walk_ref(const WalkIn &in, const RefLattice &L, int64_t w, WalkOut &out, Tr
   for (int i = 1; i < p.steps; ++i) {
     V3 ri = r;
     const double speed = in.single ? speed0 : std::sqrt(6.0 * L.getD(r) / dt);
-    const double phi = 2.0 * kPI * st.uniform();
-    const double theta = std::acos(2.0 * st.uniform() - 1);
-    r = r + V3{speed * dt * std::sin(theta) * std::cos(phi), speed * dt * std::sin(theta) * std::sin(phi),
-               speed * dt * std::cos(theta)};
+    if (in.pick) {
+      // LATTICE_PICKING (kernelPhase.cuh:31-35): stepLength * randomSign per
+      // axis, randomSign = curand % 2 ? 1 : -1 (kernelSetup.cuh:13-15); the
+      // three draws are Vector3 constructor arguments, consumed z, y, x
+      const double stepLength = speed * dt;
+      const double sz = (st.next_word() % 2) ? 1 : -1;
+      const double sy = (st.next_word() % 2) ? 1 : -1;
+      const double sx = (st.next_word() % 2) ? 1 : -1;
+      r = r + V3{stepLength * sx, stepLength * sy, stepLength * sz};
+    } else {
+      const double phi = 2.0 * kPI * st.uniform();
+      const double theta = std::acos(2.0 * st.uniform() - 1);
+      r = r + V3{speed * dt * std::sin(theta) * std::cos(phi),
+                 speed * dt * std::sin(theta) * std::sin(phi), speed * dt * std::cos(theta)};
+    }
     int hits = 0;
     if (in.single) {
       const RefBasis rb{b0};
@@ -767,19 +783,28 @@ void walk_kern(const WalkIn &in, const KGeom<T> &G, int64_t w, WalkOut &out, Tra
   const bool geom = !G.inst.empty();
   for (int i = 1; i < p.steps; ++i) {
     const T v = G.speed[slot], Ls = G.step[slot];
-    const T u1 = U(st), u2 = U(st);
-    T dx, dy, dz;
-    k_direction(u1, u2, dx, dy, dz);
+    T dx, dy, dz, Lseg = Ls;
+    if (in.pick) {
+      // the diagonal of the +-L cube, drawn z, y, x (words' low bits)
+      const T k = (T)0.57735026918962576451;
+      dz = (st.next_word() & 1u) ? k : -k;
+      dy = (st.next_word() & 1u) ? k : -k;
+      dx = (st.next_word() & 1u) ? k : -k;
+      Lseg = Ls * (T)1.7320508075688772935;
+    } else {
+      const T u1 = U(st), u2 = U(st);
+      k_direction(u1, u2, dx, dy, dz);
+    }
     T fx, fy, fz;
     int hits = 0;
     if (!geom) {
-      fx = fmaT(Ls, dx, x);
-      fy = fmaT(Ls, dy, y);
-      fz = fmaT(Ls, dz, z);
+      fx = fmaT(Lseg, dx, x);
+      fy = fmaT(Lseg, dy, y);
+      fz = fmaT(Lseg, dz, z);
     } else if (in.reject) {
-      fx = fmaT(Ls, dx, x);
-      fy = fmaT(Ls, dy, y);
-      fz = fmaT(Ls, dz, z);
+      fx = fmaT(Lseg, dx, x);
+      fy = fmaT(Lseg, dy, y);
+      fz = fmaT(Lseg, dz, z);
       if (in.single) {
         if (!(c0_of(G.inst[0], fx, fy, fz) < T(0))) {
           fx = x;
@@ -792,7 +817,7 @@ void walk_kern(const WalkIn &in, const KGeom<T> &G, int64_t w, WalkOut &out, Tra
         fz = z;
       }
     } else {
-      const KMove<T> o = k_boundary(G, x, y, z, dx, dy, dz, Ls, v, in.perm, st);
+      const KMove<T> o = k_boundary(G, x, y, z, dx, dy, dz, Lseg, v, in.perm, st, Ls);
       fx = o.fx;
       fy = o.fy;
       fz = o.fz;
@@ -1034,6 +1059,7 @@ int orc_walk(const orc_lattice *lat, const orc_basis *basis, int nbasis, const o
             lat == nullptr, false, false, (p->flags & 4u) != 0};
   in.relax = !in.single && (p->flags & 1u);
   in.perm = !in.single && (p->flags & 2u);
+  in.pick = in.single && (p->flags & 32u);
   RefLattice L{};
   if (!in.single) {
     L.a = lat->a;
@@ -1179,7 +1205,7 @@ int orc_step(const orc_lattice *lat, const orc_basis *basis, int nbasis, const o
           fz = z;
         }
       } else {
-        const KMove<T> o = k_boundary(G, x, y, z, dx, dy, dz, Ls, v, perm, st);
+        const KMove<T> o = k_boundary(G, x, y, z, dx, dy, dz, Ls, v, perm, st, Ls);
         fx = o.fx;
         fy = o.fy;
         fz = o.fz;

@@ -18,7 +18,9 @@ REFLIB = os.path.join(HERE, "_ref", "libaxxref.so")
 REF_SRC = "/root/reference"
 
 REF64, KERN64, KERN32 = 0, 1, 2
-REF_VARIANTS = ("spec_imp", "spec_imp_t2", "spec_perm", "spec_perm_t2", "rej", "rej_t2")
+REF_VARIANTS = ("spec_imp", "spec_imp_t2", "spec_perm", "spec_perm_t2", "rej", "rej_t2",
+                "pick_spec", "pick_rej")
+FLAG_LATTICE_PICKING = 32
 
 
 class Basis(C.Structure):
@@ -151,6 +153,8 @@ def ref_walk(variant, lat, bases, seqs, params, nthreads=1, ntrace=0):
 
 def variant_for(flags: int) -> str:
     spec = not (flags & 4)
+    if flags & FLAG_LATTICE_PICKING:
+        return "pick_spec" if spec else "pick_rej"
     t2 = bool(flags & 1)
     perm = bool(flags & 2)
     if spec:

@@ -45,6 +45,11 @@ def golden_cases():
     out.append(("single_sph", "spec_imp", None, [b0], seqs, cases.params(96, 1500, 17)))
     b1 = O.Basis(0, 1, 0.001, -0.002, 0.0, 4 * cases.UM, cases.D2, 0, 0, 0, 1e-14)
     out.append(("single_cyl", "spec_imp", None, [b1], seqs, cases.params(96, 1500, 18)))
+    # LATTICE_PICKING moves (kernelPhase.cuh:31-35)
+    out.append(("single_cyl_pick", "pick_spec", None, [b1], seqs,
+                cases.params(96, 1500, 19, flags=32)))
+    out.append(("single_sph_pick", "pick_spec", None, [b0], seqs,
+                cases.params(96, 1500, 20, flags=32)))
     return out
 
 

@@ -80,20 +80,44 @@ def test_trace_bit_exact_lattice(dev, orc, name, make, flags, dt):
 
 
 @pytest.mark.parametrize("sph", [0, 1])
-def test_trace_bit_exact_single_pore(dev, orc, sph):
+@pytest.mark.parametrize("flags", [0, 32, 36], ids=["spec", "pick", "pick_rej"])
+def test_trace_bit_exact_single_pore(dev, orc, sph, flags):
     import axonexa_gb300 as A
     from oracle import oracle as O
     b = O.Basis(sph, 1, 0.0 if sph else 0.001, 0.0 if sph else -0.002, 0.0, 0.004, cases.D2,
                 0, 0, 0, 1e-14)
     _, B, _ = to_product(None, [b])
     n, steps, seed = 64, 1500, 99
-    g = A.trace_single(B[0], n, steps, 0.002, seed, device=dev)
-    _, o, _ = orc.walk(None, [b], [], cases.params(n, steps, seed), orc.KERN32, ntrace=n)
+    g = A.trace_single(B[0], n, steps, 0.002, seed, specular=not (flags & 4),
+                       lattice_picking=bool(flags & 32), device=dev)
+    _, o, _ = orc.walk(None, [b], [], cases.params(n, steps, seed, flags=flags), orc.KERN32,
+                       ntrace=n)
     np.testing.assert_array_equal(g["init_pos"].astype(np.float64), o["init_pos"])
     for k in ("region", "hits", "words"):
         np.testing.assert_array_equal(g[k], o[k], err_msg=k)
     np.testing.assert_array_equal(g["pos"].astype(np.float64), o["pos"])
-    assert o["hits"].sum() > 0
+    if not flags & 4:
+        assert o["hits"].sum() > 0
+
+
+@pytest.mark.parametrize("flags", [32, 36], ids=["pick", "pick_rej"])
+def test_lattice_picking_signals_against_reference_order(dev, orc, flags):
+    """LATTICE_PICKING single-pore signals within 3 standard errors of the
+    FP64 reference-order walk (pinned to the reference's own build)."""
+    import axonexa_gb300 as A
+    from oracle import oracle as O
+    b = O.Basis(0, 1, 0.0, 0.0, 0.0, 0.004, cases.D2, 0, 0, 0, 1e-14)
+    seqs = [cases.pgse(0), cases.pgse(60), cases.cos_ogse(80, 2)]
+    L, B, S = to_product(None, [b], seqs)
+    n, steps, seed = 8192, 1200, 5
+    r = A.run_single(B[0], S, n, steps, 0.002, seed, specular=not (flags & 4),
+                     lattice_picking=True, device=dev)
+    ref, _, _ = orc.walk(None, [b], seqs, cases.params(n, steps, seed, flags=flags), orc.REF64,
+                         nthreads=8)
+    for m in range(len(seqs)):
+        mx, sxx = ref[m, 0], ref[m, 2]
+        se = math.sqrt(max(sxx / n - (mx / n) ** 2, 1e-12) / n)
+        assert abs(r.mx[m] - mx) / n < 3 * se + 1e-6, (m, r.mx[m] / n, mx / n, se)
 
 
 def test_init_modes_bit_exact(dev, orc):

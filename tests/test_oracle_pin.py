@@ -67,6 +67,26 @@ def test_oracle_matches_reference_live_packs(orc):
             np.testing.assert_array_equal(t_o[k], t_r[k], err_msg=k)
 
 
+@pytest.mark.parametrize("sph", [0, 1])
+def test_oracle_matches_reference_live_lattice_picking(orc, sph):
+    """LATTICE_PICKING single-pore walks, specular (trajectories and sums)
+    and rejection (sums: the reference's trace hook sits in boundaryNormal)."""
+    if not _ref_available(orc):
+        pytest.skip("reference walker not built here (no reference source tree)")
+    b = orc.Basis(sph, 1, 0.0 if sph else 0.001, 0.0 if sph else -0.002, 0.0, 0.004, cases.D2,
+                  0, 0, 0, 1e-14)
+    seqs = [s for s in cases.seq_mix() if s.kind != 4]
+    for flags in (32, 36):
+        p = cases.params(48, 1200, 3 + sph, flags=flags)
+        s_o, t_o, _ = orc.walk(None, [b], seqs, p, orc.REF64, ntrace=48)
+        s_r, t_r = orc.ref_walk(orc.variant_for(flags), None, [b], seqs, p, ntrace=48)
+        np.testing.assert_array_equal(s_o, s_r)
+        if flags == 32:
+            for k in ("init_pos", "pos", "region", "hits", "words"):
+                np.testing.assert_array_equal(t_o[k], t_r[k], err_msg=k)
+            assert t_o["hits"].sum() > 0
+
+
 def test_square_wave_is_rejected_by_reference_build(orc):
     # SWOGSEFunc::ampMod is pow(-1., 2 t nu): NaN for non-integer exponents,
     # so the reference build refuses it and the oracle uses the intended wave.
