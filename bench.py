@@ -16,6 +16,8 @@ Lines printed (rank 0):
                        records in and host sums out (e2e); roofline of the walk
                        kernel against the measured FP32 FMA peak; the CPU oracle
                        on a bounded sample of the same workload (cpu_baseline);
+                       "mag": the Bloch walk on the magLF low-field cell;
+                       "wc": the WCDMC walker beside the specular one;
                        "batch": the uneven 256-substrate batch in one
                        persistent graph launch against per-job launches;
                        "surrogate": tcgen05 inference signals/s on 1e6 queries
@@ -356,6 +358,8 @@ def main():
                     help="walkers per acquisition (smaller cases for profiling)")
     ap.add_argument("--no-surrogate", action="store_true", help="skip the surrogate section")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-launch section")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the magnetisation and WCDMC walker sections")
     ap.add_argument("--surrogate-only", action="store_true",
                     help="print only the surrogate section (profiling the inference kernel)")
     args = ap.parse_args()
@@ -499,6 +503,11 @@ def main():
     }
     if not args.no_batch:
         line["batch"] = batch_section(A, N, L, dev)
+    if not args.no_extra:
+        from axonexa_gb300 import workloads as W
+        # host-timed calls through the C ABI (tables uploaded per call)
+        line["mag"] = W.measure_mag(reps=3, device=dev)
+        line["wc"] = W.measure_wc(reps=3, device=dev)
     if not args.no_surrogate:
         line["surrogate"] = surrogate_section(A, N, L, dev)
     if not args.no_cpu_baseline:
