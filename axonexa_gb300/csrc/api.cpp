@@ -89,7 +89,8 @@ axx_status build_plan(axx_ctx *ctx, const GeomPlan &g, const SeqPlan &sq, int M,
     return fail(ctx, AXX_ERR_UNSUPPORTED,
                 "substrate tables and sequence sums exceed the shared-memory budget (" +
                     std::to_string(smem) + " bytes)");
-  const int occ = occupancy_walk(g.geom, kt.km, kt.kmax, false, smem);
+  const bool one = g.geo.size() == 1 && g.cstart.size() == 2;  // one instance, one cell
+  const int occ = occupancy_walk(g.geom, kt.km, kt.kmax, false, one, smem);
   if (occ <= 0) return fail(ctx, AXX_ERR_CUDA, "walk kernel cannot be resident (occupancy 0)");
   auto *pl = new axx_plan();
   pl->ctx = ctx;

@@ -107,7 +107,8 @@ extern "C" axx_status axx_run_lattice_noalloc(axx_ctx *ctx, const axx_lattice *l
   const size_t smem = walk_smem_bytes(g, M);
   if (smem > AXX_SMEM_MAX)
     return fail(ctx, AXX_ERR_UNSUPPORTED, "substrate tables exceed the shared-memory budget");
-  const int occ = occupancy_walk(g.geom, kt.km, kt.kmax, false, smem);
+  const bool one = g.geo.size() == 1 && g.cstart.size() == 2;  // one instance, one cell
+  const int occ = occupancy_walk(g.geom, kt.km, kt.kmax, false, one, smem);
   if (occ <= 0) return fail(ctx, AXX_ERR_CUDA, "walk kernel cannot be resident");
   const long long ntask = (p->num_walkers + 31) / 32;
   const long long want = (ntask + AXX_BLOCK / 32 - 1) / (AXX_BLOCK / 32);

@@ -7,10 +7,10 @@
 
 namespace axx {
 
-template <int GEOM, int KMAX, int KM, bool TRACE>
+template <int GEOM, int KMAX, int KM, bool TRACE, bool ONE = false>
 static cudaError_t walk_go(const WalkParams &P, const TraceParams &T, int grid, size_t smem,
                            cudaStream_t s) {
-  auto fn = walk_kernel<GEOM, KMAX, KM, TRACE>;
+  auto fn = walk_kernel<GEOM, KMAX, KM, TRACE, ONE>;
   if (smem > 48 * 1024) {
     const cudaError_t e =
         cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -20,9 +20,9 @@ static cudaError_t walk_go(const WalkParams &P, const TraceParams &T, int grid, 
   return cudaGetLastError();
 }
 
-template <int GEOM, int KMAX, int KM, bool TRACE>
+template <int GEOM, int KMAX, int KM, bool TRACE, bool ONE = false>
 static int walk_occ(size_t smem) {
-  auto fn = walk_kernel<GEOM, KMAX, KM, TRACE>;
+  auto fn = walk_kernel<GEOM, KMAX, KM, TRACE, ONE>;
   if (smem > 48 * 1024 &&
       cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
           cudaSuccess)
@@ -33,9 +33,38 @@ static int walk_occ(size_t smem) {
   return n;
 }
 
+// ONE: instantiations compiled for a single instance.  Single-pore modes
+// (KM >= AXX_KM_SINGLE) always have one; lattices use them for up to four
+// channels without traces when the plan has one instance and one cell.
 template <int GEOM, int KM>
-static cudaError_t walk_launch_km(int kmax, bool trace, const WalkParams &P,
+constexpr bool walk_one_variant(int kmax, bool trace, bool one) {
+  return KM >= AXX_KM_SINGLE ||
+         (one && !trace && kmax <= 4 && (GEOM == AXX_GEOM_CYL || GEOM == AXX_GEOM_SPH));
+}
+
+template <int GEOM, int KM>
+static cudaError_t walk_launch_km(int kmax, bool trace, bool one, const WalkParams &P,
                                   const TraceParams &T, int grid, size_t smem, cudaStream_t s) {
+  constexpr bool single = KM >= AXX_KM_SINGLE;
+  constexpr bool lat1 = !single && (GEOM == AXX_GEOM_CYL || GEOM == AXX_GEOM_SPH);
+  if (single) {
+    if (trace) return walk_go<GEOM, 1, KM, true, single>(P, T, grid, smem, s);
+    switch (kmax) {
+      case 1: return walk_go<GEOM, 1, KM, false, single>(P, T, grid, smem, s);
+      case 2: return walk_go<GEOM, 2, KM, false, single>(P, T, grid, smem, s);
+      case 4: return walk_go<GEOM, 4, KM, false, single>(P, T, grid, smem, s);
+      case 8: return walk_go<GEOM, 8, KM, false, single>(P, T, grid, smem, s);
+      case 16: return walk_go<GEOM, 16, KM, false, single>(P, T, grid, smem, s);
+    }
+    return cudaErrorInvalidValue;
+  }
+  if (lat1 && walk_one_variant<GEOM, KM>(kmax, trace, one)) {
+    switch (kmax) {
+      case 1: return walk_go<GEOM, 1, KM, false, lat1>(P, T, grid, smem, s);
+      case 2: return walk_go<GEOM, 2, KM, false, lat1>(P, T, grid, smem, s);
+      case 4: return walk_go<GEOM, 4, KM, false, lat1>(P, T, grid, smem, s);
+    }
+  }
   if (trace) return walk_go<GEOM, 1, KM, true>(P, T, grid, smem, s);
   switch (kmax) {
     case 1: return walk_go<GEOM, 1, KM, false>(P, T, grid, smem, s);
@@ -48,7 +77,27 @@ static cudaError_t walk_launch_km(int kmax, bool trace, const WalkParams &P,
 }
 
 template <int GEOM, int KM>
-static int walk_occ_km(int kmax, bool trace, size_t smem) {
+static int walk_occ_km(int kmax, bool trace, bool one, size_t smem) {
+  constexpr bool single = KM >= AXX_KM_SINGLE;
+  constexpr bool lat1 = !single && (GEOM == AXX_GEOM_CYL || GEOM == AXX_GEOM_SPH);
+  if (single) {
+    if (trace) return walk_occ<GEOM, 1, KM, true, single>(smem);
+    switch (kmax) {
+      case 1: return walk_occ<GEOM, 1, KM, false, single>(smem);
+      case 2: return walk_occ<GEOM, 2, KM, false, single>(smem);
+      case 4: return walk_occ<GEOM, 4, KM, false, single>(smem);
+      case 8: return walk_occ<GEOM, 8, KM, false, single>(smem);
+      case 16: return walk_occ<GEOM, 16, KM, false, single>(smem);
+    }
+    return 0;
+  }
+  if (lat1 && walk_one_variant<GEOM, KM>(kmax, trace, one)) {
+    switch (kmax) {
+      case 1: return walk_occ<GEOM, 1, KM, false, lat1>(smem);
+      case 2: return walk_occ<GEOM, 2, KM, false, lat1>(smem);
+      case 4: return walk_occ<GEOM, 4, KM, false, lat1>(smem);
+    }
+  }
   if (trace) return walk_occ<GEOM, 1, KM, true>(smem);
   switch (kmax) {
     case 1: return walk_occ<GEOM, 1, KM, false>(smem);

@@ -641,7 +641,10 @@ __device__ __forceinline__ double warp_sum(double v) {
 
 // The walk kernel.  Dynamic shared memory: [warps][M][5] FP64 sums, then the
 // instances, slot table, cell starts, slot regions and cell lists.
-template <int GEOM, int KMAX, int KM, bool TRACE>
+// ONEONLY: compiled for substrates of a single instance only (the host checks
+// n_inst == 1 and ncell == 1); the list path is left out, which frees
+// registers for one more resident block per SM.
+template <int GEOM, int KMAX, int KM, bool TRACE, bool ONEONLY = false>
 __global__ void __launch_bounds__(AXX_BLOCK, AXX_MIN_BLOCKS_FOR(KMAX))
     walk_kernel(const __grid_constant__ WalkParams P, const __grid_constant__ TraceParams T) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -692,8 +695,12 @@ __global__ void __launch_bounds__(AXX_BLOCK, AXX_MIN_BLOCKS_FOR(KMAX))
     for (int c = 0; c < KMAX; ++c) W.acc[c] = W.cmp[c] = 0.0f;
     W.t2s = W.t2c = 0.0f;
     if (active) {
-      const WalkResult r = one ? walk_one<GEOM, KMAX, KM, TRACE, true>(P, S, T, wid, W)
-                               : walk_one<GEOM, KMAX, KM, TRACE, false>(P, S, T, wid, W);
+      WalkResult r;
+      if constexpr (ONEONLY)
+        r = walk_one<GEOM, KMAX, KM, TRACE, true>(P, S, T, wid, W);
+      else
+        r = one ? walk_one<GEOM, KMAX, KM, TRACE, true>(P, S, T, wid, W)
+                : walk_one<GEOM, KMAX, KM, TRACE, false>(P, S, T, wid, W);
       caps += r.caps;
       hits += r.hits;
       init_fail += r.init_fail ? 1u : 0u;
