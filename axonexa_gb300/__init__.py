@@ -5,7 +5,7 @@ include/axx.h (libaxx.so, built in-tree by ``axonexa_gb300.build``).  This
 package is the host-side mirror of the reference's acquisition API.
 """
 from .acquisition import (GAMMA, PI, ApodCosGFunc, CosGFunc, Cylinder_XY, Device, Lattice,
-                          RectGrad, RunResult, SinGFunc, Sphere, SWOGSEFunc, Vector3,
+                          Plane, RectGrad, RunResult, SinGFunc, Sphere, SWOGSEFunc, Vector3,
                           default_device, linear_regression, phaseAcquisition,
                           phaseAcquisitionStream, philox_words, run_lattice, run_single,
                           trace_lattice, trace_single)

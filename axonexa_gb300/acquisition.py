@@ -105,6 +105,38 @@ class Sphere:
                        self.radius, self.D, self.T2, self.T1, self.permeability, self.eps)
 
 
+class Plane:
+    """Infinite impermeable wall through ``center`` with normal ``normal``
+    (plane.cuh:1-40).  It has no inside: it never holds a walker's region,
+    D or T2 (getRegion 0, getT2/getD -1), reflects every crossing and
+    transmits nothing.  Lattice bases only (planePhase.cu: walls at x = 0 and
+    x = l of an l-wide cell make parallel plates).  The normal is normalised
+    by the library."""
+
+    def __init__(self, center, normal, eps=1e-14):
+        self.center = tuple(float(v) for v in center)
+        self.normal = tuple(float(v) for v in normal)
+        self.eps = float(eps)
+        self.region = 0
+
+    def inside(self, r) -> bool:
+        return False
+
+    def getNormal(self, r=None):
+        return Vector3(*self.normal)
+
+    def getRegion(self, r=None):
+        return 0
+
+    def getPermeability(self):
+        return 0.0
+
+    def record(self) -> N.Basis:
+        c, n = self.center, self.normal
+        return N.Basis(N.PRIM_PLANE, 0, c[0], c[1], c[2], 0.0, 0.0, 0.0, 0.0, 0.0, self.eps,
+                       n[0], n[1], n[2])
+
+
 class Lattice:
     """Periodic a x b x c cell with the extracellular T2, T1, D (lattice.cuh:14-23)."""
 

@@ -197,6 +197,13 @@ static void slot_entry(double D, double T2, double kappa, double dt, bool relax,
 }
 
 static std::string check_basis(const axx_basis &b) {
+  if (b.type == AXX_PRIM_PLANE) {
+    if (!finite(b.cx) || !finite(b.cy) || !finite(b.cz) || !finite(b.nx) || !finite(b.ny) ||
+        !finite(b.nz) || !finite(b.eps) || b.eps < 0.0)
+      return "plane parameters must be finite (eps >= 0)";
+    if (!(b.nx * b.nx + b.ny * b.ny + b.nz * b.nz > 1e-24)) return "plane normal must be nonzero";
+    return "";
+  }
   if (b.type != AXX_PRIM_CYLINDER_Z && b.type != AXX_PRIM_SPHERE) return "unknown basis type";
   if (!(b.radius > 0.0) || !finite(b.radius)) return "basis radius must be > 0";
   if (!(b.D >= 0.0) || !finite(b.D)) return "basis D must be >= 0";
@@ -210,9 +217,23 @@ static float4 geo_of(double cx, double cy, double cz, double R) {
   return make_float4((float)cx, (float)cy, (float)cz, (float)(-(R * R)));
 }
 
+// A plane instance: geo = (n, n.c) with the unit normal n and a point c of
+// the plane; aux.x is unused.
+static float4 plane_geo(const double n[3], double cx, double cy, double cz) {
+  return make_float4((float)n[0], (float)n[1], (float)n[2],
+                     (float)(n[0] * cx + n[1] * cy + n[2] * cz));
+}
+
+static void unit_normal(const axx_basis &b, double n[3]) {
+  const double m = std::sqrt(b.nx * b.nx + b.ny * b.ny + b.nz * b.nz);
+  n[0] = b.nx / m;
+  n[1] = b.ny / m;
+  n[2] = b.nz / m;
+}
+
 static float4 aux_of(const axx_basis &b, int slot) {
   float4 a;
-  a.x = (float)(1.0 / b.radius);
+  a.x = b.type == AXX_PRIM_PLANE ? 1.0f : (float)(1.0 / b.radius);
   a.y = (float)b.eps;
   int s = slot, t = b.type;
   std::memcpy(&a.z, &s, 4);
@@ -231,25 +252,34 @@ std::string plan_lattice(const axx_lattice *lat, const axx_basis *basis, int nba
   if (flags & AXX_FLAG_LATTICE_PICKING)
     return "lattice picking exists only in the single-pore walk (kernelPhase.cuh:31-35)";
   const bool relax = flags & AXX_FLAG_RELAXATION;
-  bool any_cyl = false, any_sph = false;
+  bool any_cyl = false, any_sph = false, any_plane = false;
   for (int k = 0; k < nbasis; ++k) {
     std::string e = check_basis(basis[k]);
     if (!e.empty()) return e;
     if (basis[k].type == AXX_PRIM_SPHERE) any_sph = true;
+    else if (basis[k].type == AXX_PRIM_PLANE) any_plane = true;
     else any_cyl = true;
   }
   if (relax) {
     if (!(lat->T2 > 0.0)) return "relaxation needs lattice T2 > 0";
     for (int k = 0; k < nbasis; ++k)
-      if (!(basis[k].T2 > 0.0)) return "relaxation needs basis T2 > 0";
+      if (basis[k].type != AXX_PRIM_PLANE && !(basis[k].T2 > 0.0))
+        return "relaxation needs basis T2 > 0";
   }
+  // planes run in the mixed-type kernels (per-instance type)
   g.geom = nbasis == 0 ? AXX_GEOM_FREE
-                       : (any_cyl && any_sph ? AXX_GEOM_MIX
-                                             : (any_sph ? AXX_GEOM_SPH : AXX_GEOM_CYL));
+                       : ((any_cyl && any_sph) || any_plane
+                              ? AXX_GEOM_MIX
+                              : (any_sph ? AXX_GEOM_SPH : AXX_GEOM_CYL));
   g.slot_tab.resize(nbasis + 1);
   g.slot_region.resize(nbasis + 1);
   for (int k = 0; k < nbasis; ++k) {
-    slot_entry(basis[k].D, basis[k].T2, basis[k].permeability, dt, relax, g.slot_tab[k]);
+    if (basis[k].type == AXX_PRIM_PLANE) {
+      // never a walker's region; only its zero transmission is read
+      slot_entry(lat->D, lat->T2, 0.0, dt, relax, g.slot_tab[k]);
+    } else {
+      slot_entry(basis[k].D, basis[k].T2, basis[k].permeability, dt, relax, g.slot_tab[k]);
+    }
     g.slot_region[k] = basis[k].region;
   }
   slot_entry(lat->D, lat->T2, 0.0, dt, relax, g.slot_tab[nbasis]);
@@ -273,9 +303,26 @@ std::string plan_lattice(const axx_lattice *lat, const axx_basis *basis, int nba
     int k;
     double cx, cy, cz, R;
     int type;
+    double n[3];  // unit normal of a plane
   };
   std::vector<Inst> inst;
+  // a plane meets a box when the signed distances n.(x - c) of the box's
+  // corners do not all have one sign
+  auto plane_meets = [](const Inst &q, double x0, double x1, double y0, double y1, double z0,
+                        double z1) {
+    double lo = 0.0, hi = 0.0;
+    const double xs[2] = {x0, x1}, ys[2] = {y0, y1}, zs[2] = {z0, z1};
+    for (int i = 0; i < 8; ++i) {
+      const double d = q.n[0] * (xs[i & 1] - q.cx) + q.n[1] * (ys[(i >> 1) & 1] - q.cy) +
+                       q.n[2] * (zs[i >> 2] - q.cz);
+      lo = i ? std::min(lo, d) : d;
+      hi = i ? std::max(hi, d) : d;
+    }
+    return lo <= 0.0 && hi >= 0.0;
+  };
   auto reach = [&](const Inst &q) {
+    if (q.type == AXX_PRIM_PLANE)
+      return plane_meets(q, -dil, A + dil, -dil, B + dil, -dil, C + dil);
     // distance from the centre to the cell box dilated by dil
     auto axis = [](double c, double lo, double hi) {
       return c < lo ? lo - c : (c > hi ? c - hi : 0.0);
@@ -292,6 +339,17 @@ std::string plan_lattice(const axx_lattice *lat, const axx_basis *basis, int nba
     for (int j = 0; j < nbasis; ++j) {
       const axx_basis &o = basis[j];
       if (o.type != q.type) continue;
+      if (q.type == AXX_PRIM_PLANE) {
+        // the same plane: parallel normals (either sense) and q's point on it
+        double n[3];
+        unit_normal(o, n);
+        const double cr = std::fabs(n[1] * q.n[2] - n[2] * q.n[1]) +
+                          std::fabs(n[2] * q.n[0] - n[0] * q.n[2]) +
+                          std::fabs(n[0] * q.n[1] - n[1] * q.n[0]);
+        const double d = n[0] * (q.cx - o.cx) + n[1] * (q.cy - o.cy) + n[2] * (q.cz - o.cz);
+        if (cr < 1e-12 && std::fabs(d) <= tol) return true;
+        continue;
+      }
       if (std::fabs(o.radius - q.R) > tol) continue;
       if (std::fabs(o.cx - q.cx) > tol || std::fabs(o.cy - q.cy) > tol) continue;
       if (q.type == AXX_PRIM_SPHERE && std::fabs(o.cz - q.cz) > tol) continue;
@@ -301,27 +359,33 @@ std::string plan_lattice(const axx_lattice *lat, const axx_basis *basis, int nba
   };
   for (int k = 0; k < nbasis; ++k) {
     const axx_basis &b = basis[k];
-    inst.push_back({k, b.cx, b.cy, b.cz, b.radius, b.type});
-    const int zr = b.type == AXX_PRIM_SPHERE ? 1 : 0;
+    Inst q0{k, b.cx, b.cy, b.cz, b.radius, b.type, {0.0, 0.0, 0.0}};
+    if (b.type == AXX_PRIM_PLANE) unit_normal(b, q0.n);
+    inst.push_back(q0);
+    const int zr = b.type == AXX_PRIM_CYLINDER_Z ? 0 : 1;
     for (int i = -1; i <= 1; ++i)
       for (int j = -1; j <= 1; ++j)
         for (int l = -zr; l <= zr; ++l) {
           if (i == 0 && j == 0 && l == 0) continue;
-          Inst q{k, b.cx + A * i, b.cy + B * j, b.cz + C * l, b.radius, b.type};
+          Inst q = q0;
+          q.cx += A * i;
+          q.cy += B * j;
+          q.cz += C * l;
           if (!reach(q) || coincides(q)) continue;
           inst.push_back(q);
         }
   }
   if (inst.size() > 65535) return "too many basis instances (ghosts included)";
   for (auto &q : inst) {
-    g.geo.push_back(geo_of(q.cx, q.cy, q.cz, q.R));
+    g.geo.push_back(q.type == AXX_PRIM_PLANE ? plane_geo(q.n, q.cx, q.cy, q.cz)
+                                             : geo_of(q.cx, q.cy, q.cz, q.R));
     g.aux.push_back(aux_of(basis[q.k], q.k));
   }
   // grid over the cell
   const double h = std::max(2.0 * (double)lmax, std::sqrt(A * B / (double)nbasis));
   g.gx = (int)std::min(64.0, std::max(1.0, std::floor(A / h)));
   g.gy = (int)std::min(64.0, std::max(1.0, std::floor(B / h)));
-  g.gz = any_sph ? (int)std::min(64.0, std::max(1.0, std::floor(C / h))) : 1;
+  g.gz = (any_sph || any_plane) ? (int)std::min(64.0, std::max(1.0, std::floor(C / h))) : 1;
   g.inv_hx = (float)((double)g.gx / A);
   g.inv_hy = (float)((double)g.gy / B);
   g.inv_hz = (float)((double)g.gz / C);
@@ -340,6 +404,12 @@ std::string plan_lattice(const axx_lattice *lat, const axx_basis *basis, int nba
         const double sx = 1e-5 * A / g.gx, sy = 1e-5 * B / g.gy, sz = 1e-5 * C / g.gz;
         for (size_t n = 0; n < inst.size(); ++n) {
           const Inst &q = inst[n];
+          if (q.type == AXX_PRIM_PLANE) {
+            if (plane_meets(q, x0 - dil - sx, x1 + dil + sx, y0 - dil - sy, y1 + dil + sy,
+                            z0 - dil - sz, z1 + dil + sz))
+              g.clist.push_back((uint16_t)n);
+            continue;
+          }
           auto axis = [](double c, double lo, double hi) {
             return c < lo ? lo - c : (c > hi ? c - hi : 0.0);
           };
@@ -363,6 +433,7 @@ std::string plan_single(const axx_basis *basis, double dt, GeomPlan &g, float &s
   if (!basis) return "basis is NULL";
   std::string e = check_basis(*basis);
   if (!e.empty()) return e;
+  if (basis->type == AXX_PRIM_PLANE) return "a plane is not a pore (it has no inside)";
   g.geom = basis->type == AXX_PRIM_SPHERE ? AXX_GEOM_SPH : AXX_GEOM_CYL;
   g.geo.push_back(geo_of(basis->cx, basis->cy, basis->cz, basis->radius));
   g.aux.push_back(aux_of(*basis, 0));

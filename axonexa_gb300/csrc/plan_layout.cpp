@@ -101,6 +101,8 @@ std::string init_spec(const GeomPlan &g, const axx_basis *basis, int nbasis, int
     if (p->init_arg < 0 || p->init_arg >= nbasis)
       return "init_arg must name a basis for AXX_INIT_IN_BASIS";
     k = p->init_arg;
+    if (basis[k].type == AXX_PRIM_PLANE)
+      return "a plane has no inside to start walkers in (AXX_INIT_IN_BASIS)";
   }
   if (k < 0) return "";
   for (int n = 0; n < (int)g.aux.size(); ++n) {

@@ -191,6 +191,7 @@ extern "C" axx_status axx_substrate_pack(uint64_t seed, int n, const double *rad
     b.T1 = 0.0;
     b.permeability = permeability;
     b.eps = 1e-14 * L;
+    b.nx = b.ny = b.nz = 0.0;
     return true;
   };
   for (int i = 0; i < n; ++i)

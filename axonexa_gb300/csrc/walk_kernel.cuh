@@ -95,6 +95,13 @@ __device__ __forceinline__ bool is_sphere(const float4 &aux) {
   return aux_type(aux) == 1;
 }
 
+// Planes (type 2) occur only in the mixed-type kernels.
+template <int GEOM>
+__device__ __forceinline__ bool is_plane(const float4 &aux) {
+  if (GEOM != AXX_GEOM_MIX) return false;
+  return aux_type(aux) == 2;
+}
+
 // |p|^2 - R^2 for the point (x, y, z) against one instance.
 __device__ __forceinline__ float c0_of(const float4 &g, bool sph, float x, float y, float z) {
   const float px = x - g.x, py = y - g.y;
@@ -105,6 +112,15 @@ __device__ __forceinline__ float c0_of(const float4 &g, bool sph, float x, float
   return fma_f(px, px, fma_f(py, py, g.w));
 }
 
+// Whether an instance contains the point; a plane contains none (it has no
+// inside: Lattice::inRegion never reports it).
+template <int GEOM>
+__device__ __forceinline__ bool contains(const float4 &g, const float4 &aux, float x, float y,
+                                         float z) {
+  if (is_plane<GEOM>(aux)) return false;
+  return c0_of(g, is_sphere<GEOM>(aux), x, y, z) < 0.0f;
+}
+
 // First instance (ascending basis order) of list [b, e) that contains the
 // point; its slot, or the extracellular slot.
 template <int GEOM>
@@ -113,9 +129,26 @@ __device__ __forceinline__ int lookup_list(const SmemView &S, uint32_t b, uint32
   for (uint32_t j = b; j < e; ++j) {
     const int k = S.clist[j];
     const float4 aux = S.aux[k];
-    if (c0_of(S.geo[k], is_sphere<GEOM>(aux), x, y, z) < 0.0f) return aux_slot(aux);
+    if (contains<GEOM>(S.geo[k], aux, x, y, z)) return aux_slot(aux);
   }
   return ecs;
+}
+
+// Distance along the unit direction d from the start s to a plane
+// g = (n, n.c), if in (0, rem) and >= eps, or +inf (Plane::intersect,
+// plane.cuh:19-28: v = n.(c - ri) / n.dr on the segment, with the segment
+// length folded in; the plane just reflected from is skipped, as its
+// doub_equal test drops the zero root).  A direction parallel to the plane
+// divides by zero and fails the range test.
+__device__ __forceinline__ float plane_hit(const float4 &g, float eps, bool on_surface,
+                                           float sx, float sy, float sz, float dx, float dy,
+                                           float dz, float rem) {
+  if (on_surface) return AXX_INF;
+  const float np = fma_f(g.x, sx, fma_f(g.y, sy, g.z * sz));
+  const float dn = fma_f(g.x, dx, fma_f(g.y, dy, g.z * dz));
+  const float s = div_f(g.w - np, dn);
+  if (!(s > 0.0f && s < rem && s >= eps)) return AXX_INF;
+  return s;
 }
 
 // Distance to the first boundary of one instance along the segment
@@ -259,7 +292,7 @@ struct Cands {
   float4 g0, a0;
   uint32_t b, e;
   __device__ __forceinline__ int lookup(int ecs, float x, float y, float z) const {
-    if (ONE) return (c0_of(g0, is_sphere<GEOM>(a0), x, y, z) < 0.0f) ? aux_slot(a0) : ecs;
+    if (ONE) return contains<GEOM>(g0, a0, x, y, z) ? aux_slot(a0) : ecs;
     return lookup_list<GEOM>(S, b, e, ecs, x, y, z);
   }
 };
@@ -279,7 +312,11 @@ __device__ __forceinline__ MoveOut boundary(const WalkParams &P, const Cands<GEO
   {
     const float aa_c = fma_f(dx, dx, dy * dy);
     const float aa_s = fma_f(dx, dx, fma_f(dy, dy, dz * dz));
-    auto may = [&](const float4 &g, bool sph) {
+    auto may = [&](const float4 &g, const float4 &aux) {
+      // a plane: the test of the nearest-hit loop's first pass itself
+      if (is_plane<GEOM>(aux))
+        return plane_hit(g, aux.y, false, sx, sy, sz, dx, dy, dz, L) < AXX_INF;
+      const bool sph = is_sphere<GEOM>(aux);
       const float px = sx - g.x, py = sy - g.y;
       const float pz = sph ? (sz - g.z) : 0.0f;
       const float ex = fma_f(L, dx, px), ey = fma_f(L, dy, py);
@@ -303,11 +340,11 @@ __device__ __forceinline__ MoveOut boundary(const WalkParams &P, const Cands<GEO
       return !no;
     };
     if (ONE) {
-      maybe = may(C.g0, is_sphere<GEOM>(C.a0));
+      maybe = may(C.g0, C.a0);
     } else {
       for (uint32_t j = C.b; j < C.e; ++j) {
         const int k = C.S.clist[j];
-        maybe |= may(C.S.geo[k], is_sphere<GEOM>(C.S.aux[k]));
+        maybe |= may(C.S.geo[k], C.S.aux[k]);
       }
     }
   }
@@ -330,7 +367,10 @@ __device__ __forceinline__ MoveOut boundary(const WalkParams &P, const Cands<GEO
     float4 bg, ba;
     if (ONE) {
       const bool sph = is_sphere<GEOM>(C.a0);
-      best = seg_hit(C.g0, C.a0.y, sph, last == 0, sx, sy, sz, dx, dy, dz, sph ? aa_s : aa_c, rem);
+      best = is_plane<GEOM>(C.a0)
+                 ? plane_hit(C.g0, C.a0.y, last == 0, sx, sy, sz, dx, dy, dz, rem)
+                 : seg_hit(C.g0, C.a0.y, sph, last == 0, sx, sy, sz, dx, dy, dz,
+                           sph ? aa_s : aa_c, rem);
       if (best < AXX_INF) bk = 0;
       bg = C.g0;
       ba = C.a0;
@@ -339,8 +379,11 @@ __device__ __forceinline__ MoveOut boundary(const WalkParams &P, const Cands<GEO
         const int k = C.S.clist[j];
         const float4 aux = C.S.aux[k];
         const bool sph = is_sphere<GEOM>(aux);
-        const float s = seg_hit(C.S.geo[k], aux.y, sph, k == last, sx, sy, sz, dx, dy, dz,
-                                sph ? aa_s : aa_c, rem);
+        const float s =
+            is_plane<GEOM>(aux)
+                ? plane_hit(C.S.geo[k], aux.y, k == last, sx, sy, sz, dx, dy, dz, rem)
+                : seg_hit(C.S.geo[k], aux.y, sph, k == last, sx, sy, sz, dx, dy, dz,
+                          sph ? aa_s : aa_c, rem);
         if (s < best) {
           best = s;
           bk = k;
@@ -378,14 +421,25 @@ __device__ __forceinline__ MoveOut boundary(const WalkParams &P, const Cands<GEO
         return o;
       }
     }
-    const bool sph = is_sphere<GEOM>(ba);
-    const float nx = (hx - bg.x) * ba.x, ny = (hy - bg.y) * ba.x;
-    const float nz = sph ? (hz - bg.z) * ba.x : 0.0f;
-    const float dn = sph ? fma_f(dx, nx, fma_f(dy, ny, dz * nz)) : fma_f(dx, nx, dy * ny);
+    // unit normal: radial for cylinders and spheres, the stored normal of a
+    // plane (Plane::getNormal)
+    const bool pl = is_plane<GEOM>(ba);
+    const bool n3 = is_sphere<GEOM>(ba) || pl;
+    float nx, ny, nz;
+    if (pl) {
+      nx = bg.x;
+      ny = bg.y;
+      nz = bg.z;
+    } else {
+      nx = (hx - bg.x) * ba.x;
+      ny = (hy - bg.y) * ba.x;
+      nz = n3 ? (hz - bg.z) * ba.x : 0.0f;
+    }
+    const float dn = n3 ? fma_f(dx, nx, fma_f(dy, ny, dz * nz)) : fma_f(dx, nx, dy * ny);
     const float t = -2.0f * dn;
     dx = fma_f(t, nx, dx);
     dy = fma_f(t, ny, dy);
-    if (sph) dz = fma_f(t, nz, dz);
+    if (n3) dz = fma_f(t, nz, dz);
     sx = hx;
     sy = hy;
     sz = hz;
@@ -576,7 +630,7 @@ __device__ __forceinline__ WalkResult walk_one(const WalkParams &P, const SmemVi
   W.slot = single ? 0 : P.ecs_slot;
   if (!single && GEOM != AXX_GEOM_FREE) {
     if (ONE) {
-      W.slot = (c0_of(g0, is_sphere<GEOM>(a0), x, y, z) < 0.0f) ? aux_slot(a0) : P.ecs_slot;
+      W.slot = contains<GEOM>(g0, a0, x, y, z) ? aux_slot(a0) : P.ecs_slot;
     } else {
       const int cell = cell_of<GEOM>(P, x, y, z);
       W.slot = lookup_list<GEOM>(S, S.cstart[cell], S.cstart[cell + 1], P.ecs_slot, x, y, z);

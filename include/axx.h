@@ -80,19 +80,28 @@ typedef struct axx_plan axx_plan;
 /* ---- geometry ------------------------------------------------------------ */
 
 enum { AXX_PRIM_CYLINDER_Z = 0, /* Cylinder_XY: infinite cylinder, axis along z */
-       AXX_PRIM_SPHERE = 1 };   /* Sphere */
+       AXX_PRIM_SPHERE = 1,     /* Sphere */
+       AXX_PRIM_PLANE = 2 };    /* Plane: infinite impermeable wall (lattices only) */
 
-/* One basis object (src/primitives/cylinderXY.cuh:1-40, Sphere.cuh:4-44). */
+/* One basis object (src/primitives/cylinderXY.cuh:1-40, Sphere.cuh:4-44,
+ * plane.cuh:1-40).  A plane is the wall through (cx, cy, cz) with normal
+ * (nx, ny, nz) (normalised by the library; Plane::getNormal returns it as
+ * given and the reflection assumes unit length).  It has no inside: it never
+ * contains a point (no region, D or T2 of its own), reflects every crossing
+ * and transmits nothing (Plane::getPermeability is 0); radius, D, T2, T1 and
+ * permeability are ignored for it. */
 typedef struct {
   int32_t type;          /* AXX_PRIM_* */
   int32_t region;        /* value reported by the region lookup (Lattice::inRegion) */
-  double cx, cy, cz;     /* centre; cz is ignored for cylinders */
+  double cx, cy, cz;     /* centre (a point of a plane); cz is ignored for cylinders */
   double radius;
   double D;              /* diffusion coefficient inside */
   double T2;             /* transverse relaxation time inside */
   double T1;             /* carried for layout parity; unused on the phase path */
   double permeability;   /* kappa; transmission probability is 4*kappa/v */
-  double eps;            /* minimum hit distance (cylEPS / sphereEPS) */
+  double eps;            /* minimum hit distance (cylEPS / sphereEPS; doub_equal's
+                            1e-14 for a plane) */
+  double nx, ny, nz;     /* plane normal; ignored for cylinders and spheres */
 } axx_basis;
 
 /* Periodic cell (src/substrate/lattice.cuh:3-23): a x b x c box with the

@@ -114,7 +114,11 @@ int sgn(double v) { return (0.0 < v) - (v < 0.0); }  // misc.cuh:3
 struct RefBasis {
   const orc_basis *b;
   bool sph() const { return b->type == 1; }
+  bool plane() const { return b->type == 2; }
   bool inside(V3 r) const {  // cylinderXY.cuh:69-74, Sphere.cuh:89-94
+    // Plane (plane.cuh:1-40) defines no inside; Lattice's region, D and T2
+    // lookups pass over it to the next basis or the lattice
+    if (plane()) return false;
     const double cx = b->cx, cy = b->cy, cz = b->cz, R = b->radius;
     if (sph())
       return (r.x - cx) * (r.x - cx) + (r.y - cy) * (r.y - cy) + (r.z - cz) * (r.z - cz) < R * R;
@@ -122,6 +126,12 @@ struct RefBasis {
   }
   // cylinderXY.cuh:82-122, Sphere.cuh:102-139
   bool intersect(V3 ri, V3 rf, double &v) const {
+    if (plane()) {  // plane.cuh:19-28 (doub_equal: |x| < 1e-14)
+      const V3 dr = rf - ri;
+      const V3 n{b->nx, b->ny, b->nz}, pdr = V3{b->cx, b->cy, b->cz} - ri;
+      v = dot(n, pdr) / dot(n, dr);
+      return v > 0.0 && v < 1.0 && !(std::fabs(v * mag(dr) - 0.0) < 1e-14);
+    }
     const double cx = b->cx, cy = b->cy, cz = b->cz, R = b->radius;
     const V3 dr = rf - ri;
     const double step_mag = mag(dr);
@@ -157,6 +167,7 @@ struct RefBasis {
     return false;
   }
   V3 normal(V3 r) const {  // cylinderXY.cuh:125-131, Sphere.cuh:142-149
+    if (plane()) return {b->nx, b->ny, b->nz};  // plane.cuh:32
     const double nx = r.x - b->cx, ny = r.y - b->cy;
     if (sph()) {
       const double nz = r.z - b->cz;
@@ -246,9 +257,9 @@ T fmaT(T a, T b, T c) {
 
 template <typename T>
 struct KInst {
-  T cx, cy, cz, negR2, invR, eps;
+  T cx, cy, cz, negR2, invR, eps;  // a plane: (cx, cy, cz) = unit normal, negR2 = n.c
   int slot;
-  bool sph;
+  bool sph, plane;
 };
 
 template <typename T>
@@ -273,13 +284,21 @@ T c0_of(const KInst<T> &g, T x, T y, T z) {
 template <typename T>
 int k_lookup(const KGeom<T> &G, T x, T y, T z) {
   for (const auto &g : G.inst)
-    if (c0_of(g, x, y, z) < T(0)) return g.slot;
+    if (!g.plane && c0_of(g, x, y, z) < T(0)) return g.slot;
   return G.ecs;
 }
 
 template <typename T>
 T k_seg_hit(const KInst<T> &g, bool on_surface, T sx, T sy, T sz, T dx, T dy, T dz, T aa, T rem) {
   const T inf = std::numeric_limits<T>::infinity();
+  if (g.plane) {  // (n.c - n.s) / n.d along the unit direction
+    if (on_surface) return inf;
+    const T np = fmaT(g.cx, sx, fmaT(g.cy, sy, g.cz * sz));
+    const T dn = fmaT(g.cx, dx, fmaT(g.cy, dy, g.cz * dz));
+    const T s = (g.negR2 - np) / dn;
+    if (!(s > T(0) && s < rem && s >= g.eps)) return inf;
+    return s;
+  }
   const T px = sx - g.cx, py = sy - g.cy;
   const T pz = g.sph ? (sz - g.cz) : T(0);
   T bh, c0, c1;
@@ -373,13 +392,15 @@ KMove<T> k_boundary(const KGeom<T> &G, T sx, T sy, T sz, T dx, T dy, T dz, T L, 
         return o;
       }
     }
-    const T nx = (hx - g.cx) * g.invR, ny = (hy - g.cy) * g.invR;
-    const T nz = g.sph ? (hz - g.cz) * g.invR : T(0);
-    const T dn = g.sph ? fmaT(dx, nx, fmaT(dy, ny, dz * nz)) : fmaT(dx, nx, dy * ny);
+    const bool n3 = g.sph || g.plane;
+    const T nx = g.plane ? g.cx : (hx - g.cx) * g.invR;
+    const T ny = g.plane ? g.cy : (hy - g.cy) * g.invR;
+    const T nz = g.plane ? g.cz : (g.sph ? (hz - g.cz) * g.invR : T(0));
+    const T dn = n3 ? fmaT(dx, nx, fmaT(dy, ny, dz * nz)) : fmaT(dx, nx, dy * ny);
     const T t = T(-2) * dn;
     dx = fmaT(t, nx, dx);
     dy = fmaT(t, ny, dy);
-    if (g.sph) dz = fmaT(t, nz, dz);
+    if (n3) dz = fmaT(t, nz, dz);
     sx = hx;
     sy = hy;
     sz = hz;
@@ -472,21 +493,39 @@ void k_build(const orc_lattice *lat, const orc_basis *basis, int nbasis, double 
     G.kappa4.push_back((T)(4.0 * kappa));
   };
   for (int k = 0; k < nbasis; ++k) {
-    slot(basis[k].D, basis[k].T2, basis[k].permeability);
+    if (basis[k].type == 2) slot(lat->D, lat->T2, 0.0);  // a plane transmits nothing
+    else slot(basis[k].D, basis[k].T2, basis[k].permeability);
     G.region.push_back(basis[k].region);
   }
   if (single) slot(basis[0].D, basis[0].T2, 0.0);
   else slot(lat->D, lat->T2, 0.0);
   G.region.push_back(0);
   G.ecs = nbasis;
+  auto unit = [](const orc_basis &b, double n[3]) {
+    const double m = std::sqrt(b.nx * b.nx + b.ny * b.ny + b.nz * b.nz);
+    n[0] = b.nx / m;
+    n[1] = b.ny / m;
+    n[2] = b.nz / m;
+  };
   auto add = [&](int k, double cx, double cy, double cz) {
     const orc_basis &b = basis[k];
     KInst<T> g;
-    g.cx = (T)cx;
-    g.cy = (T)cy;
-    g.cz = (T)cz;
-    g.negR2 = (T)(-(b.radius * b.radius));
-    g.invR = (T)(1.0 / b.radius);
+    g.plane = b.type == 2;
+    if (g.plane) {
+      double n[3];
+      unit(b, n);
+      g.cx = (T)n[0];
+      g.cy = (T)n[1];
+      g.cz = (T)n[2];
+      g.negR2 = (T)(n[0] * cx + n[1] * cy + n[2] * cz);
+      g.invR = T(1);
+    } else {
+      g.cx = (T)cx;
+      g.cy = (T)cy;
+      g.cz = (T)cz;
+      g.negR2 = (T)(-(b.radius * b.radius));
+      g.invR = (T)(1.0 / b.radius);
+    }
     g.eps = (T)b.eps;
     g.slot = k;
     g.sph = b.type == 1;
@@ -504,7 +543,7 @@ void k_build(const orc_lattice *lat, const orc_basis *basis, int nbasis, double 
   for (int k = 0; k < nbasis; ++k) {
     const orc_basis &b = basis[k];
     add(k, b.cx, b.cy, b.cz);
-    const int zr = b.type == 1 ? 1 : 0;
+    const int zr = b.type == 0 ? 0 : 1;
     for (int i = -1; i <= 1; ++i)
       for (int j = -1; j <= 1; ++j)
         for (int l = -zr; l <= zr; ++l) {
@@ -513,7 +552,19 @@ void k_build(const orc_lattice *lat, const orc_basis *basis, int nbasis, double 
           bool dup = false;
           for (int o = 0; o < nbasis && !dup; ++o) {
             const orc_basis &q = basis[o];
-            if (q.type != b.type || std::fabs(q.radius - b.radius) > tol) continue;
+            if (q.type != b.type) continue;
+            if (b.type == 2) {  // the same plane: parallel normals, the point on it
+              double n[3], m[3];
+              unit(q, n);
+              unit(b, m);
+              const double cr = std::fabs(n[1] * m[2] - n[2] * m[1]) +
+                                std::fabs(n[2] * m[0] - n[0] * m[2]) +
+                                std::fabs(n[0] * m[1] - n[1] * m[0]);
+              const double d = n[0] * (cx - q.cx) + n[1] * (cy - q.cy) + n[2] * (cz - q.cz);
+              dup = cr < 1e-12 && std::fabs(d) <= tol;
+              continue;
+            }
+            if (std::fabs(q.radius - b.radius) > tol) continue;
             if (std::fabs(q.cx - cx) > tol || std::fabs(q.cy - cy) > tol) continue;
             if (b.type == 1 && std::fabs(q.cz - cz) > tol) continue;
             dup = true;
@@ -1055,6 +1106,11 @@ int orc_walk(const orc_lattice *lat, const orc_basis *basis, int nbasis, const o
   if (nbasis < 0 || (nbasis > 0 && !basis) || (nseq > 0 && (!seqs || !sums))) return -1;
   if (!lat && nbasis < 1) return -1;
   if (mode < 0 || mode > 2) return -1;
+  // a plane is no pore and has no inside to start walkers in
+  if (!lat && basis[0].type == 2) return -1;
+  if (lat && p->init_mode == 2 && p->init_arg >= 0 && p->init_arg < nbasis &&
+      basis[p->init_arg].type == 2)
+    return -1;
   WalkIn in{lat, basis, nbasis, seqs, nseq, p, p->gamma > 0.0 ? p->gamma : kGAMMA,
             lat == nullptr, false, false, (p->flags & 4u) != 0};
   in.relax = !in.single && (p->flags & 1u);

@@ -34,8 +34,9 @@ extern "C" {
 #endif
 
 typedef struct {
-  int32_t type, region;
+  int32_t type, region;  /* type 0 cylinder along z, 1 sphere, 2 plane */
   double cx, cy, cz, radius, D, T2, T1, permeability, eps;
+  double nx, ny, nz;     /* plane normal */
 } orc_basis;
 
 typedef struct {

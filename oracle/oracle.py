@@ -27,7 +27,8 @@ class Basis(C.Structure):
     _fields_ = [("type", C.c_int32), ("region", C.c_int32), ("cx", C.c_double),
                 ("cy", C.c_double), ("cz", C.c_double), ("radius", C.c_double),
                 ("D", C.c_double), ("T2", C.c_double), ("T1", C.c_double),
-                ("permeability", C.c_double), ("eps", C.c_double)]
+                ("permeability", C.c_double), ("eps", C.c_double),
+                ("nx", C.c_double), ("ny", C.c_double), ("nz", C.c_double)]
 
 
 class Lattice(C.Structure):

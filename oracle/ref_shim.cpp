@@ -27,6 +27,7 @@
 #include <cstring>
 #include <iostream>
 #include <thread>
+#include <type_traits>
 #include <vector>
 
 #include <cuda_runtime_api.h>
@@ -84,6 +85,7 @@ using std::vector;
 #include "lattice.cuh"
 #include "cylinderXY.cuh"
 #include "Sphere.cuh"
+#include "plane.cuh"
 #include "boundaryCheck.cuh"
 #include "gfunctors.cuh"
 #include "kernelSetup.cuh"
@@ -173,8 +175,24 @@ int first_inside_single(const void *, const void *basisp, const Vector3 &r) {
   return basis[0].inside(r) ? 0 : -1;
 }
 
+// The reference's Plane (plane.cuh:1-40) has no inside(), which the
+// Lattice's region, D and T2 lookups call on every basis, so no lattice walk
+// over planes compiles as shipped.  A wall encloses nothing: inside() = false
+// completes the class consistently with its getRegion 0, getT2 -1 and
+// getD -1; everything else (intersect, getNormal, getPermeability) is the
+// reference's own code.
+struct PlaneBasis : Plane {
+  PlaneBasis() {}
+  explicit PlaneBasis(const Plane &p) : Plane(p) {}
+  bool inside(const Vector3 &) const { return false; }
+};
+
 template <class B>
 B make_basis(const orc_basis &q);
+template <>
+PlaneBasis make_basis<PlaneBasis>(const orc_basis &q) {
+  return PlaneBasis(Plane(Vector3(q.cx, q.cy, q.cz), Vector3(q.nx, q.ny, q.nz)));
+}
 template <>
 Cylinder_XY make_basis<Cylinder_XY>(const orc_basis &q) {
   Cylinder_XY c(q.cx, q.cy, q.radius, q.T2, q.T1, q.D, q.region, q.permeability, q.eps);
@@ -238,17 +256,27 @@ int run(const orc_lattice *latp, const orc_basis *bases, int nbasis, const orc_s
         hook.last_calls = calls0;
         curandState tmp = states[w];
         Vector3 r0;
-        if (single) r0 = basis[0].unifRand(tmp);
-        else lat.initializeUniformly(r0, tmp);
+        if constexpr (!std::is_same<B, PlaneBasis>::value) {
+          if (single) r0 = basis[0].unifRand(tmp);
+          else lat.initializeUniformly(r0, tmp);
+        } else {
+          lat.initializeUniformly(r0, tmp);
+        }
         tr->init_pos[w * 3 + 0] = r0.x;
         tr->init_pos[w * 3 + 1] = r0.y;
         tr->init_pos[w * 3 + 2] = r0.z;
       }
-      if (single)
-        updateWalkersPhase<AnyG, Counted<B>>(&par, basis.data(), G.data(), states.data(), phase.data());
-      else
+      if constexpr (!std::is_same<B, PlaneBasis>::value) {
+        if (single)
+          updateWalkersPhase<AnyG, Counted<B>>(&par, basis.data(), G.data(), states.data(),
+                                               phase.data());
+        else
+          updateWalkersLatticePhase<AnyG, Counted<B>>(&par, &lat, basis.data(), G.data(),
+                                                      states.data(), t2.data(), phase.data());
+      } else {
         updateWalkersLatticePhase<AnyG, Counted<B>>(&par, &lat, basis.data(), G.data(), states.data(),
                                                     t2.data(), phase.data());
+      }
       hook = Hook();
     }
   };
@@ -293,6 +321,11 @@ extern "C" int SHIM_CAT(ref_walk_, SHIM_NS)(const orc_lattice *lat, const orc_ba
   int type = nbasis > 0 ? basis[0].type : 0;
   for (int k = 0; k < nbasis; ++k)
     if (basis[k].type != type) return -3;  // one Basis type per lattice in the reference
+  if (type == 2) {
+    if (lat == nullptr) return -1;  // a plane is no pore
+    return SHIM_NS::run<SHIM_NS::PlaneBasis>(lat, basis, nbasis, seqs, nseq, p, nthreads, sums,
+                                             trace);
+  }
   if (type == 1)
     return SHIM_NS::run<SHIM_NS::Sphere>(lat, basis, nbasis, seqs, nseq, p, nthreads, sums, trace);
   return SHIM_NS::run<SHIM_NS::Cylinder_XY>(lat, basis, nbasis, seqs, nseq, p, nthreads, sums,

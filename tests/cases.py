@@ -41,6 +41,20 @@ def sphere_lattice(a_um=10.0, r_um=3.0):
                  for k, (x, y, z) in enumerate(pts)]
 
 
+def parallel_plates(l_um=8.0, D=D2, with_cylinder=False):
+    """Walls at x = 0 and x = l of an l-wide cubic cell, normals pointing
+    into the cell, as the reference's planePhase example sets them up
+    (Plane(Vector3(0,0,0), Vector3(1,0,0)), Plane(Vector3(l,0,0),
+    Vector3(-1,0,0))); optionally a cylinder along z between them."""
+    l = l_um * UM
+    lat = O.Lattice(l, l, l, 60.0, 0.0, D)
+    bases = [O.Basis(2, 0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 1e-14, 1.0, 0.0, 0.0),
+             O.Basis(2, 0, l, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 1e-14, -1.0, 0.0, 0.0)]
+    if with_cylinder:
+        bases.append(O.Basis(0, 1, l / 2, l / 2, 0.0, 0.3 * l, 1.2e-6, 80.0, 0.0, 3e-5, 1e-14))
+    return lat, bases
+
+
 def pgse(G_mTm, delta=10.0, Delta=40.0, g=(1.0, 0.0, 0.0)):
     return O.Sequence(0, 0, G_mTm * MTM, delta, Delta - delta, *g)
 

@@ -45,6 +45,11 @@ def golden_cases():
     out.append(("single_sph", "spec_imp", None, [b0], seqs, cases.params(96, 1500, 17)))
     b1 = O.Basis(0, 1, 0.001, -0.002, 0.0, 4 * cases.UM, cases.D2, 0, 0, 0, 1e-14)
     out.append(("single_cyl", "spec_imp", None, [b1], seqs, cases.params(96, 1500, 18)))
+    # Plane bases (plane.cuh): parallel plates as in the planePhase example
+    latq, plates = cases.parallel_plates()
+    out.append(("plates_imp_t2", "spec_imp_t2", latq, plates, seqs,
+                cases.params(96, 1500, 21, flags=1)))
+    out.append(("plates_perm", "spec_perm", latq, plates, seqs, cases.params(96, 1500, 22, flags=2)))
     # LATTICE_PICKING moves (kernelPhase.cuh:31-35)
     out.append(("single_cyl_pick", "pick_spec", None, [b1], seqs,
                 cases.params(96, 1500, 19, flags=32)))

@@ -32,6 +32,8 @@ def to_product(lat, bases, seqs=()):
         if b.type == 0:
             B.append(A.Cylinder_XY(b.cx, b.cy, b.radius, b.T2, b.T1, b.D, b.region,
                                    b.permeability, b.eps))
+        elif b.type == 2:
+            B.append(A.Plane((b.cx, b.cy, b.cz), (b.nx, b.ny, b.nz), b.eps))
         else:
             B.append(A.Sphere(b.cx, b.cy, b.cz, b.radius, b.T2, b.T1, b.D, b.region,
                               b.permeability, b.eps))
@@ -59,6 +61,10 @@ LATTICE_CASES = [
     ("hex_perm", lambda: cases.hex_cylinders(kappa=2e-5), 3, 0.001),
     ("spheres", lambda: cases.sphere_lattice(), 1, 0.002),
     ("gamma_perm", lambda: cases.gamma_packing(), 3, 0.001),
+    ("plates", lambda: cases.parallel_plates(), 1, 0.002),
+    ("plates_perm", lambda: cases.parallel_plates(l_um=5.0), 3, 0.002),
+    ("plates_reject", lambda: cases.parallel_plates(), 5, 0.002),
+    ("plates_cyl_perm", lambda: cases.parallel_plates(with_cylinder=True), 3, 0.002),
 ]
 
 
@@ -200,6 +206,8 @@ SIGNAL_CASES = [
     ("hex_perm_t2", lambda: cases.hex_cylinders(kappa=2e-5), 3, 0.001, 3000),
     ("spheres", lambda: cases.sphere_lattice(), 1, 0.002, 2000),
     ("free", lambda: (cases.lattice_box(50.0), []), 0, 0.005, 2000),
+    ("plates_t2", lambda: cases.parallel_plates(), 1, 0.002, 2500),
+    ("plates_cyl_perm", lambda: cases.parallel_plates(with_cylinder=True), 3, 0.002, 2500),
 ]
 
 

@@ -67,6 +67,25 @@ def test_oracle_matches_reference_live_packs(orc):
             np.testing.assert_array_equal(t_o[k], t_r[k], err_msg=k)
 
 
+@pytest.mark.parametrize("flags", [0, 1, 2, 3, 4, 5])
+def test_oracle_matches_reference_live_plates(orc, flags):
+    """Plane bases: the reference's Lattice walk over its own Plane class
+    (completed with inside() = false), every switch; with simple rejection
+    walkers cross the walls (a plane holds no region)."""
+    if not _ref_available(orc):
+        pytest.skip("reference walker not built here (no reference source tree)")
+    lat, plates = cases.parallel_plates(l_um=5.0)
+    seqs = [s for s in cases.seq_mix() if s.kind != 4]
+    p = cases.params(48, 1500, 40 + flags, flags=flags)
+    s_o, t_o, _ = orc.walk(lat, plates, seqs, p, orc.REF64, ntrace=48)
+    s_r, t_r = orc.ref_walk(orc.variant_for(flags), lat, plates, seqs, p, ntrace=48)
+    np.testing.assert_array_equal(s_o, s_r)
+    for k in ("init_pos", "pos", "region", "hits", "words"):
+        np.testing.assert_array_equal(t_o[k], t_r[k], err_msg=k)
+    if not flags & 4:
+        assert t_o["hits"].sum() > 0
+
+
 @pytest.mark.parametrize("sph", [0, 1])
 def test_oracle_matches_reference_live_lattice_picking(orc, sph):
     """LATTICE_PICKING single-pore walks, specular (trajectories and sums)
