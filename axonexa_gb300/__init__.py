@@ -4,8 +4,8 @@ The compute runs in hand-written sm_103a CUDA kernels behind the C ABI of
 include/axx.h (libaxx.so, built in-tree by ``axonexa_gb300.build``).  This
 package is the host-side mirror of the reference's acquisition API.
 """
-from .acquisition import (GAMMA, PI, ApodCosGFunc, CosGFunc, Cylinder_XY, Device, Lattice,
-                          Plane, RectGrad, RunResult, SinGFunc, Sphere, SWOGSEFunc, Vector3,
+from .acquisition import (GAMMA, PI, ApodCosGFunc, CosGFunc, Cylinder, Cylinder_XY, Device,
+                          Lattice, Plane, RectGrad, RunResult, SinGFunc, Sphere, SWOGSEFunc, Vector3,
                           default_device, linear_regression, phaseAcquisition,
                           phaseAcquisitionStream, philox_words, run_lattice, run_single,
                           trace_lattice, trace_single)

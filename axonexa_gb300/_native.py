@@ -17,7 +17,7 @@ STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "reflection cap hi
           4: "timeout", 5: "no CUDA device", 6: "out of device memory", 7: "aborted",
           8: "unsupported", 9: "non-finite value"}
 
-PRIM_CYLINDER_Z, PRIM_SPHERE, PRIM_PLANE = 0, 1, 2
+PRIM_CYLINDER_Z, PRIM_SPHERE, PRIM_PLANE, PRIM_CYLINDER = 0, 1, 2, 3
 SEQ_PGSE, SEQ_COS, SEQ_SIN, SEQ_APODCOS, SEQ_SQUARE = 0, 1, 2, 3, 4
 FLAG_RELAXATION, FLAG_PERMEABLE, FLAG_SIMPLE_REJECTION = 1, 2, 4
 FLAG_KEEP_INIT_QUIRK, FLAG_FIX_INIT_QUIRK = 8, 16

@@ -105,6 +105,53 @@ class Sphere:
                        self.radius, self.D, self.T2, self.T1, self.permeability, self.eps)
 
 
+class Cylinder:
+    """Infinite cylinder through ``center`` along ``axis`` (cylinder.cuh:1-199;
+    the reference's class is a draft that does not compile).  The library runs
+    it as a Cylinder_XY in the cylinder's frame (ahat, bhat, chat) built as
+    in cylinder.cuh:20-40, with gradient directions rotated into that frame:
+    any axis for a single pore; in a lattice the cylinders share one axis
+    along a cell axis (x, y or z)."""
+
+    def __init__(self, center, axis, radius, T2, T1, D, region, permeability, eps=1e-14):
+        self.center = tuple(float(v) for v in center)
+        self.axis = tuple(float(v) for v in axis)
+        self.radius, self.T2, self.T1, self.D = float(radius), float(T2), float(T1), float(D)
+        self.region, self.permeability, self.eps = int(region), float(permeability), float(eps)
+
+    def frame(self) -> np.ndarray:
+        """Rows ahat, bhat, chat: r_frame = frame() @ r (cylinder.cuh:20-40)."""
+        c = np.array(self.axis) / np.linalg.norm(self.axis)
+        a = np.array([c[1], -c[0], 0.0])  # chat x z
+        if np.hypot(a[0], a[1]) < 1e-14:
+            a, b = np.array([1.0, 0.0, 0.0]), np.array([0.0, 1.0, 0.0])
+        else:
+            a = a / np.hypot(a[0], a[1])
+            b = np.cross(c, a)
+            b = b / np.linalg.norm(b)
+        return np.vstack([a, b, c])
+
+    def inside(self, r) -> bool:
+        d = np.asarray(r, float) - np.array(self.center)
+        c = np.array(self.axis) / np.linalg.norm(self.axis)
+        p = d - np.dot(d, c) * c
+        return float(np.dot(p, p)) < self.radius ** 2
+
+    def getCenter(self):
+        return Vector3(*self.center)
+
+    def getRadius(self):
+        return self.radius
+
+    def getRegion(self):
+        return self.region
+
+    def record(self) -> N.Basis:
+        c, a = self.center, self.axis
+        return N.Basis(N.PRIM_CYLINDER, self.region, c[0], c[1], c[2], self.radius, self.D,
+                       self.T2, self.T1, self.permeability, self.eps, a[0], a[1], a[2])
+
+
 class Plane:
     """Infinite impermeable wall through ``center`` with normal ``normal``
     (plane.cuh:1-40).  It has no inside: it never holds a walker's region,
@@ -432,6 +479,14 @@ def wc_start(basis, n: int, seed: int):
     in the pore (the host side of runAcquisitionWC, seeded generator)."""
     rng = np.random.default_rng(int(seed) & 0xFFFFFFFFFFFFFFFF)
     state = rng.integers(1, 1 << 32, size=n, dtype=np.uint64).astype(np.uint32)
+    if isinstance(basis, Cylinder):
+        # the same draws for the cylinder in its own frame, rotated back
+        F = basis.frame()
+        cf = F @ np.array(basis.center)
+        xy = Cylinder_XY(cf[0], cf[1], basis.radius, basis.T2, basis.T1, basis.D,
+                         basis.region, basis.permeability, basis.eps)
+        st2, pf = wc_start(xy, n, seed)
+        return st2, pf @ F
     R = basis.radius if hasattr(basis, "radius") else basis.getRadius()
     sph = isinstance(basis, Sphere)
     c = np.array([basis.centerX, basis.centerY, basis.centerZ if sph else 0.0])

@@ -37,7 +37,7 @@ CUDA_SOURCES = [
     "calcf.cu",
     "wc.cu",
 ]
-HOST_SOURCES = ["api.cpp", "host_plan.cpp", "plan_layout.cpp", "substrate.cpp"]
+HOST_SOURCES = ["api.cpp", "frame.cpp", "host_plan.cpp", "plan_layout.cpp", "substrate.cpp"]
 
 
 def nvcc() -> str:

@@ -19,6 +19,7 @@
 
 #include "../../include/axx.h"
 #include "ctx_internal.h"
+#include "frame.h"
 #include "host_plan.h"
 #include "plan_layout.h"
 #include "walk_launch.h"
@@ -37,6 +38,10 @@ struct axx_plan {
   unsigned long long *counters = nullptr;
   long long walker_steps = 0;
   bool launched = false;
+  // the walk runs in the frame of arbitrary-axis cylinders: traces are
+  // rotated back with R^T
+  bool rotated = false;
+  double R[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
 };
 
 namespace {
@@ -128,6 +133,12 @@ axx_status build_plan(axx_ctx *ctx, const GeomPlan &g, const SeqPlan &sq, int M,
   return AXX_OK;
 }
 
+void keep_frame(axx_plan *pl, const Frame &fr) {
+  pl->rotated = !fr.identity;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) pl->R[i][j] = fr.R[i][j];
+}
+
 axx_status make_lattice_plan(axx_ctx *ctx, const axx_lattice *lat, const axx_basis *basis,
                              int nbasis, const axx_sequence *seqs, int nseq,
                              const axx_run_params *params, axx_plan **out) {
@@ -135,13 +146,18 @@ axx_status make_lattice_plan(axx_ctx *ctx, const axx_lattice *lat, const axx_bas
   if (s != AXX_OK) return s;
   const double gamma = params->gamma > 0.0 ? params->gamma : kGammaDefault;
   GeomPlan g;
-  std::string e = plan_lattice(lat, basis, nbasis, params->timestep, params->flags, g);
+  Frame fr;
+  std::string e = frame_lattice(lat, basis, nbasis, seqs, nseq, fr);
+  if (!e.empty()) return fail(ctx, AXX_ERR_INVALID_ARG, e);
+  e = plan_lattice(fr.lat_p, fr.basis_p, nbasis, params->timestep, params->flags, g);
   if (!e.empty()) return fail(ctx, AXX_ERR_INVALID_ARG, e);
   SeqPlan sq;
-  e = plan_sequences(seqs, nseq, params->steps, params->timestep, gamma, sq);
+  e = plan_sequences(fr.seqs_p, nseq, params->steps, params->timestep, gamma, sq);
   if (!e.empty()) return fail(ctx, AXX_ERR_INVALID_ARG, e);
-  const double cell[3] = {lat->a, lat->b, lat->c};
-  return build_plan(ctx, g, sq, nseq, params, AXX_MODE_LATTICE, basis, nbasis, cell, out);
+  const double cell[3] = {fr.lat_p->a, fr.lat_p->b, fr.lat_p->c};
+  s = build_plan(ctx, g, sq, nseq, params, AXX_MODE_LATTICE, fr.basis_p, nbasis, cell, out);
+  if (s == AXX_OK) keep_frame(*out, fr);
+  return s;
 }
 
 axx_status make_single_plan(axx_ctx *ctx, const axx_basis *basis, const axx_sequence *seqs,
@@ -154,13 +170,18 @@ axx_status make_single_plan(axx_ctx *ctx, const axx_basis *basis, const axx_sequ
   const double gamma = params->gamma > 0.0 ? params->gamma : kGammaDefault;
   GeomPlan g;
   float sp = 0.f, st = 0.f;
-  std::string e = plan_single(basis, params->timestep, g, sp, st);
+  Frame fr;
+  std::string e = frame_single(basis, seqs, nseq, fr);
+  if (!e.empty()) return fail(ctx, AXX_ERR_INVALID_ARG, e);
+  e = plan_single(fr.basis_p, params->timestep, g, sp, st);
   if (!e.empty()) return fail(ctx, AXX_ERR_INVALID_ARG, e);
   SeqPlan sq;
-  e = plan_sequences(seqs, nseq, params->steps, params->timestep, gamma, sq);
+  e = plan_sequences(fr.seqs_p, nseq, params->steps, params->timestep, gamma, sq);
   if (!e.empty()) return fail(ctx, AXX_ERR_INVALID_ARG, e);
   const double cell[3] = {1.0, 1.0, 1.0};
-  return build_plan(ctx, g, sq, nseq, params, AXX_MODE_SINGLE, basis, 1, cell, out);
+  s = build_plan(ctx, g, sq, nseq, params, AXX_MODE_SINGLE, fr.basis_p, 1, cell, out);
+  if (s == AXX_OK) keep_frame(*out, fr);
+  return s;
 }
 
 axx_status read_results(axx_plan *pl, double *mx, double *my, axx_stats *stats) {
@@ -455,6 +476,10 @@ static axx_status run_trace(axx_ctx *ctx, axx_plan *pl, int ntrace, float *init_
   if (e == cudaSuccess && words) e = cudaMemcpy(words, T.words, nrec * 4, cudaMemcpyDeviceToHost);
   cudaFree(buf);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "trace");
+  if (pl->rotated) {
+    if (init_pos) frame_to_sim(pl->R, init_pos, (size_t)ntrace);
+    if (pos) frame_to_sim(pl->R, pos, nrec);
+  }
   return AXX_OK;
 }
 

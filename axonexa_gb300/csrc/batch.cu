@@ -32,6 +32,7 @@
 
 #include "../../include/axx.h"
 #include "ctx_internal.h"
+#include "frame.h"
 #include "host_plan.h"
 #include "plan_layout.h"
 #include "walk_kernel.cuh"
@@ -425,6 +426,7 @@ static axx_status batch_build(axx_ctx *ctx, const axx_job *jobs, int njobs,
     axx_run_params p;
     int mode;
     double cell[3];
+    Frame f;  // arbitrary-axis cylinders: the job in the cylinders' frame
   };
   std::vector<JobPlan> jp(njobs);
   int kmax = 1;
@@ -448,15 +450,19 @@ static axx_status batch_build(axx_ctx *ctx, const axx_job *jobs, int njobs,
       if (p.flags & (AXX_FLAG_PERMEABLE | AXX_FLAG_RELAXATION))
         return bfail(ctx, AXX_ERR_INVALID_ARG, "single-pore jobs have no permeability or relaxation");
       float sp, st;
-      err = plan_single(J.basis, p.timestep, q.g, sp, st);
+      err = frame_single(J.basis, J.seqs, J.nseq, q.f);
+      if (err.empty()) err = plan_single(q.f.basis_p, p.timestep, q.g, sp, st);
       q.cell[0] = q.cell[1] = q.cell[2] = 1.0;
     } else {
-      err = plan_lattice(&J.lattice, J.basis, J.nbasis, p.timestep, p.flags, q.g);
-      q.cell[0] = J.lattice.a;
-      q.cell[1] = J.lattice.b;
-      q.cell[2] = J.lattice.c;
+      err = frame_lattice(&J.lattice, J.basis, J.nbasis, J.seqs, J.nseq, q.f);
+      if (err.empty()) err = plan_lattice(q.f.lat_p, q.f.basis_p, J.nbasis, p.timestep, p.flags, q.g);
+      if (err.empty()) {
+        q.cell[0] = q.f.lat_p->a;
+        q.cell[1] = q.f.lat_p->b;
+        q.cell[2] = q.f.lat_p->c;
+      }
     }
-    if (err.empty()) err = plan_sequences(J.seqs, J.nseq, p.steps, p.timestep, gamma, q.sq);
+    if (err.empty()) err = plan_sequences(q.f.seqs_p, J.nseq, p.steps, p.timestep, gamma, q.sq);
     if (!err.empty()) return bfail(ctx, AXX_ERR_INVALID_ARG, "job " + std::to_string(j) + ": " + err);
     int k = 1;
     while (k < (int)q.sq.channels.size()) k <<= 1;
@@ -470,7 +476,7 @@ static axx_status batch_build(axx_ctx *ctx, const axx_job *jobs, int njobs,
     JobPlan &q = jp[j];
     std::string err = make_kernel_tables(q.g, q.sq, jobs[j].nseq, q.p.steps, q.mode, q.p.flags,
                                          q.kt, kmax);
-    if (err.empty()) err = init_spec(q.g, jobs[j].basis, jobs[j].nbasis, q.mode, &q.p, q.init);
+    if (err.empty()) err = init_spec(q.g, q.f.basis_p, jobs[j].nbasis, q.mode, &q.p, q.init);
     if (!err.empty()) return bfail(ctx, AXX_ERR_INVALID_ARG, "job " + std::to_string(j) + ": " + err);
     geo_max = std::max(geo_max, walk_smem_bytes(q.g, 0));
     job_off[j] = off;

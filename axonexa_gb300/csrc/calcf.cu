@@ -17,6 +17,7 @@
 
 #include "../../include/axx.h"
 #include "ctx_internal.h"
+#include "frame.h"
 #include "host_plan.h"
 #include "plan_layout.h"
 #include "walk_kernel.cuh"
@@ -85,7 +86,12 @@ extern "C" axx_status axx_volume_fraction(axx_ctx *ctx, const axx_lattice *lat,
   // a vanishing time step: the instance set and cell lists of the walk at
   // (almost) zero step length -- bases and the ghosts that meet the cell
   GeomPlan g;
-  std::string err = plan_lattice(lat, basis, nbasis, 1e-12, 0u, g);
+  Frame fr;  // lattices of x- or y-axis cylinders run with permuted axes
+  std::string err = frame_lattice(lat, basis, nbasis, nullptr, 0, fr);
+  if (!err.empty()) return fail(AXX_ERR_INVALID_ARG, err);
+  lat = fr.lat_p;
+  basis = fr.basis_p;
+  err = plan_lattice(lat, basis, nbasis, 1e-12, 0u, g);
   if (!err.empty()) return fail(AXX_ERR_INVALID_ARG, err);
   axx_run_params rp{points, 1, 0, 0, 0u, seed, 1e-12, kGammaDefault, 0};
   KernelTables kt;

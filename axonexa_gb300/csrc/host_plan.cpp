@@ -204,6 +204,8 @@ static std::string check_basis(const axx_basis &b) {
     if (!(b.nx * b.nx + b.ny * b.ny + b.nz * b.nz > 1e-24)) return "plane normal must be nonzero";
     return "";
   }
+  if (b.type == AXX_PRIM_CYLINDER)
+    return "arbitrary-axis cylinders are not supported by this entry point";
   if (b.type != AXX_PRIM_CYLINDER_Z && b.type != AXX_PRIM_SPHERE) return "unknown basis type";
   if (!(b.radius > 0.0) || !finite(b.radius)) return "basis radius must be > 0";
   if (!(b.D >= 0.0) || !finite(b.D)) return "basis D must be >= 0";

@@ -31,6 +31,7 @@
 
 #include "../../include/axx.h"
 #include "ctx_internal.h"
+#include "frame.h"
 #include "host_plan.h"
 #include "plan_layout.h"
 #include "walk_launch.h"
@@ -92,7 +93,13 @@ extern "C" axx_status axx_run_lattice_noalloc(axx_ctx *ctx, const axx_lattice *l
 
   const double gamma = p->gamma > 0.0 ? p->gamma : kGammaDefault;
   GeomPlan g;
-  std::string err = plan_lattice(lat, basis, nbasis, p->timestep, p->flags, g);
+  Frame fr;
+  std::string err = frame_lattice(lat, basis, nbasis, seqs, nseq, fr);
+  if (!err.empty()) return fail(ctx, AXX_ERR_INVALID_ARG, err);
+  lat = fr.lat_p;
+  basis = fr.basis_p;
+  seqs = fr.seqs_p;
+  err = plan_lattice(lat, basis, nbasis, p->timestep, p->flags, g);
   if (!err.empty()) return fail(ctx, AXX_ERR_INVALID_ARG, err);
   SeqPlan sq;
   err = plan_sequences(seqs, nseq, p->steps, p->timestep, gamma, sq);

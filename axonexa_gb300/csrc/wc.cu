@@ -25,6 +25,7 @@
 #include "../../include/axx.h"
 #include "axx_rng.cuh"
 #include "ctx_internal.h"
+#include "frame.h"
 #include "walk_launch.h"
 
 namespace axx {
@@ -121,15 +122,25 @@ extern "C" axx_status axx_run_wc(axx_ctx *ctx, const axx_basis *pore, int64_t nu
   if (!pore || !rng_state || !start || !grad || num_walkers < 1 || steps < 0 ||
       !(timestep > 0.0) || !std::isfinite(gamma) || !(pore->radius > 0.0) || !(pore->D > 0.0))
     return fail(AXX_ERR_INVALID_ARG, "pore, walkers, steps, timestep or arrays out of range");
-  if (pore->type != AXX_PRIM_CYLINDER_Z && pore->type != AXX_PRIM_SPHERE)
+  if (pore->type != AXX_PRIM_CYLINDER_Z && pore->type != AXX_PRIM_SPHERE &&
+      pore->type != AXX_PRIM_CYLINDER)
     return fail(AXX_ERR_INVALID_ARG, "unknown pore type");
+  // an arbitrary-axis cylinder: positions and gradients in its frame
+  Frame fr;
+  std::string ferr = frame_single(pore, nullptr, 0, fr);
+  if (!ferr.empty()) return fail(AXX_ERR_INVALID_ARG, ferr);
+  pore = fr.basis_p;
+  auto to_frame = [&](const double *v) {
+    const double x = v[0], y = v[1], z = v[2];
+    return make_float4((float)(fr.R[0][0] * x + fr.R[0][1] * y + fr.R[0][2] * z),
+                       (float)(fr.R[1][0] * x + fr.R[1][1] * y + fr.R[1][2] * z),
+                       (float)(fr.R[2][0] * x + fr.R[2][1] * y + fr.R[2][2] * z), 0.f);
+  };
   const double g = gamma != 0.0 ? gamma : 267500.0;
   const long long n = num_walkers;
   std::vector<float4> h_start((size_t)n), h_grad((size_t)std::max(steps, 1));
-  for (long long i = 0; i < n; ++i)
-    h_start[i] = make_float4((float)start[3 * i], (float)start[3 * i + 1], (float)start[3 * i + 2], 0.f);
-  for (int t = 0; t < steps; ++t)
-    h_grad[t] = make_float4((float)grad[3 * t], (float)grad[3 * t + 1], (float)grad[3 * t + 2], 0.f);
+  for (long long i = 0; i < n; ++i) h_start[i] = to_frame(start + 3 * i);
+  for (int t = 0; t < steps; ++t) h_grad[t] = to_frame(grad + 3 * t);
   const int grid = (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, (long long)ctx->nsm * 8));
   auto up = [](size_t x) { return (x + 255) & ~(size_t)255; };
   const size_t o_st = 0, o_p0 = up(o_st + (size_t)n * 4), o_g = up(o_p0 + (size_t)n * 16),

@@ -81,10 +81,16 @@ typedef struct axx_plan axx_plan;
 
 enum { AXX_PRIM_CYLINDER_Z = 0, /* Cylinder_XY: infinite cylinder, axis along z */
        AXX_PRIM_SPHERE = 1,     /* Sphere */
-       AXX_PRIM_PLANE = 2 };    /* Plane: infinite impermeable wall (lattices only) */
+       AXX_PRIM_PLANE = 2,      /* Plane: infinite impermeable wall (lattices only) */
+       AXX_PRIM_CYLINDER = 3 }; /* Cylinder: infinite cylinder along (nx, ny, nz) */
 
 /* One basis object (src/primitives/cylinderXY.cuh:1-40, Sphere.cuh:4-44,
- * plane.cuh:1-40).  A plane is the wall through (cx, cy, cz) with normal
+ * plane.cuh:1-40, cylinder.cuh:1-199).  An AXX_PRIM_CYLINDER runs through
+ * (cx, cy, cz) along the axis (nx, ny, nz): any axis for a single pore (the
+ * walk runs in the cylinder's frame (ahat, bhat, chat) of cylinder.cuh:20-40
+ * and traces come back in simulation coordinates); in a lattice all such
+ * cylinders share one axis along a cell axis (x, y or z), and z-cylinders
+ * (AXX_PRIM_CYLINDER_Z) may join them only when that axis is z.  A plane is the wall through (cx, cy, cz) with normal
  * (nx, ny, nz) (normalised by the library; Plane::getNormal returns it as
  * given and the reflection assumes unit length).  It has no inside: it never
  * contains a point (no region, D or T2 of its own), reflects every crossing
@@ -101,7 +107,7 @@ typedef struct {
   double permeability;   /* kappa; transmission probability is 4*kappa/v */
   double eps;            /* minimum hit distance (cylEPS / sphereEPS; doub_equal's
                             1e-14 for a plane) */
-  double nx, ny, nz;     /* plane normal; ignored for cylinders and spheres */
+  double nx, ny, nz;     /* plane normal, or AXX_PRIM_CYLINDER axis; ignored otherwise */
 } axx_basis;
 
 /* Periodic cell (src/substrate/lattice.cuh:3-23): a x b x c box with the
