@@ -88,7 +88,13 @@ AXX_HD int float_bits(float f) {
 
 AXX_HD float word_to_uniform(uint32_t x) {
   // (k + 1/2) * 2^-23 with k = x >> 9: exact in FP32.
+#if defined(__CUDA_ARCH__)
+  // without an int-to-float conversion: the bits of 1 + k 2^-23 minus
+  // (1 - 2^-24), exact by Sterbenz's lemma (both operands lie in [1/2, 2])
+  return __uint_as_float((x >> 9) | 0x3F800000u) - 0.999999940395355224609375f;
+#else
   return (float)(x >> 9) * 1.1920928955078125e-07f + 5.9604644775390625e-08f;
+#endif
 }
 
 // Sequential per-walker stream over Philox blocks.

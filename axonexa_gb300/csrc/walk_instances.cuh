@@ -47,7 +47,7 @@ static cudaError_t walk_launch_km(int kmax, bool trace, bool one, const WalkPara
                                   const TraceParams &T, int grid, size_t smem, cudaStream_t s) {
   constexpr bool single = KM >= AXX_KM_SINGLE;
   constexpr bool lat1 = !single && (GEOM == AXX_GEOM_CYL || GEOM == AXX_GEOM_SPH);
-  if (single) {
+  if constexpr (single) {
     if (trace) return walk_go<GEOM, 1, KM, true, single>(P, T, grid, smem, s);
     switch (kmax) {
       case 1: return walk_go<GEOM, 1, KM, false, single>(P, T, grid, smem, s);
@@ -57,7 +57,7 @@ static cudaError_t walk_launch_km(int kmax, bool trace, bool one, const WalkPara
       case 16: return walk_go<GEOM, 16, KM, false, single>(P, T, grid, smem, s);
     }
     return cudaErrorInvalidValue;
-  }
+  } else {
   if (lat1 && walk_one_variant<GEOM, KM>(kmax, trace, one)) {
     switch (kmax) {
       case 1: return walk_go<GEOM, 1, KM, false, lat1>(P, T, grid, smem, s);
@@ -74,13 +74,14 @@ static cudaError_t walk_launch_km(int kmax, bool trace, bool one, const WalkPara
     case 16: return walk_go<GEOM, 16, KM, false>(P, T, grid, smem, s);
   }
   return cudaErrorInvalidValue;
+  }
 }
 
 template <int GEOM, int KM>
 static int walk_occ_km(int kmax, bool trace, bool one, size_t smem) {
   constexpr bool single = KM >= AXX_KM_SINGLE;
   constexpr bool lat1 = !single && (GEOM == AXX_GEOM_CYL || GEOM == AXX_GEOM_SPH);
-  if (single) {
+  if constexpr (single) {
     if (trace) return walk_occ<GEOM, 1, KM, true, single>(smem);
     switch (kmax) {
       case 1: return walk_occ<GEOM, 1, KM, false, single>(smem);
@@ -90,7 +91,7 @@ static int walk_occ_km(int kmax, bool trace, bool one, size_t smem) {
       case 16: return walk_occ<GEOM, 16, KM, false, single>(smem);
     }
     return 0;
-  }
+  } else {
   if (lat1 && walk_one_variant<GEOM, KM>(kmax, trace, one)) {
     switch (kmax) {
       case 1: return walk_occ<GEOM, 1, KM, false, lat1>(smem);
@@ -107,6 +108,7 @@ static int walk_occ_km(int kmax, bool trace, bool one, size_t smem) {
     case 16: return walk_occ<GEOM, 16, KM, false>(smem);
   }
   return 0;
+  }
 }
 
 }  // namespace axx

@@ -151,14 +151,14 @@ __device__ __forceinline__ float plane_hit(const float4 &g, float eps, bool on_s
   return s;
 }
 
-// Distance to the first boundary of one instance along the segment
-// start + s*d, 0 < s < rem, or +inf.
-__device__ __forceinline__ float seg_hit(const float4 &g, float eps, bool sph, bool on_surface,
-                                         float sx, float sy, float sz, float dx, float dy,
-                                         float dz, float aa, float rem) {
+// The quadratic of one instance along the segment start + s*d, s in
+// [0, rem]: half the linear coefficient bh = p.d and |p|^2 - R^2 at both
+// ends (c0 at the start, c1 at s = rem), p = start - centre.
+__device__ __forceinline__ void seg_coef(const float4 &g, bool sph, float sx, float sy, float sz,
+                                         float dx, float dy, float dz, float rem, float &bh,
+                                         float &c0, float &c1) {
   const float px = sx - g.x, py = sy - g.y;
   const float pz = sph ? (sz - g.z) : 0.0f;
-  float bh, c0, c1;
   const float ex = fma_f(rem, dx, px), ey = fma_f(rem, dy, py);
   if (sph) {
     const float ez = fma_f(rem, dz, pz);
@@ -170,7 +170,20 @@ __device__ __forceinline__ float seg_hit(const float4 &g, float eps, bool sph, b
     c0 = fma_f(px, px, fma_f(py, py, g.w));
     c1 = fma_f(ex, ex, fma_f(ey, ey, g.w));
   }
-  if (on_surface) c0 = 0.0f;
+}
+
+// The segment can meet the instance (the rejections the hit test applies
+// first fail), given its quadratic.
+__device__ __forceinline__ bool seg_may(float bh, float c0, float c1, float aa, float rem) {
+  return !((c0 < 0.0f && c1 < 0.0f) ||
+           (c0 >= 0.0f && (bh >= 0.0f || (c0 > 0.0f && c1 > 0.0f && fma_f(aa, rem, bh) <= 0.0f))));
+}
+
+// Distance to the first boundary of one instance along the segment
+// start + s*d, 0 < s < rem, or +inf, given its quadratic (c0 = 0 for a start
+// on the instance's surface).
+__device__ __forceinline__ float seg_root(float bh, float c0, float c1, float eps, float aa,
+                                          float rem) {
   // cheap rejections: both ends inside; outside or on the surface and moving
   // away; outside with the closest approach beyond the end
   if (c0 < 0.0f && c1 < 0.0f) return AXX_INF;
@@ -187,6 +200,29 @@ __device__ __forceinline__ float seg_hit(const float4 &g, float eps, bool sph, b
   } else {  // on the surface: the far root
     s = div_f(-2.0f * bh, aa);
   }
+  if (!(s > 0.0f && s < rem && s >= eps)) return AXX_INF;
+  return s;
+}
+
+__device__ __forceinline__ float seg_hit(const float4 &g, float eps, bool sph, bool on_surface,
+                                         float sx, float sy, float sz, float dx, float dy,
+                                         float dz, float aa, float rem) {
+  float bh, c0, c1;
+  seg_coef(g, sph, sx, sy, sz, dx, dy, dz, rem, bh, c0, c1);
+  if (on_surface) c0 = 0.0f;
+  return seg_root(bh, c0, c1, eps, aa, rem);
+}
+
+// seg_hit for a start on the instance's surface (c0 = 0), which needs only
+// bh: moving away (bh >= 0) misses, else the far root -2 bh / aa.
+__device__ __forceinline__ float surface_hit(const float4 &g, float eps, bool sph, float sx,
+                                             float sy, float sz, float dx, float dy, float dz,
+                                             float aa, float rem) {
+  const float px = sx - g.x, py = sy - g.y;
+  const float pz = sph ? (sz - g.z) : 0.0f;
+  const float bh = sph ? fma_f(px, dx, fma_f(py, dy, pz * dz)) : fma_f(px, dx, py * dy);
+  if (bh >= 0.0f) return AXX_INF;
+  const float s = div_f(-2.0f * bh, aa);
   if (!(s > 0.0f && s < rem && s >= eps)) return AXX_INF;
   return s;
 }
@@ -279,7 +315,9 @@ struct Walker {
   float ux, uy, uz;  // unbounded position
   int slot;          // slot of the region at (x, y, z)
   float acc[KMAX], cmp[KMAX];
+  float part[KMAX];  // phase of the current block of moves (DEFER)
   float t2s, t2c;
+  int nin;  // ONE: moves weighted by the instance's region (T2 by counts)
 };
 
 // The instances and the list a move may test: either the cell list of the
@@ -309,6 +347,9 @@ __device__ __forceinline__ MoveOut boundary(const WalkParams &P, const Cands<GEO
                                             float dz, float L, float v, DevStream &st,
                                             float Lb) {
   bool maybe = false;
+  // ONE: the quadratic of the first pass (no instance hit yet, segment L),
+  // reused by the nearest-hit loop's first pass
+  float bh1 = 0.0f, c01 = 0.0f, c11 = 0.0f;
   {
     const float aa_c = fma_f(dx, dx, dy * dy);
     const float aa_s = fma_f(dx, dx, fma_f(dy, dy, dz * dz));
@@ -317,30 +358,20 @@ __device__ __forceinline__ MoveOut boundary(const WalkParams &P, const Cands<GEO
       if (is_plane<GEOM>(aux))
         return plane_hit(g, aux.y, false, sx, sy, sz, dx, dy, dz, L) < AXX_INF;
       const bool sph = is_sphere<GEOM>(aux);
-      const float px = sx - g.x, py = sy - g.y;
-      const float pz = sph ? (sz - g.z) : 0.0f;
-      const float ex = fma_f(L, dx, px), ey = fma_f(L, dy, py);
       float bh, c0, c1;
-      if (sph) {
-        const float ez = fma_f(L, dz, pz);
-        bh = fma_f(px, dx, fma_f(py, dy, pz * dz));
-        c0 = fma_f(px, px, fma_f(py, py, fma_f(pz, pz, g.w)));
-        c1 = fma_f(ex, ex, fma_f(ey, ey, fma_f(ez, ez, g.w)));
-      } else {
-        bh = fma_f(px, dx, py * dy);
-        c0 = fma_f(px, px, fma_f(py, py, g.w));
-        c1 = fma_f(ex, ex, fma_f(ey, ey, g.w));
-      }
-      const float aa = sph ? aa_s : aa_c;
-      // the same rejections seg_hit applies first (c0 is exact here: no
+      seg_coef(g, sph, sx, sy, sz, dx, dy, dz, L, bh, c0, c1);
+      // the same rejections seg_root applies first (c0 is exact here: no
       // instance has been hit yet in this move)
-      const bool no = (c0 < 0.0f && c1 < 0.0f) ||
-                      (c0 >= 0.0f && (bh >= 0.0f || (c0 > 0.0f && c1 > 0.0f &&
-                                                     fma_f(aa, L, bh) <= 0.0f)));
-      return !no;
+      return seg_may(bh, c0, c1, sph ? aa_s : aa_c, L);
     };
     if (ONE) {
-      maybe = may(C.g0, C.a0);
+      if (is_plane<GEOM>(C.a0)) {
+        maybe = may(C.g0, C.a0);
+      } else {
+        const bool sph = is_sphere<GEOM>(C.a0);
+        seg_coef(C.g0, sph, sx, sy, sz, dx, dy, dz, L, bh1, c01, c11);
+        maybe = seg_may(bh1, c01, c11, sph ? aa_s : aa_c, L);
+      }
     } else {
       for (uint32_t j = C.b; j < C.e; ++j) {
         const int k = C.S.clist[j];
@@ -366,11 +397,16 @@ __device__ __forceinline__ MoveOut boundary(const WalkParams &P, const Cands<GEO
     int bk = -1;
     float4 bg, ba;
     if (ONE) {
+      // the only instance: the first pass reuses the pre-filter's quadratic;
+      // after a hit the start is on its surface
       const bool sph = is_sphere<GEOM>(C.a0);
-      best = is_plane<GEOM>(C.a0)
-                 ? plane_hit(C.g0, C.a0.y, last == 0, sx, sy, sz, dx, dy, dz, rem)
-                 : seg_hit(C.g0, C.a0.y, sph, last == 0, sx, sy, sz, dx, dy, dz,
-                           sph ? aa_s : aa_c, rem);
+      const float aa = sph ? aa_s : aa_c;
+      if (is_plane<GEOM>(C.a0))
+        best = plane_hit(C.g0, C.a0.y, last == 0, sx, sy, sz, dx, dy, dz, rem);
+      else if (last < 0)
+        best = seg_root(bh1, c01, c11, C.a0.y, aa, rem);
+      else
+        best = surface_hit(C.g0, C.a0.y, sph, sx, sy, sz, dx, dy, dz, aa, rem);
       if (best < AXX_INF) bk = 0;
       bg = C.g0;
       ba = C.a0;
@@ -462,7 +498,10 @@ __device__ __forceinline__ float wrap_sel(float x, float a) {
 // PICK (single pore, LATTICE_PICKING, kernelPhase.cuh:31-35): the move is
 // +-L along every axis, the signs in bits 0..2 of `signs` (x, y, z): a
 // sqrt(3) L segment along a cube diagonal with path budget L.
-template <int GEOM, int KMAX, int KM, bool TRACE, bool ONE, bool PICK = false>
+// DEFER: the move's phase terms go to W.part (FP32 sums over a block of
+// moves, folded into the compensated sums by the caller) instead of the
+// compensated sums directly.
+template <int GEOM, int KMAX, int KM, bool TRACE, bool ONE, bool PICK = false, bool DEFER = false>
 __device__ __forceinline__ void do_move(const WalkParams &P, const SmemView &S,
                                         const TraceParams &T, long long wid, int i, float u1,
                                         float u2, DevStream &st, Walker<KMAX> &W,
@@ -555,7 +594,10 @@ __device__ __forceinline__ void do_move(const WalkParams &P, const SmemView &S,
 #pragma unroll
   for (int c = 0; c < KMAX; ++c) {
     const float d = fma_f(P.ch_p[c][2], pz, fma_f(P.ch_p[c][1], py, P.ch_p[c][0] * px));
-    kahan_add(W.acc[c], W.cmp[c], wv[c] * d);
+    if (DEFER)
+      W.part[c] = fma_f(wv[c], d, W.part[c]);
+    else
+      kahan_add(W.acc[c], W.cmp[c], wv[c] * d);
   }
   if (!single) {
     int new_slot = P.ecs_slot;
@@ -569,8 +611,13 @@ __device__ __forceinline__ void do_move(const WalkParams &P, const SmemView &S,
       }
     }
     // dt/T2 of the move's region (0 without relaxation); the permeable walk
-    // weights the region after the move (accumtime is always 0)
-    kahan_add(W.t2s, W.t2c, perm ? S.slot[new_slot].z : s4.z);
+    // weights the region after the move (accumtime is always 0).  With one
+    // instance there are two regions: count the moves in the instance's and
+    // form the sum at the end.
+    if (ONE)
+      W.nin += ((perm ? new_slot : W.slot) != P.ecs_slot) ? 1 : 0;
+    else
+      kahan_add(W.t2s, W.t2c, perm ? S.slot[new_slot].z : s4.z);
     W.slot = new_slot;
   }
   W.x = fx;
@@ -627,6 +674,7 @@ __device__ __forceinline__ WalkResult walk_one(const WalkParams &P, const SmemVi
   }
   W.t2s = 0.0f;
   W.t2c = 0.0f;
+  W.nin = 0;
   W.slot = single ? 0 : P.ecs_slot;
   if (!single && GEOM != AXX_GEOM_FREE) {
     if (ONE) {
@@ -657,8 +705,12 @@ __device__ __forceinline__ WalkResult walk_one(const WalkParams &P, const SmemVi
   }
   // Two moves per Philox block when every walker of the warp has its stream
   // at a block boundary and moves draw nothing else (the lattice walk from a
-  // uniform start); otherwise the general stream.
-  if (!perm && __all_sync(__activemask(), st.pos == 4)) {
+  // uniform start); otherwise the general stream.  With up to 4 channels the
+  // phase terms of up to 32 moves are summed in FP32 and then added to the
+  // compensated sums (more channels keep per-move compensation: the block
+  // sums would cost registers the list walk needs).
+  constexpr bool defer = KMAX <= 4;
+  if (!defer && !perm && __all_sync(__activemask(), st.pos == 4)) {
     for (; i + 1 < P.steps; i += 2) {
       if (((i + 1) & 1023) == 0 && P.abort_flag != nullptr && *P.abort_flag) {
         res.aborted = true;
@@ -675,6 +727,29 @@ __device__ __forceinline__ WalkResult walk_one(const WalkParams &P, const SmemVi
                                            word_to_uniform(w3), st, W, res, g0, a0);
     }
   }
+  if (defer && !perm && __all_sync(__activemask(), st.pos == 4)) {
+    while (i + 1 < P.steps) {
+      if (((i - 1) & 1023) == 0 && P.abort_flag != nullptr && *P.abort_flag) {
+        res.aborted = true;
+        return res;
+      }
+#pragma unroll
+      for (int c = 0; c < KMAX; ++c) W.part[c] = 0.0f;
+      for (int q = 0; q < 16 && i + 1 < P.steps; ++q, i += 2) {
+        ++st.blk;
+        st.load(P);
+        const uint32_t w0 = st.b0, w1 = st.b1, w2 = st.b2, w3 = st.b3;
+        st.pos = 2;
+        do_move<GEOM, KMAX, KM, TRACE, ONE, false, defer>(
+            P, S, T, wid, i, word_to_uniform(w0), word_to_uniform(w1), st, W, res, g0, a0);
+        st.pos = 4;
+        do_move<GEOM, KMAX, KM, TRACE, ONE, false, defer>(
+            P, S, T, wid, i + 1, word_to_uniform(w2), word_to_uniform(w3), st, W, res, g0, a0);
+      }
+#pragma unroll
+      for (int c = 0; c < KMAX; ++c) kahan_add(W.acc[c], W.cmp[c], W.part[c]);
+    }
+  }
   for (; i < P.steps; ++i) {
     if ((i & 1023) == 0 && P.abort_flag != nullptr && *P.abort_flag) {
       res.aborted = true;
@@ -683,6 +758,12 @@ __device__ __forceinline__ WalkResult walk_one(const WalkParams &P, const SmemVi
     float u1, u2;
     st.next2(P, u1, u2);
     do_move<GEOM, KMAX, KM, TRACE, ONE>(P, S, T, wid, i, u1, u2, st, W, res, g0, a0);
+  }
+  if (ONE && !single) {  // the T2 sum from the move counts of the two regions
+    const float tin = S.slot[aux_slot(a0)].z, tout = S.slot[P.ecs_slot].z;
+    const double t = (double)W.nin * (double)tin + (double)(i - 1 - W.nin) * (double)tout;
+    W.t2s = (float)t;
+    W.t2c = (float)((double)W.t2s - t);
   }
   return res;
 }
@@ -699,7 +780,8 @@ __device__ __forceinline__ double warp_sum(double v) {
 // n_inst == 1 and ncell == 1); the list path is left out, which frees
 // registers for one more resident block per SM.
 template <int GEOM, int KMAX, int KM, bool TRACE, bool ONEONLY = false>
-__global__ void __launch_bounds__(AXX_BLOCK, AXX_MIN_BLOCKS_FOR(KMAX))
+__global__ void __launch_bounds__(AXX_BLOCK, ONEONLY && KMAX <= 4 ? AXX_MIN_BLOCKS + 1
+                                                                 : AXX_MIN_BLOCKS_FOR(KMAX))
     walk_kernel(const __grid_constant__ WalkParams P, const __grid_constant__ TraceParams T) {
   extern __shared__ __align__(16) unsigned char smem[];
   constexpr int warps = AXX_BLOCK / 32;
@@ -752,6 +834,8 @@ __global__ void __launch_bounds__(AXX_BLOCK, AXX_MIN_BLOCKS_FOR(KMAX))
       WalkResult r;
       if constexpr (ONEONLY)
         r = walk_one<GEOM, KMAX, KM, TRACE, true>(P, S, T, wid, W);
+      else if constexpr (KMAX > 4)  // (the list path serves one instance too)
+        r = walk_one<GEOM, KMAX, KM, TRACE, false>(P, S, T, wid, W);
       else
         r = one ? walk_one<GEOM, KMAX, KM, TRACE, true>(P, S, T, wid, W)
                 : walk_one<GEOM, KMAX, KM, TRACE, false>(P, S, T, wid, W);
