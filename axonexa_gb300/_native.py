@@ -22,6 +22,7 @@ SEQ_PGSE, SEQ_COS, SEQ_SIN, SEQ_APODCOS, SEQ_SQUARE = 0, 1, 2, 3, 4
 FLAG_RELAXATION, FLAG_PERMEABLE, FLAG_SIMPLE_REJECTION = 1, 2, 4
 FLAG_KEEP_INIT_QUIRK, FLAG_FIX_INIT_QUIRK = 8, 16
 FLAG_LATTICE_PICKING = 32
+FLAG_COMPARTMENTS = 64
 INIT_UNIFORM, INIT_IN_REGION, INIT_IN_BASIS = 0, 1, 2
 
 
@@ -63,7 +64,9 @@ class RunParams(C.Structure):
 class Stats(C.Structure):
     _fields_ = [("sxx", C.POINTER(C.c_double)), ("syy", C.POINTER(C.c_double)),
                 ("sxy", C.POINTER(C.c_double)), ("reflection_cap_hits", C.c_int64),
-                ("walker_steps", C.c_int64), ("boundary_hits", C.c_int64)]
+                ("walker_steps", C.c_int64), ("boundary_hits", C.c_int64),
+                ("mx_in", C.POINTER(C.c_double)), ("my_in", C.POINTER(C.c_double)),
+                ("walkers_in", C.c_int64)]
 
 
 class Job(C.Structure):

@@ -351,6 +351,10 @@ class RunResult:
         self.sxx, self.syy, self.sxy = sxx, syy, sxy
         self.cap_hits, self.walker_steps, self.n = cap_hits, walker_steps, n
         self.hits = hits
+        # start-compartment sums (run_lattice(compartments=True)): walkers
+        # that start inside a basis, and how many they are
+        self.mx_in = self.my_in = None
+        self.n_in = None
 
     @property
     def signal(self):
@@ -382,24 +386,31 @@ def _params(n, steps, seed, timestep, flags, init_mode=0, init_arg=0, gamma=GAMM
 def run_lattice(lattice: Lattice, basis: Sequence, seqs: Sequence, num_walkers: int, steps: int,
                 timestep: float, seed: int, *, specular=True, relaxation=False, permeable=False,
                 init_mode=0, init_arg=0, gamma=GAMMA, walker_offset=0, device: Device = None,
-                allow_cap=False) -> RunResult:
-    """One lattice walk (axx_run_lattice): host records in, FP64 sums out."""
+                allow_cap=False, compartments=False) -> RunResult:
+    """One lattice walk (axx_run_lattice): host records in, FP64 sums out.
+    compartments: also the sums over the walkers that start inside a basis
+    (result.mx_in, result.my_in, result.n_in)."""
     dev = device or default_device()
     L = N.lib()
     M = len(seqs)
     b = N.array_of(N.Basis, [x.record() for x in basis])
     s = N.array_of(N.SequenceRec, [q.record() for q in seqs])
-    p = _params(num_walkers, steps, seed, timestep, run_flags(specular, relaxation, permeable),
-                init_mode, init_arg, gamma, walker_offset)
-    out = [np.zeros(max(M, 1)) for _ in range(5)]
+    flags = run_flags(specular, relaxation, permeable) | (N.FLAG_COMPARTMENTS if compartments
+                                                          else 0)
+    p = _params(num_walkers, steps, seed, timestep, flags, init_mode, init_arg, gamma,
+                walker_offset)
+    out = [np.zeros(max(M, 1)) for _ in range(7)]
     ptr = [o.ctypes.data_as(C.POINTER(C.c_double)) for o in out]
-    st = N.Stats(ptr[2], ptr[3], ptr[4], 0, 0, 0)
+    st = N.Stats(ptr[2], ptr[3], ptr[4], 0, 0, 0, ptr[5], ptr[6], 0)
     rc = L.axx_run_lattice(dev.h, C.byref(lattice.record()), b, len(basis), s, M, C.byref(p),
                            ptr[0], ptr[1], C.byref(st))
     if not (allow_cap and rc == 3):
         N.check(rc, dev.h)
-    return RunResult(*(o[:M] for o in out), st.reflection_cap_hits, st.walker_steps,
-                     int(num_walkers), st.boundary_hits)
+    r = RunResult(*(o[:M] for o in out[:5]), st.reflection_cap_hits, st.walker_steps,
+                  int(num_walkers), st.boundary_hits)
+    if compartments:
+        r.mx_in, r.my_in, r.n_in = out[5][:M], out[6][:M], int(st.walkers_in)
+    return r
 
 
 def run_single(basis, seqs: Sequence, num_walkers: int, steps: int, timestep: float, seed: int,

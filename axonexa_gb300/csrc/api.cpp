@@ -31,6 +31,7 @@ struct axx_plan {
   axx_ctx *ctx = nullptr;
   WalkParams P{};
   int geom = 0, km = 0, kmax = 1, grid = 0, M = 0, K = 0, n_inst = 0;
+  int Mo = 0;  // rows of sums: M, or 2M with the start-compartment sums
   size_t smem = 0;
   size_t upload_bytes = 0;
   void *arena = nullptr;
@@ -89,12 +90,16 @@ axx_status build_plan(axx_ctx *ctx, const GeomPlan &g, const SeqPlan &sq, int M,
   InitSpec init;
   err = init_spec(g, basis, nbasis, mode, p, init);
   if (!err.empty()) return fail(ctx, AXX_ERR_INVALID_ARG, err);
-  const size_t smem = walk_smem_bytes(g, M);
+  if ((p->flags & AXX_FLAG_COMPARTMENTS) && mode != AXX_MODE_LATTICE)
+    return fail(ctx, AXX_ERR_INVALID_ARG, "compartment sums exist for lattice walks only");
+  const int Mo = (p->flags & AXX_FLAG_COMPARTMENTS) ? 2 * M : M;
+  const size_t smem = walk_smem_bytes(g, Mo);
   if (smem > AXX_SMEM_MAX)
     return fail(ctx, AXX_ERR_UNSUPPORTED,
                 "substrate tables and sequence sums exceed the shared-memory budget (" +
                     std::to_string(smem) + " bytes)");
-  const bool one = g.geo.size() == 1 && g.cstart.size() == 2;  // one instance, one cell
+  // one instance, one cell, no compartment sums: the single-instance kernels
+  const bool one = g.geo.size() == 1 && g.cstart.size() == 2 && !(p->flags & AXX_FLAG_COMPARTMENTS);
   const int occ = occupancy_walk(g.geom, kt.km, kt.kmax, false, one, smem);
   if (occ <= 0) return fail(ctx, AXX_ERR_CUDA, "walk kernel cannot be resident (occupancy 0)");
   auto *pl = new axx_plan();
@@ -104,13 +109,14 @@ axx_status build_plan(axx_ctx *ctx, const GeomPlan &g, const SeqPlan &sq, int M,
   pl->kmax = kt.kmax;
   pl->K = kt.K;
   pl->M = M;
+  pl->Mo = Mo;
   pl->n_inst = (int)g.geo.size();
   pl->smem = smem;
   // grid: the device's resident capacity, at most one warp per 32 walkers
   const long long ntask = (p->num_walkers + 31) / 32;
   const long long want = (ntask + AXX_BLOCK / 32 - 1) / (AXX_BLOCK / 32);
   pl->grid = (int)std::min<long long>(want, (long long)occ * ctx->nsm);
-  const ArenaLayout L = arena_layout(g, kt, M);
+  const ArenaLayout L = arena_layout(g, kt, Mo);
   pl->upload_bytes = L.upload;
   cudaError_t e = cudaMalloc(&pl->arena, L.fixed + L.per_block * pl->grid);
   if (e != cudaSuccess) {
@@ -187,9 +193,9 @@ axx_status make_single_plan(axx_ctx *ctx, const axx_basis *basis, const axx_sequ
 axx_status read_results(axx_plan *pl, double *mx, double *my, axx_stats *stats) {
   axx_ctx *ctx = pl->ctx;
   AXX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-  std::vector<double> h((size_t)pl->M * 5);
+  std::vector<double> h((size_t)pl->Mo * 5);
   unsigned long long cnt[AXX_CNT_N] = {0};
-  if (pl->M > 0)
+  if (pl->Mo > 0)
     AXX_CUDA(ctx, cudaMemcpy(h.data(), pl->out, h.size() * 8, cudaMemcpyDeviceToHost));
   AXX_CUDA(ctx, cudaMemcpy(cnt, pl->counters, sizeof(cnt), cudaMemcpyDeviceToHost));
   for (int m = 0; m < pl->M; ++m) {
@@ -205,6 +211,13 @@ axx_status read_results(axx_plan *pl, double *mx, double *my, axx_stats *stats) 
     stats->reflection_cap_hits = (int64_t)cnt[AXX_CNT_CAP];
     stats->walker_steps = pl->walker_steps;
     stats->boundary_hits = (int64_t)cnt[AXX_CNT_HITS];
+    if (pl->Mo > pl->M) {
+      for (int m = 0; m < pl->M; ++m) {
+        if (stats->mx_in) stats->mx_in[m] = h[(pl->M + m) * 5 + 0];
+        if (stats->my_in) stats->my_in[m] = h[(pl->M + m) * 5 + 1];
+      }
+      stats->walkers_in = (int64_t)cnt[AXX_CNT_START_IN];
+    }
   }
   if (cnt[AXX_CNT_ABORTED]) return fail(ctx, AXX_ERR_ABORTED, "run aborted by axx_abort");
   if (cnt[AXX_CNT_INIT_FAIL])
@@ -327,7 +340,7 @@ axx_status axx_plan_launch(axx_plan *pl) {
   TraceParams T{};
   AXX_CUDA(ctx, launch_walk(pl->geom, pl->km, pl->kmax, false, pl->P, T, pl->grid, pl->smem,
                             ctx->stream));
-  AXX_CUDA(ctx, launch_reduce_partials(pl->P.partials, pl->grid, pl->M * 5, pl->out, ctx->stream));
+  AXX_CUDA(ctx, launch_reduce_partials(pl->P.partials, pl->grid, pl->Mo * 5, pl->out, ctx->stream));
   pl->launched = true;
   return AXX_OK;
 }

@@ -14,7 +14,8 @@
 //                      (one row of KMAX values per step; padded channels 0)
 //   coef[M*KMAX]       FP64 gamma*dt*G_m*alpha_mc: phase of sequence m from
 //                      the channel accumulators (0 for padded channels)
-//   partials[grid*M*5] FP64 per-block sums (x, y, x^2, y^2, xy), scratch
+//   partials[grid*Mo*5] FP64 per-block sums (x, y, x^2, y^2, xy) of the Mo = M
+//                      rows (2M with compartment sums), scratch
 #pragma once
 #include <stdint.h>
 
@@ -43,7 +44,7 @@ enum { AXX_GEOM_FREE = 0, AXX_GEOM_CYL = 1, AXX_GEOM_SPH = 2, AXX_GEOM_MIX = 3 }
 
 // counters[] slots
 enum { AXX_CNT_CAP = 0, AXX_CNT_INIT_FAIL = 1, AXX_CNT_ABORTED = 2, AXX_CNT_HITS = 3,
-       AXX_CNT_N = 4 };
+       AXX_CNT_START_IN = 4, AXX_CNT_N = 5 };
 
 struct WalkParams {
   float a, b, c;  // periodic cell
@@ -78,6 +79,7 @@ struct WalkParams {
   const float *wave_il;       // [steps][kmax]
   float ch_p[AXX_KMAX][3];    // channel projections (0 for padded channels)
   int M;
+  int compart;                // also sums over walkers starting in a basis: rows M..2M-1
   const double *coef;         // [M][kmax]
   double *partials;
   unsigned long long *counters;

@@ -442,6 +442,8 @@ static axx_status batch_build(axx_ctx *ctx, const axx_job *jobs, int njobs,
       return bfail(ctx, AXX_ERR_INVALID_ARG, "job " + std::to_string(j) + ": invalid run parameters");
     if (p.flags & AXX_FLAG_SIMPLE_REJECTION)
       return bfail(ctx, AXX_ERR_UNSUPPORTED, "batched jobs use specular reflection");
+    if (p.flags & AXX_FLAG_COMPARTMENTS)
+      return bfail(ctx, AXX_ERR_UNSUPPORTED, "batched jobs return whole-substrate sums only");
     if (J.nseq > kBatchMaxSeq)
       return bfail(ctx, AXX_ERR_INVALID_ARG, "a batched job has at most 64 sequences");
     const double gamma = p.gamma > 0.0 ? p.gamma : kGammaDefault;

@@ -111,10 +111,12 @@ extern "C" axx_status axx_run_lattice_noalloc(axx_ctx *ctx, const axx_lattice *l
   InitSpec init;
   err = init_spec(g, basis, nbasis, AXX_MODE_LATTICE, p, init);
   if (!err.empty()) return fail(ctx, AXX_ERR_INVALID_ARG, err);
-  const size_t smem = walk_smem_bytes(g, M);
+  const int Mo = (p->flags & AXX_FLAG_COMPARTMENTS) ? 2 * M : M;  // rows of sums
+  const size_t smem = walk_smem_bytes(g, Mo);
   if (smem > AXX_SMEM_MAX)
     return fail(ctx, AXX_ERR_UNSUPPORTED, "substrate tables exceed the shared-memory budget");
-  const bool one = g.geo.size() == 1 && g.cstart.size() == 2;  // one instance, one cell
+  // one instance, one cell, no compartment sums: the single-instance kernels
+  const bool one = g.geo.size() == 1 && g.cstart.size() == 2 && !(p->flags & AXX_FLAG_COMPARTMENTS);
   const int occ = occupancy_walk(g.geom, kt.km, kt.kmax, false, one, smem);
   if (occ <= 0) return fail(ctx, AXX_ERR_CUDA, "walk kernel cannot be resident");
   const long long ntask = (p->num_walkers + 31) / 32;
@@ -122,7 +124,7 @@ extern "C" axx_status axx_run_lattice_noalloc(axx_ctx *ctx, const axx_lattice *l
   long long grid = std::min<long long>(want, (long long)occ * ctx->nsm);
 
   // layout inside the scratch array; the partials shrink the grid if needed
-  const ArenaLayout Lo = arena_layout(g, kt, M);
+  const ArenaLayout Lo = arena_layout(g, kt, Mo);
   if (Lo.fixed > kScratchBytes ||
       (Lo.per_block > 0 &&
        Lo.fixed + Lo.per_block * std::min<long long>(grid, ctx->nsm) > kScratchBytes)) {
@@ -147,13 +149,13 @@ extern "C" axx_status axx_run_lattice_noalloc(axx_ctx *ctx, const axx_lattice *l
   TraceParams T{};
   e = launch_walk(g.geom, kt.km, kt.kmax, false, P, T, (int)grid, smem, s);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "walk kernel launch");
-  e = launch_reduce_partials(P.partials, (int)grid, M * 5, (double *)(base + Lo.o_out), s);
+  e = launch_reduce_partials(P.partials, (int)grid, Mo * 5, (double *)(base + Lo.o_out), s);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "reduction launch");
   const size_t o_out = Lo.o_out, o_cnt = Lo.o_cnt;
 
-  std::vector<double> h((size_t)M * 5);
+  std::vector<double> h((size_t)Mo * 5);
   unsigned long long cnt[AXX_CNT_N] = {0};
-  if (M > 0) e = cudaMemcpyAsync(h.data(), base + o_out, h.size() * 8, cudaMemcpyDeviceToHost, s);
+  if (Mo > 0) e = cudaMemcpyAsync(h.data(), base + o_out, h.size() * 8, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(cnt, base + o_cnt, sizeof(cnt), cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "reading the no-allocation results");
@@ -170,6 +172,13 @@ extern "C" axx_status axx_run_lattice_noalloc(axx_ctx *ctx, const axx_lattice *l
     stats->reflection_cap_hits = (int64_t)cnt[AXX_CNT_CAP];
     stats->walker_steps = p->num_walkers * (int64_t)(p->steps - 1);
     stats->boundary_hits = (int64_t)cnt[AXX_CNT_HITS];
+    if (Mo > M) {
+      for (int m = 0; m < M; ++m) {
+        if (stats->mx_in) stats->mx_in[m] = h[(M + m) * 5 + 0];
+        if (stats->my_in) stats->my_in[m] = h[(M + m) * 5 + 1];
+      }
+      stats->walkers_in = (int64_t)cnt[AXX_CNT_START_IN];
+    }
   }
   if (cnt[AXX_CNT_ABORTED]) return fail(ctx, AXX_ERR_ABORTED, "run aborted by axx_abort");
   if (cnt[AXX_CNT_INIT_FAIL])

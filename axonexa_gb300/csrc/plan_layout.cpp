@@ -175,6 +175,7 @@ void fill_walk_params(WalkParams &P, char *base, const ArenaLayout &L, const Geo
   for (int c = 0; c < AXX_KMAX; ++c)
     for (int k = 0; k < 3; ++k) P.ch_p[c][k] = kt.ch_p[c][k];
   P.M = M;
+  P.compart = (mode == AXX_MODE_LATTICE && (p->flags & AXX_FLAG_COMPARTMENTS)) ? 1 : 0;
   P.coef = (const double *)(base + L.o_coef);
   P.partials = (double *)(base + L.o_part);
   P.counters = (unsigned long long *)(base + L.o_cnt);

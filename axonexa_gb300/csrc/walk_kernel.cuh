@@ -768,6 +768,22 @@ __device__ __forceinline__ WalkResult walk_one(const WalkParams &P, const SmemVi
   return res;
 }
 
+// Whether the lattice walker `wid` starts inside a basis (region != 0): its
+// start drawn again from the head of its stream, so the walk itself keeps
+// no register for it.
+template <int GEOM, int KM>
+__device__ __forceinline__ bool starts_inside(const WalkParams &P, const SmemView &S,
+                                           long long wid) {
+  if (GEOM == AXX_GEOM_FREE) return false;
+  DevStream st;
+  st.init(P, (uint64_t)(wid + P.walker_offset), 1u);
+  float x, y, z;
+  init_position<GEOM, KM>(P, S, st, x, y, z);
+  const int cell = cell_of<GEOM>(P, x, y, z);
+  return S.region[lookup_list<GEOM>(S, S.cstart[cell], S.cstart[cell + 1], P.ecs_slot, x, y,
+                                    z)] != 0;
+}
+
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -788,10 +804,13 @@ __global__ void __launch_bounds__(AXX_BLOCK, ONEONLY && KMAX <= 4 ? AXX_MIN_BLOC
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   double *wsum = reinterpret_cast<double *>(smem);
   const int M = P.M;
-  for (int j = threadIdx.x; j < warps * M * 5; j += blockDim.x) wsum[j] = 0.0;
+  // rows of sums: all walkers, then those starting inside a basis (the
+  // compartment sums run in the general instantiations only)
+  const int Mo = (!ONEONLY && P.compart) ? 2 * M : M;
+  for (int j = threadIdx.x; j < warps * Mo * 5; j += blockDim.x) wsum[j] = 0.0;
 
   // stage the substrate tables (layout fixed by the host planner)
-  float4 *sg = reinterpret_cast<float4 *>(smem + (size_t)warps * M * 5 * sizeof(double));
+  float4 *sg = reinterpret_cast<float4 *>(smem + (size_t)warps * Mo * 5 * sizeof(double));
   float4 *sa = sg + P.n_inst;
   float4 *ss = sa + P.n_inst;
   uint32_t *sc = reinterpret_cast<uint32_t *>(ss + P.n_slot);
@@ -819,7 +838,7 @@ __global__ void __launch_bounds__(AXX_BLOCK, ONEONLY && KMAX <= 4 ? AXX_MIN_BLOC
   const long long ntask = (P.n_walkers + 31) / 32;
   const long long gwarp = (long long)blockIdx.x * warps + wib;
   const long long nwarp = (long long)gridDim.x * warps;
-  unsigned caps = 0, hits = 0, init_fail = 0, aborted = 0;
+  unsigned caps = 0, hits = 0, init_fail = 0, aborted = 0, start_in = 0;
   // a single instance (one basis without reachable ghosts, or a single pore)
   // is held in registers instead of walking a list
   const bool one = (GEOM != AXX_GEOM_FREE) && P.n_inst == 1 && P.ncell == 1;
@@ -830,6 +849,7 @@ __global__ void __launch_bounds__(AXX_BLOCK, ONEONLY && KMAX <= 4 ? AXX_MIN_BLOC
 #pragma unroll
     for (int c = 0; c < KMAX; ++c) W.acc[c] = W.cmp[c] = 0.0f;
     W.t2s = W.t2c = 0.0f;
+    bool in0 = false;
     if (active) {
       WalkResult r;
       if constexpr (ONEONLY)
@@ -843,6 +863,10 @@ __global__ void __launch_bounds__(AXX_BLOCK, ONEONLY && KMAX <= 4 ? AXX_MIN_BLOC
       hits += r.hits;
       init_fail += r.init_fail ? 1u : 0u;
       aborted += r.aborted ? 1u : 0u;
+      if constexpr (KM < AXX_KM_SINGLE && !ONEONLY) {
+        if (P.compart) in0 = starts_inside<GEOM, KM>(P, S, wid);
+        start_in += in0 ? 1u : 0u;
+      }
     }
     // FP64 epilogue (reference: transformAndSumTwoVectors with
     // COS/SIN_EXP_BINARY, src/util/cudaVector.cu:165-171, src/util/misc.cuh:29-39)
@@ -860,12 +884,21 @@ __global__ void __launch_bounds__(AXX_BLOCK, ONEONLY && KMAX <= 4 ? AXX_MIN_BLOC
       const double s0 = warp_sum(xv), s1 = warp_sum(yv), s2 = warp_sum(xv * xv),
                    s3 = warp_sum(yv * yv), s4 = warp_sum(xv * yv);
       if (lane == 0) {
-        double *d = wsum + ((size_t)wib * M + m) * 5;
+        double *d = wsum + ((size_t)wib * Mo + m) * 5;
         d[0] += s0;
         d[1] += s1;
         d[2] += s2;
         d[3] += s3;
         d[4] += s4;
+      }
+      if (!ONEONLY && P.compart) {  // the same over the walkers that started inside a basis
+        // (x and y only: the rows' other entries stay 0)
+        const double t0 = warp_sum(in0 ? xv : 0.0), t1 = warp_sum(in0 ? yv : 0.0);
+        if (lane == 0) {
+          double *d = wsum + ((size_t)wib * Mo + M + m) * 5;
+          d[0] += t0;
+          d[1] += t1;
+        }
       }
     }
   }
@@ -873,11 +906,13 @@ __global__ void __launch_bounds__(AXX_BLOCK, ONEONLY && KMAX <= 4 ? AXX_MIN_BLOC
   if (hits) atomicAdd(&P.counters[AXX_CNT_HITS], (unsigned long long)hits);
   if (init_fail) atomicAdd(&P.counters[AXX_CNT_INIT_FAIL], (unsigned long long)init_fail);
   if (aborted) atomicAdd(&P.counters[AXX_CNT_ABORTED], (unsigned long long)aborted);
+  if (!ONEONLY && start_in)
+    atomicAdd(&P.counters[AXX_CNT_START_IN], (unsigned long long)start_in);
   __syncthreads();
-  for (int j = threadIdx.x; j < M * 5; j += blockDim.x) {
+  for (int j = threadIdx.x; j < Mo * 5; j += blockDim.x) {
     double s = 0.0;
-    for (int q = 0; q < warps; ++q) s += wsum[(size_t)q * M * 5 + j];
-    P.partials[(size_t)blockIdx.x * M * 5 + j] = s;
+    for (int q = 0; q < warps; ++q) s += wsum[(size_t)q * Mo * 5 + j];
+    P.partials[(size_t)blockIdx.x * Mo * 5 + j] = s;
   }
 }
 

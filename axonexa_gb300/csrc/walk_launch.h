@@ -20,11 +20,12 @@ AXX_DECLARE_WALK(mix)
 #undef AXX_DECLARE_WALK
 
 // one: the plan has a single instance and a single cell (P.n_inst == 1,
-// P.ncell == 1), which selects the instantiations compiled for that case.
+// P.ncell == 1) and no compartment sums, which selects the instantiations
+// compiled for that case.
 inline cudaError_t launch_walk(int geom, int km, int kmax, bool trace, const WalkParams &P,
                                const TraceParams &T, int grid, size_t smem, cudaStream_t s) {
   const bool single = km >= AXX_KM_SINGLE;
-  const bool one = P.n_inst == 1 && P.ncell == 1;
+  const bool one = P.n_inst == 1 && P.ncell == 1 && !P.compart;
   switch (geom) {
     case AXX_GEOM_FREE: return launch_walk_free(km, kmax, trace, one, P, T, grid, smem, s);
     case AXX_GEOM_CYL:

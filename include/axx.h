@@ -146,9 +146,13 @@ enum {
                                            by value does (Sphere.cuh:55); default on in
                                            axx_run_single unless AXX_FLAG_FIX_INIT_QUIRK */
   AXX_FLAG_FIX_INIT_QUIRK = 1u << 4,
-  AXX_FLAG_LATTICE_PICKING = 1u << 5    /* single pore, LATTICE_PICKING (kernelPhase.cuh:31-35):
+  AXX_FLAG_LATTICE_PICKING = 1u << 5,   /* single pore, LATTICE_PICKING (kernelPhase.cuh:31-35):
                                            every move is +-stepLength along each axis, the
                                            signs from three stream words */
+  AXX_FLAG_COMPARTMENTS = 1u << 6       /* lattice walks: also the sums over the walkers that
+                                           start inside a basis (Lattice::inRegion != 0), in
+                                           axx_stats.mx_in/my_in/walkers_in; the rest of the
+                                           signal is the extracellular start compartment */
 };
 
 enum { AXX_INIT_UNIFORM = 0,     /* Lattice::initializeUniformly (lattice.cuh:31-37) */
@@ -175,6 +179,10 @@ typedef struct {
   int64_t reflection_cap_hits; /* walker-steps that hit the reflection cap */
   int64_t walker_steps;  /* moves simulated (num_walkers * (steps - 1)) */
   int64_t boundary_hits; /* reflections and transmissions over all moves */
+  /* With AXX_FLAG_COMPARTMENTS (else left untouched): */
+  double *mx_in;         /* nseq sums of x over the walkers starting inside a basis */
+  double *my_in;         /* nseq sums of y over them */
+  int64_t walkers_in;    /* how many walkers started inside a basis */
 } axx_stats;
 
 /* ---- context ------------------------------------------------------------- */

@@ -591,6 +591,7 @@ struct WalkOut {
   std::vector<double> phase;
   double t2factor = 0.0;  // the value whose exp weights the signal
   int64_t caps = 0;
+  bool start_in = false;  // lattice walks: the start lies inside a basis (region != 0)
 };
 
 struct TraceRow {
@@ -665,6 +666,7 @@ void walk_ref(const WalkIn &in, const RefLattice &L, int64_t w, WalkOut &out, Tr
     tr->init_pos[2] = r.z;
   }
   V3 ru = r;
+  out.start_in = !in.single && L.region(r) != 0;
   if (on_move) (*on_move)(0, r);
   for (int j = 0; j < in.nseq; ++j) out.phase[j] = in.gamma * dot(gfunc(in.seqs[j], 0.0), r) * dt;
   double T2f = 0.0;
@@ -831,6 +833,7 @@ void walk_kern(const WalkIn &in, const KGeom<T> &G, int64_t w, WalkOut &out, Tra
     out.phase[j] = in.gamma * dot(gfunc(in.seqs[j], 0.0), V3{(double)x, (double)y, (double)z}) * dt;
   T t2s = 0, t2c = 0;
   int slot = in.single ? 0 : k_lookup(G, x, y, z);
+  out.start_in = !in.single && G.region[slot] != 0;
   const bool geom = !G.inst.empty();
   for (int i = 1; i < p.steps; ++i) {
     const T v = G.speed[slot], Ls = G.step[slot];
@@ -1132,7 +1135,10 @@ int orc_walk(const orc_lattice *lat, const orc_basis *basis, int nbasis, const o
   const int64_t N = p->num_walkers;
   if (nthreads < 1) nthreads = 1;
   if ((int64_t)nthreads > N) nthreads = (int)N;
-  std::vector<std::vector<double>> part(nthreads, std::vector<double>((size_t)nseq * 5, 0.0));
+  // flag 64 (compartment sums): rows nseq..2nseq-1 sum the walkers that start
+  // inside a basis
+  const int rows = (!in.single && (p->flags & 64u)) ? 2 * nseq : nseq;
+  std::vector<std::vector<double>> part(nthreads, std::vector<double>((size_t)rows * 5, 0.0));
   std::vector<int64_t> caps(nthreads, 0);
   auto work = [&](int t) {
     const int64_t w0 = N * t / nthreads, w1 = N * (t + 1) / nthreads;
@@ -1162,6 +1168,14 @@ int orc_walk(const orc_lattice *lat, const orc_basis *basis, int nbasis, const o
         s[2] += xv * xv;
         s[3] += yv * yv;
         s[4] += xv * yv;
+        if (rows > nseq && out.start_in) {
+          double *q = &part[t][(size_t)(nseq + j) * 5];
+          q[0] += xv;
+          q[1] += yv;
+          q[2] += xv * xv;
+          q[3] += yv * yv;
+          q[4] += xv * yv;
+        }
       }
     }
   };
@@ -1172,7 +1186,7 @@ int orc_walk(const orc_lattice *lat, const orc_basis *basis, int nbasis, const o
     for (int t = 0; t < nthreads; ++t) th.emplace_back(work, t);
     for (auto &x : th) x.join();
   }
-  for (int j = 0; j < nseq * 5; ++j) {
+  for (int j = 0; j < rows * 5; ++j) {
     double s = 0.0;
     for (int t = 0; t < nthreads; ++t) s += part[t][j];
     sums[j] = s;

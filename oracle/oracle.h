@@ -80,8 +80,11 @@ void orc_sincos_2pi_f32(float u, float *s, float *c);
 
 /* Signal sums of a lattice walk (lat != NULL) or a single-pore walk
  * (lat == NULL, walkers start in basis[0]).  sums[5*j..5*j+4] =
- * (sum x, sum y, sum x^2, sum y^2, sum xy) for sequence j.  Walkers are
- * split over nthreads host threads (partial sums combined in thread order).
+ * (sum x, sum y, sum x^2, sum y^2, sum xy) for sequence j.  With flag 64
+ * (compartment sums) on a lattice, rows nseq..2*nseq-1 hold the same sums
+ * over the walkers that start inside a basis (sums has 10*nseq entries).
+ * Walkers are split over nthreads host threads (partial sums combined in
+ * thread order).
  * Returns 0, or a negative code for invalid input. */
 int orc_walk(const orc_lattice *lat, const orc_basis *basis, int nbasis,
              const orc_sequence *seqs, int nseq, const orc_params *p, int mode, int nthreads,

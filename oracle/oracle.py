@@ -116,11 +116,14 @@ def _shape_trace(bufs, ntrace, steps):
 
 
 def walk(lat, bases, seqs, params, mode=REF64, nthreads=1, ntrace=0):
-    """Runs the oracle.  lat None = single pore.  Returns (sums[M,5], trace|None, caps)."""
+    """Runs the oracle.  lat None = single pore.  Returns (sums[M,5], trace|None, caps);
+    with flag 64 (compartment sums) on a lattice, sums[2M,5]: rows M.. sum the
+    walkers that start inside a basis."""
     L = lib()
     b = _arr(bases, Basis)
     s = _arr(seqs, Sequence)
-    sums = np.zeros(max(len(seqs), 1) * 5)
+    rows = 2 * len(seqs) if (lat is not None and params.flags & 64) else len(seqs)
+    sums = np.zeros(max(rows, 1) * 5)
     tr, bufs = (make_trace(ntrace, params.steps) if ntrace else (None, None))
     caps = C.c_int64(0)
     rc = L.orc_walk(C.byref(lat) if lat is not None else None, b, len(bases), s, len(seqs),
@@ -129,7 +132,7 @@ def walk(lat, bases, seqs, params, mode=REF64, nthreads=1, ntrace=0):
                     C.byref(tr) if tr is not None else None, C.byref(caps))
     if rc != 0:
         raise ValueError("orc_walk failed: %d" % rc)
-    return (sums[: len(seqs) * 5].reshape(len(seqs), 5),
+    return (sums[: rows * 5].reshape(rows, 5),
             _shape_trace(bufs, ntrace, params.steps) if ntrace else None, caps.value)
 
 
