@@ -15,5 +15,6 @@ from .magnetization import (COS_GRE, QSC_COS_GRE, QSC_GRE, QSC_GRE_TRAP, QSC_PGS
                             SIN_GRE, UCN_lowfield, magAcquisition, magAcquisitionStream,
                             run_mag, trace_mag)
 from .acquisition import run_wc, wc_start
+from .mesh import Mesh, Triangle, cube, icosphere, prism, run_mesh, trace_mesh
 
 __all__ = [n for n in dir() if not n.startswith("_")]

@@ -69,6 +69,11 @@ class Stats(C.Structure):
                 ("walkers_in", C.c_int64)]
 
 
+class MeshRec(C.Structure):
+    _fields_ = [("vertices", C.POINTER(C.c_double)), ("nvert", C.c_int32),
+                ("triangles", C.POINTER(C.c_int32)), ("ntri", C.c_int32), ("D", C.c_double)]
+
+
 class Job(C.Structure):
     _fields_ = [("mode", C.c_int32), ("lattice", LatticeRec), ("basis", C.POINTER(Basis)),
                 ("nbasis", C.c_int32), ("seqs", C.POINTER(SequenceRec)), ("nseq", C.c_int32),
@@ -191,6 +196,12 @@ _SIGS = {
                        C.POINTER(MagParams), C.c_int, C.POINTER(C.c_float),
                        C.POINTER(C.c_float), C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                        C.POINTER(C.c_float)], C.c_int),
+    "axx_run_mesh": ([C.c_void_p, C.POINTER(MeshRec), C.POINTER(SequenceRec), C.c_int,
+                      C.POINTER(RunParams), C.POINTER(C.c_double), C.POINTER(C.c_double),
+                      C.POINTER(Stats), C.POINTER(C.c_int64)], C.c_int),
+    "axx_trace_mesh": ([C.c_void_p, C.POINTER(MeshRec), C.POINTER(RunParams), C.c_int,
+                        C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_int32),
+                        C.POINTER(C.c_int32), C.POINTER(C.c_int64)], C.c_int),
 }
 
 _lib = None

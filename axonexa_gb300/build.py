@@ -36,6 +36,7 @@ CUDA_SOURCES = [
     "mag.cu",
     "calcf.cu",
     "wc.cu",
+    "mesh.cu",
 ]
 HOST_SOURCES = ["api.cpp", "frame.cpp", "host_plan.cpp", "plan_layout.cpp", "substrate.cpp"]
 

@@ -479,6 +479,37 @@ axx_status axx_trace_mag(axx_ctx *ctx, const axx_basis *pore, const axx_field *f
                          const axx_mag_params *params, int ntrace, float *init_pos, float *pos,
                          int32_t *hits, int32_t *words, float *m_final);
 
+/* ---- triangle-mesh pores -------------------------------------------------- */
+
+/* A closed triangle mesh as a single pore (src/primitives/mesh.cuh:1-75 and
+ * triangle.cuh:1-59, drafts that do not compile: "We assume no holes -> a
+ * closed surface mesh").  Walkers start uniformly inside (rejection in the
+ * bounding box with the mesh's vertical-ray parity test), move with speed
+ * sqrt(6 D / dt) and reflect specularly off the nearest triangle hit
+ * (Triangle::intersect: the plane of the triangle, then the barycentric
+ * inside test, slightly widened so that shared edges leave no gap); the phase
+ * uses the bounded position as the single-pore walk does. */
+typedef struct {
+  const double *vertices;    /* [nvert][3] */
+  int32_t nvert;
+  const int32_t *triangles;  /* [ntri][3] vertex indices, any orientation */
+  int32_t ntri;
+  double D;                  /* diffusion coefficient inside */
+} axx_mesh;
+
+/* One mesh-pore walk; params->flags must be 0 (specular reflection only),
+ * init_mode is ignored.  escaped: walkers found outside the mesh after their
+ * walk (a leak through the surface; 0 for a closed mesh), may be NULL. */
+axx_status axx_run_mesh(axx_ctx *ctx, const axx_mesh *mesh, const axx_sequence *seqs, int nseq,
+                        const axx_run_params *params, double *mx, double *my, axx_stats *stats,
+                        int64_t *escaped);
+/* The first ntrace walkers of the same walk: start init_pos[3], position
+ * after every move pos[(steps-1)*3], triangle hits and next stream word per
+ * move. */
+axx_status axx_trace_mesh(axx_ctx *ctx, const axx_mesh *mesh, const axx_run_params *params,
+                          int ntrace, float *init_pos, float *pos, int32_t *hits, int32_t *words,
+                          int64_t *escaped);
+
 /* The placement step of axx_substrate_rps_gamma for caller-chosen radii
  * (radii[n], any order; they are sorted ascending and region = index+1 in that
  * order).  Same cell, gap, image and output rules. */

@@ -12,6 +12,7 @@
 #include <cstring>
 #include <functional>
 #include <limits>
+#include <map>
 #include <thread>
 #include <type_traits>
 #include <vector>
@@ -1061,6 +1062,318 @@ V3 mag_update(const orc_field &f, const orc_mag_params &p, const V3 &r, const V3
 
 }  // namespace
 
+// ----------------------------------------------------------- mesh pores ---
+// A closed triangle mesh as a single pore (the reference's drafts
+// src/primitives/mesh.cuh:1-75, triangle.cuh:1-59, which do not compile):
+// Triangle::intersect (plane crossing, then barycentric inside test),
+// Mesh::intersect (nearest crossing), Mesh::inside (parity of a vertical
+// ray).  Restated in the GPU walker's formulation: triangles oriented
+// outward, crossings from inside to outside only (n.d > 0, from at most a
+// rounding slack beyond the plane), the watertight hit test; the parity of
+// the vertical rays up and down must agree.  Every triangle is tested (the
+// GPU's grid lists are conservative, so both find the same nearest hit).
+template <typename T>
+struct KMesh {
+  struct Tri {
+    T n[3], w, v[3][3];  // unit outward normal, n.v0, the vertices
+  };
+  std::vector<Tri> tri;
+  std::vector<char> vertical;  // |n_z| < 1e-9: never crossed by a vertical line
+  T lo[3], hi[3];
+  T slack = T(0);  // 4e-6 of the largest |coordinate|: a start rounded beyond a face meets it
+};
+
+// Outward orientation: the two triangles of an edge traverse it in opposite
+// directions ((b, c) swapped where they do not, breadth-first from the
+// lowest unvisited triangle), then each connected component with negative
+// signed volume flips.  -1 unless every edge has exactly two triangles.
+inline int mesh_orient(const double *vx, const int32_t *in, int ntri, std::vector<int32_t> &tris) {
+  tris.assign(in, in + 3 * (size_t)ntri);
+  std::map<std::pair<int, int>, std::vector<int>> edges;
+  for (int t = 0; t < ntri; ++t)
+    for (int j = 0; j < 3; ++j) {
+      const int a = tris[3 * t + j], b = tris[3 * t + (j + 1) % 3];
+      if (a == b) return -1;
+      edges[{std::min(a, b), std::max(a, b)}].push_back(t);
+    }
+  for (auto &kv : edges)
+    if (kv.second.size() != 2) return -1;
+  auto dir = [&](int t, int a, int b) {
+    for (int j = 0; j < 3; ++j) {
+      const int u = tris[3 * t + j], v = tris[3 * t + (j + 1) % 3];
+      if (u == a && v == b) return 1;
+      if (u == b && v == a) return -1;
+    }
+    return 0;
+  };
+  std::vector<int> comp(ntri, -1);
+  int nc = 0;
+  for (int s0 = 0; s0 < ntri; ++s0) {
+    if (comp[s0] >= 0) continue;
+    std::vector<int> q{s0};
+    comp[s0] = nc;
+    for (size_t i = 0; i < q.size(); ++i) {
+      const int t = q[i];
+      for (int j = 0; j < 3; ++j) {
+        const int a = tris[3 * t + j], b = tris[3 * t + (j + 1) % 3];
+        for (int u : edges[{std::min(a, b), std::max(a, b)}]) {
+          if (u == t) continue;
+          if (comp[u] >= 0) {
+            if (dir(u, a, b) == dir(t, a, b)) return -1;
+            continue;
+          }
+          if (dir(u, a, b) == dir(t, a, b)) std::swap(tris[3 * u + 1], tris[3 * u + 2]);
+          comp[u] = nc;
+          q.push_back(u);
+        }
+      }
+    }
+    ++nc;
+  }
+  std::vector<double> vol(nc, 0.0);
+  for (int t = 0; t < ntri; ++t) {
+    const double *a = &vx[3 * tris[3 * t]], *b = &vx[3 * tris[3 * t + 1]],
+                 *c = &vx[3 * tris[3 * t + 2]];
+    vol[comp[t]] += a[0] * (b[1] * c[2] - b[2] * c[1]) - a[1] * (b[0] * c[2] - b[2] * c[0]) +
+                    a[2] * (b[0] * c[1] - b[1] * c[0]);
+  }
+  for (int t = 0; t < ntri; ++t)
+    if (vol[comp[t]] < 0.0) std::swap(tris[3 * t + 1], tris[3 * t + 2]);
+  return 0;
+}
+
+template <typename T>
+int mesh_build(const double *vx, int nvert, const int32_t *tris_in, int ntri, KMesh<T> &K) {
+  for (int i = 0; i < 3 * ntri; ++i)
+    if (tris_in[i] < 0 || tris_in[i] >= nvert) return -1;
+  std::vector<int32_t> tv;
+  if (mesh_orient(vx, tris_in, ntri, tv) != 0) return -1;
+  const int32_t *tris = tv.data();
+  double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+  for (int t = 0; t < ntri; ++t)
+    for (int j = 0; j < 3; ++j) {
+      const int v = tris[3 * t + j];
+      if (v < 0 || v >= nvert) return -1;
+      for (int k = 0; k < 3; ++k) {
+        lo[k] = std::min(lo[k], vx[3 * v + k]);
+        hi[k] = std::max(hi[k], vx[3 * v + k]);
+      }
+    }
+  for (int k = 0; k < 3; ++k) {
+    K.lo[k] = (T)lo[k];
+    K.hi[k] = (T)hi[k];
+  }
+  K.tri.resize(ntri);
+  K.vertical.assign(ntri, 0);
+  for (int t = 0; t < ntri; ++t) {
+    const double *p0 = &vx[3 * tris[3 * t]];
+    const double *p1 = &vx[3 * tris[3 * t + 1]];
+    const double *p2 = &vx[3 * tris[3 * t + 2]];
+    const double u[3] = {p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2]};
+    const double v[3] = {p2[0] - p0[0], p2[1] - p0[1], p2[2] - p0[2]};
+    double n[3] = {u[1] * v[2] - u[2] * v[1], u[2] * v[0] - u[0] * v[2],
+                   u[0] * v[1] - u[1] * v[0]};
+    const double nm = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    if (!(nm > 0.0)) return -1;
+    for (double &c : n) c /= nm;
+    const double w = n[0] * p0[0] + n[1] * p0[1] + n[2] * p0[2];
+    auto &r = K.tri[t];
+    for (int k = 0; k < 3; ++k) {
+      r.n[k] = (T)n[k];
+      r.v[0][k] = (T)p0[k];
+      r.v[1][k] = (T)p1[k];
+      r.v[2][k] = (T)p2[k];
+    }
+    r.w = (T)w;
+    K.vertical[t] = std::fabs(n[2]) < 1e-9 ? 1 : 0;
+  }
+  return 0;
+}
+
+// The vertical line through (px, py) against the triangle's projection on
+// (x, y): edge functions from the vertices relative to the point, zeros
+// counted only on "top-left" edges of the counter-clockwise oriented
+// projection (each edge or vertex counts for exactly one triangle).
+template <typename T>
+bool covers_xy(T px, T py, const T (&v)[3][3]) {
+  const T ax = v[0][0] - px, ay = v[0][1] - py, bx = v[1][0] - px, by = v[1][1] - py;
+  const T cx = v[2][0] - px, cy = v[2][1] - py;
+  T e0 = bx * cy - by * cx, e1 = cx * ay - cy * ax, e2 = ax * by - ay * bx;
+  const T area = e0 + e1 + e2;
+  if (area == T(0)) return false;
+  const T sg = area > T(0) ? T(1) : T(-1);
+  e0 *= sg;
+  e1 *= sg;
+  e2 *= sg;
+  auto tl = [&](T ux, T uy, T vx, T vy) {
+    const T dx = (vx - ux) * sg, dy = (vy - uy) * sg;
+    return dy > T(0) || (dy == T(0) && dx < T(0));
+  };
+  return (e0 > T(0) || (e0 == T(0) && tl(v[1][0], v[1][1], v[2][0], v[2][1]))) &&
+         (e1 > T(0) || (e1 == T(0) && tl(v[2][0], v[2][1], v[0][0], v[0][1]))) &&
+         (e2 > T(0) || (e2 == T(0) && tl(v[0][0], v[0][1], v[1][0], v[1][1])));
+}
+
+// 1 inside, 0 outside, -1 when the rays up and down disagree
+template <typename T>
+int mesh_side(const KMesh<T> &K, T x, T y, T z) {
+  int up = 0, down = 0;
+  for (size_t k = 0; k < K.tri.size(); ++k) {
+    if (K.vertical[k]) continue;
+    const auto &r = K.tri[k];
+    if (!covers_xy(x, y, r.v)) continue;
+    const T zh = (r.w - fmaT(r.n[0], x, r.n[1] * y)) / r.n[2];
+    up += zh > z ? 1 : 0;
+    down += zh < z ? 1 : 0;
+  }
+  if ((up & 1) != (down & 1)) return -1;
+  return up & 1;
+}
+
+// The watertight ray/triangle test (Woop, Benthin and Wald, JCGT 2013): the
+// ray's shear frame (rows m0, m1: 2-D coordinates with the ray at the
+// origin; m2: distance along the ray; kz the direction's largest
+// component), edge functions as differences of two products, zero edge
+// functions counted as hits.
+template <typename T>
+struct KShear {
+  T m[3][3];
+};
+
+template <typename T>
+KShear<T> k_shear(T dx, T dy, T dz) {
+  const T ax = std::fabs(dx), ay = std::fabs(dy), az = std::fabs(dz);
+  const int kz = (ax > ay) ? ((ax > az) ? 0 : 2) : ((ay > az) ? 1 : 2);
+  int kx = kz == 2 ? 0 : kz + 1, ky = kx == 2 ? 0 : kx + 1;
+  const T d[3] = {dx, dy, dz};
+  if (d[kz] < T(0)) std::swap(kx, ky);
+  const T sx = d[kx] / d[kz], sy = d[ky] / d[kz], sz = T(1) / d[kz];
+  KShear<T> M;
+  for (int c = 0; c < 3; ++c) {
+    M.m[0][c] = c == kx ? T(1) : (c == kz ? -sx : T(0));
+    M.m[1][c] = c == ky ? T(1) : (c == kz ? -sy : T(0));
+    M.m[2][c] = c == kz ? sz : T(0);
+  }
+  return M;
+}
+
+template <typename T>
+T k_watertight(const KShear<T> &M, T px, T py, T pz, const T (&v)[3][3]) {
+  T X[3], Y[3], Z[3];
+  for (int i = 0; i < 3; ++i) {
+    const T a = v[i][0] - px, b = v[i][1] - py, c = v[i][2] - pz;
+    X[i] = fmaT(M.m[0][0], a, fmaT(M.m[0][1], b, M.m[0][2] * c));
+    Y[i] = fmaT(M.m[1][0], a, fmaT(M.m[1][1], b, M.m[1][2] * c));
+    Z[i] = fmaT(M.m[2][0], a, fmaT(M.m[2][1], b, M.m[2][2] * c));
+  }
+  const T U = X[2] * Y[1] - Y[2] * X[1];
+  const T V = X[0] * Y[2] - Y[0] * X[2];
+  const T W = X[1] * Y[0] - Y[1] * X[0];
+  const T inf = std::numeric_limits<T>::infinity();
+  if ((U < T(0) || V < T(0) || W < T(0)) && (U > T(0) || V > T(0) || W > T(0))) return inf;
+  const T det = U + V + W;
+  if (det == T(0)) return inf;
+  const T Tn = fmaT(U, Z[0], fmaT(V, Z[1], W * Z[2]));
+  return Tn / det;
+}
+
+template <typename T>
+T mesh_hit(const KMesh<T> &K, int last, T px, T py, T pz, T dx, T dy, T dz, T rem, int &bk) {
+  T best = std::numeric_limits<T>::infinity();
+  bk = -1;
+  const KShear<T> M = k_shear(dx, dy, dz);
+  for (int k = 0; k < (int)K.tri.size(); ++k) {
+    if (k == last) continue;
+    const auto &r = K.tri[k];
+    const T dn = fmaT(r.n[0], dx, fmaT(r.n[1], dy, r.n[2] * dz));
+    if (!(dn > T(0))) continue;  // crossings from inside to outside only
+    const T np = fmaT(r.n[0], px, fmaT(r.n[1], py, r.n[2] * pz));
+    if (!(r.w - np > -K.slack)) continue;
+    const T s = k_watertight(M, px, py, pz, r.v);
+    if (s < rem && s < best) {
+      best = s;
+      bk = k;
+    }
+  }
+  return best;
+}
+
+template <typename T>
+void mesh_walk_one(const KMesh<T> &K, double D, const orc_sequence *seqs, int nseq,
+                   const orc_params &p, double gamma, int64_t w, WalkOut &out, TraceRow *tr,
+                   bool &escaped) {
+  const double dt = p.timestep;
+  Stream st{p.seed, (uint64_t)(w + p.walker_offset), 1u};
+  auto U = [](Stream &s) { return (T)s.uniform(); };
+  T x = 0, y = 0, z = 0;
+  bool ok = false;
+  for (int t = 0; t < 100000 && !ok; ++t) {
+    x = fmaT(U(st), K.hi[0] - K.lo[0], K.lo[0]);
+    y = fmaT(U(st), K.hi[1] - K.lo[1], K.lo[1]);
+    z = fmaT(U(st), K.hi[2] - K.lo[2], K.lo[2]);
+    ok = mesh_side(K, x, y, z) == 1;
+  }
+  if (tr) {
+    tr->init_pos[0] = (double)x;
+    tr->init_pos[1] = (double)y;
+    tr->init_pos[2] = (double)z;
+  }
+  for (int j = 0; j < nseq; ++j)
+    out.phase[j] = gamma * dot(gfunc(seqs[j], 0.0), V3{(double)x, (double)y, (double)z}) * dt;
+  const double sp = std::sqrt(6.0 * D / dt);
+  const T L = (T)(sp * dt);
+  for (int i = 1; i < p.steps; ++i) {
+    const T u1 = U(st), u2 = U(st);
+    T dx, dy, dz;
+    k_direction(u1, u2, dx, dy, dz);
+    T rem = L, sx = x, sy = y, sz = z;
+    int last = -1, nh = 0;
+    bool capped = false;
+    for (;;) {
+      int bk;
+      const T best = mesh_hit(K, last, sx, sy, sz, dx, dy, dz, rem, bk);
+      if (bk < 0) break;
+      if (nh == 1024) {
+        capped = true;
+        break;
+      }
+      sx = fmaT(best, dx, sx);
+      sy = fmaT(best, dy, sy);
+      sz = fmaT(best, dz, sz);
+      rem = rem - best;
+      const auto &r = K.tri[bk];
+      const T t = T(-2) * fmaT(dx, r.n[0], fmaT(dy, r.n[1], dz * r.n[2]));
+      dx = fmaT(t, r.n[0], dx);
+      dy = fmaT(t, r.n[1], dy);
+      dz = fmaT(t, r.n[2], dz);
+      last = bk;
+      ++nh;
+    }
+    if (capped) {
+      x = sx;
+      y = sy;
+      z = sz;
+    } else {
+      x = fmaT(rem, dx, sx);
+      y = fmaT(rem, dy, sy);
+      z = fmaT(rem, dz, sz);
+    }
+    out.caps += capped ? 1 : 0;
+    const V3 pp{(double)x, (double)y, (double)z};
+    for (int j = 0; j < nseq; ++j) out.phase[j] += gamma * dot(gfunc(seqs[j], dt * i), pp) * dt;
+    if (tr) {
+      const size_t o = (size_t)(i - 1);
+      tr->pos[o * 3 + 0] = (double)x;
+      tr->pos[o * 3 + 1] = (double)y;
+      tr->pos[o * 3 + 2] = (double)z;
+      tr->region[o] = 0;
+      tr->hits[o] = nh;
+      tr->words[o] = (int32_t)st.word;
+    }
+  }
+  escaped = ok && mesh_side(K, x, y, z) == 0;
+}
+
 extern "C" {
 
 void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
@@ -1350,6 +1663,81 @@ int orc_wc(const orc_basis *pore, int64_t n, int steps, double timestep, double 
   }
   if (sum_cos) *sum_cos = sc;
   if (sum_sin) *sum_sin = ss;
+  return 0;
+}
+
+int orc_mesh_walk(const double *vertices, int nvert, const int32_t *triangles, int ntri, double D,
+                  const orc_sequence *seqs, int nseq, const orc_params *p, int mode, int nthreads,
+                  double *sums, orc_trace *trace, int64_t *escaped) {
+  if (!vertices || !triangles || nvert < 4 || ntri < 4 || !p || p->num_walkers < 1 ||
+      p->steps < 1 || !(p->timestep > 0.0) || !(D > 0.0) || (nseq > 0 && (!seqs || !sums)))
+    return -1;
+  if (mode != ORC_KERN64 && mode != ORC_KERN32) return -1;
+  KMesh<double> K64;
+  KMesh<float> K32;
+  if ((mode == ORC_KERN64 ? mesh_build(vertices, nvert, triangles, ntri, K64)
+                          : mesh_build(vertices, nvert, triangles, ntri, K32)) != 0)
+    return -1;
+  double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300}, cmax = 0.0;
+  for (int t = 0; t < ntri; ++t)
+    for (int j = 0; j < 3; ++j)
+      for (int k = 0; k < 3; ++k) {
+        const double c = vertices[3 * triangles[3 * t + j] + k];
+        lo[k] = std::min(lo[k], c);
+        hi[k] = std::max(hi[k], c);
+      }
+  for (int k = 0; k < 3; ++k) cmax = std::max(cmax, std::max(std::fabs(lo[k]), std::fabs(hi[k])));
+  K64.slack = 4e-6 * cmax;
+  K32.slack = (float)(4e-6 * cmax);
+  const double gamma = p->gamma > 0.0 ? p->gamma : kGAMMA;
+  const int64_t N = p->num_walkers;
+  if (nthreads < 1) nthreads = 1;
+  if ((int64_t)nthreads > N) nthreads = (int)N;
+  std::vector<std::vector<double>> part(nthreads, std::vector<double>((size_t)nseq * 5, 0.0));
+  std::vector<int64_t> esc(nthreads, 0);
+  auto work = [&](int t) {
+    WalkOut out;
+    out.phase.assign(nseq, 0.0);
+    for (int64_t w = N * t / nthreads; w < N * (t + 1) / nthreads; ++w) {
+      TraceRow row, *tr = nullptr;
+      if (trace && w < trace->ntrace) {
+        const size_t o = (size_t)w * (size_t)(p->steps - 1);
+        row = {trace->init_pos + w * 3, trace->pos + o * 3, trace->region + o, trace->hits + o,
+               trace->words + o};
+        tr = &row;
+      }
+      bool e = false;
+      if (mode == ORC_KERN64) mesh_walk_one(K64, D, seqs, nseq, *p, gamma, w, out, tr, e);
+      else mesh_walk_one(K32, D, seqs, nseq, *p, gamma, w, out, tr, e);
+      esc[t] += e ? 1 : 0;
+      for (int j = 0; j < nseq; ++j) {
+        const double xv = std::cos(out.phase[j]), yv = std::sin(out.phase[j]);
+        double *s = &part[t][(size_t)j * 5];
+        s[0] += xv;
+        s[1] += yv;
+        s[2] += xv * xv;
+        s[3] += yv * yv;
+        s[4] += xv * yv;
+      }
+    }
+  };
+  if (nthreads == 1) {
+    work(0);
+  } else {
+    std::vector<std::thread> th;
+    for (int t = 0; t < nthreads; ++t) th.emplace_back(work, t);
+    for (auto &x : th) x.join();
+  }
+  for (int j = 0; j < nseq * 5; ++j) {
+    double s = 0.0;
+    for (int t = 0; t < nthreads; ++t) s += part[t][j];
+    sums[j] = s;
+  }
+  if (escaped) {
+    int64_t c = 0;
+    for (auto v : esc) c += v;
+    *escaped = c;
+  }
   return 0;
 }
 

@@ -78,6 +78,14 @@ void orc_stream_words(uint64_t seed, uint64_t walker, int n, uint32_t *out);
 /* sin and cos of 2*pi*u by the kernel's FP32 polynomial (for host checks). */
 void orc_sincos_2pi_f32(float u, float *s, float *c);
 
+/* A closed triangle mesh as a single pore (GPU walker formulation, see
+ * oracle.cpp): vertices[nvert][3], triangles[ntri][3]; mode ORC_KERN64 or
+ * ORC_KERN32; sums as orc_walk; escaped = walkers outside the mesh after
+ * their walk. */
+int orc_mesh_walk(const double *vertices, int nvert, const int32_t *triangles, int ntri, double D,
+                  const orc_sequence *seqs, int nseq, const orc_params *p, int mode, int nthreads,
+                  double *sums, orc_trace *trace, int64_t *escaped);
+
 /* Signal sums of a lattice walk (lat != NULL) or a single-pore walk
  * (lat == NULL, walkers start in basis[0]).  sums[5*j..5*j+4] =
  * (sum x, sum y, sum x^2, sum y^2, sum xy) for sequence j.  With flag 64

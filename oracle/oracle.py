@@ -136,6 +136,27 @@ def walk(lat, bases, seqs, params, mode=REF64, nthreads=1, ntrace=0):
             _shape_trace(bufs, ntrace, params.steps) if ntrace else None, caps.value)
 
 
+def mesh_walk(vertices, triangles, D, seqs, params, mode=KERN32, nthreads=1, ntrace=0):
+    """The mesh-pore walk (GPU formulation, FP64 or FP32).  Returns
+    (sums[M,5], trace|None, escaped)."""
+    L = lib()
+    v = np.ascontiguousarray(vertices, np.float64)
+    t = np.ascontiguousarray(triangles, np.int32)
+    s = _arr(seqs, Sequence)
+    sums = np.zeros(max(len(seqs), 1) * 5)
+    tr, bufs = (make_trace(ntrace, params.steps) if ntrace else (None, None))
+    esc = C.c_int64(0)
+    rc = L.orc_mesh_walk(v.ctypes.data_as(C.POINTER(C.c_double)), len(v),
+                         t.ctypes.data_as(C.POINTER(C.c_int32)), len(t), C.c_double(D), s, len(seqs),
+                         C.byref(params), mode, nthreads,
+                         sums.ctypes.data_as(C.POINTER(C.c_double)),
+                         C.byref(tr) if tr is not None else None, C.byref(esc))
+    if rc != 0:
+        raise ValueError("orc_mesh_walk failed: %d" % rc)
+    return (sums[: len(seqs) * 5].reshape(len(seqs), 5),
+            _shape_trace(bufs, ntrace, params.steps) if ntrace else None, esc.value)
+
+
 def ref_walk(variant, lat, bases, seqs, params, nthreads=1, ntrace=0):
     """Runs the reference's own walker (compiled here); None if unavailable."""
     R = reflib()
