@@ -219,7 +219,7 @@ def main(argv=None):
     import json
     ap = argparse.ArgumentParser(description="time one seeded workload on the GPU")
     ap.add_argument("workload", choices=["free_box", "one_cylinder", "gamma_pack", "mag_lowfield",
-                                         "wc_sphere"])
+                                         "wc_sphere", "mesh_sphere"])
     ap.add_argument("--steps", type=int, default=0, help="cut every walk to this many steps")
     ap.add_argument("--walkers", type=int, default=0)
     ap.add_argument("--reps", type=int, default=3)
@@ -230,6 +230,8 @@ def main(argv=None):
         print(json.dumps(measure_mag(a.walkers, a.steps, a.reps, a.cpu_sample)))
     elif a.workload == "wc_sphere":
         print(json.dumps(measure_wc(a.walkers or 32768, a.steps or 22000, a.reps)))
+    elif a.workload == "mesh_sphere":
+        print(json.dumps(measure_mesh(a.walkers or (1 << 20), a.steps or 6001, a.reps)))
     else:
         print(json.dumps(measure(a.workload, a.steps, a.walkers, a.reps)))
 
@@ -312,6 +314,29 @@ def measure_wc(walkers: int = 32768, steps: int = 22000, reps: int = 3, device=N
     return {"workload": "wc_sphere", "walkers": walkers, "steps": steps,
             "wc_walker_steps_per_s": walkers * steps / t_wc, "wc_seconds": t_wc,
             "specular_walker_steps_per_s": walkers * (steps - 1) / t_sp, "specular_seconds": t_sp}
+
+
+def measure_mesh(walkers: int = 1 << 20, steps: int = 6001, reps: int = 3, device=None) -> dict:
+    """A 5 um sphere as a 5,120-triangle icosphere mesh (axx_run_mesh) against
+    the analytic sphere pore (axx_run_single): D 2 um^2/ms, dt 2 us, PGSE 16
+    G values (delta 2, Delta 10 ms)."""
+    from .acquisition import RectGrad, Sphere, run_single
+    from .mesh import icosphere, run_mesh
+    mesh = icosphere(5 * UM, 4, 2 * D1)
+    seqs = [RectGrad(g * MTM, 2.0, 8.0) for g in np.linspace(0, 300, 16)]
+    run_mesh(mesh, seqs, walkers, steps, 0.002, 7, device=device)
+    t_m = min(_timed(lambda: run_mesh(mesh, seqs, walkers, steps, 0.002, 7, device=device))
+              for _ in range(reps))
+    r = run_mesh(mesh, seqs, walkers, steps, 0.002, 7, device=device)
+    pore = Sphere(0.0, 0.0, 0.0, 5 * UM, 0.0, 0.0, 2 * D1, 1, 0.0)
+    run_single(pore, seqs, walkers, steps, 0.002, 7, device=device)
+    t_s = min(_timed(lambda: run_single(pore, seqs, walkers, steps, 0.002, 7, device=device))
+              for _ in range(reps))
+    return {"workload": "mesh_sphere", "triangles": len(mesh.triangles), "walkers": walkers,
+            "steps": steps, "mesh_walker_steps_per_s": walkers * (steps - 1) / t_m,
+            "mesh_seconds": t_m, "escaped": r.escaped,
+            "hits_per_move": r.hits / r.walker_steps,
+            "sphere_walker_steps_per_s": walkers * (steps - 1) / t_s}
 
 
 def _timed(fn):

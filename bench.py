@@ -508,6 +508,7 @@ def main():
         # host-timed calls through the C ABI (tables uploaded per call)
         line["mag"] = W.measure_mag(reps=3, device=dev)
         line["wc"] = W.measure_wc(reps=3, device=dev)
+        line["mesh"] = W.measure_mesh(reps=3, device=dev)
     if not args.no_surrogate:
         line["surrogate"] = surrogate_section(A, N, L, dev)
     if not args.no_cpu_baseline:
