@@ -208,7 +208,9 @@ __device__ __forceinline__ float mesh_hit(const MeshArgs &Q, uint32_t b, uint32_
     const float dn = fma_f(n.x, dx, fma_f(n.y, dy, n.z * dz));
     if (!(dn > 0.0f)) continue;  // only crossings from inside to outside
     const float np = fma_f(n.x, px, fma_f(n.y, py, n.z * pz));
-    if (!(n.w - np > -Q.slack)) continue;  // not beyond the face's plane
+    const float dist = n.w - np;
+    if (!(dist > -Q.slack)) continue;        // not beyond the face's plane
+    if (!(dist < rem * dn)) continue;        // the plane lies beyond the path
     const float s = watertight_hit(M, px, py, pz, __ldg(&Q.tri[4 * k]),
                                    __ldg(&Q.tri[4 * k + 1]), __ldg(&Q.tri[4 * k + 2]));
     if (s < rem && s < best) {

@@ -1288,7 +1288,9 @@ T mesh_hit(const KMesh<T> &K, int last, T px, T py, T pz, T dx, T dy, T dz, T re
     const T dn = fmaT(r.n[0], dx, fmaT(r.n[1], dy, r.n[2] * dz));
     if (!(dn > T(0))) continue;  // crossings from inside to outside only
     const T np = fmaT(r.n[0], px, fmaT(r.n[1], py, r.n[2] * pz));
-    if (!(r.w - np > -K.slack)) continue;
+    const T dist = r.w - np;
+    if (!(dist > -K.slack)) continue;
+    if (!(dist < rem * dn)) continue;  // the plane lies beyond the path
     const T s = k_watertight(M, px, py, pz, r.v);
     if (s < rem && s < best) {
       best = s;
