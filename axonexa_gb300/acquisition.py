@@ -606,6 +606,12 @@ class phaseAcquisition:
     def getADC(self):
         return self.ADC
 
+    def getADCMeanSquare(self):
+        return self.ADCmeansquare
+
+    def getPoints(self):
+        return self.points
+
     def getADCError(self):
         return math.sqrt(max(self.ADCmeansquare - self.ADC * self.ADC, 0.0))
 
@@ -670,6 +676,12 @@ class phaseAcquisitionStream:
                              plan=None, numOfSMPerDevice=None, **kw):
         for i in range(len(self.acqSet)):
             self.runAcquisition(i, basis, timestep, **kw)
+
+    def addMagnetizationSet(self, host_mx, host_my):
+        """Stores per-acquisition sums (phaseAcquisitionStream.cuh:615-621)."""
+        for i, a in enumerate(self.acqSet):
+            a.mx = [float(v) for v in host_mx[i]]
+            a.my = [float(v) for v in host_my[i]]
 
     def changeSeeds(self, seed):
         for i, a in enumerate(self.acqSet):
