@@ -138,6 +138,27 @@ def test_init_modes_bit_exact(dev, orc):
         np.testing.assert_array_equal(g["words"], o["words"])
 
 
+def test_walker_ids_beyond_32_bits(dev, orc):
+    """Walker ids above 2^32 (a shard of a very large job): the stream key
+    uses the id's high word; traces and sums match the FP32 mirror."""
+    import axonexa_gb300 as A
+    lat, bases = cases.one_cylinder()
+    L, B, S = to_product(lat, bases, cases.seq_mix()[:3])
+    off = (1 << 33) + 12345
+    g = A.trace_lattice(L, B, 64, 800, 0.002, 9, relaxation=True, walker_offset=off, device=dev)
+    p = cases.params(64, 800, 9, flags=1, offset=off)
+    _, o, _ = orc.walk(lat, bases, [], p, orc.KERN32, ntrace=64)
+    np.testing.assert_array_equal(g["init_pos"].astype(np.float64), o["init_pos"])
+    np.testing.assert_array_equal(g["pos"].astype(np.float64), o["pos"])
+    np.testing.assert_array_equal(g["words"], o["words"])
+    r = A.run_lattice(L, B, S, 4096, 800, 0.002, 9, relaxation=True, walker_offset=off,
+                      device=dev)
+    k32, _, _ = orc.walk(lat, bases, cases.seq_mix()[:3], cases.params(4096, 800, 9, flags=1,
+                                                                       offset=off),
+                         orc.KERN32, nthreads=8)
+    assert np.all(np.abs(r.mx - k32[:, 0]) <= 2e-5 * 4096)
+
+
 def _tie(orc, lat, bases, p, w, i, start, word, want_region, want_hits):
     """True if some FP32-size nudge of the start makes the FP64 reference move
     reproduce the GPU's events (the move sits on a rounding tie)."""
