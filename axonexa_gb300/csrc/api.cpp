@@ -84,23 +84,28 @@ axx_status check_params(axx_ctx *ctx, const axx_run_params *p) {
 axx_status build_plan(axx_ctx *ctx, const GeomPlan &g, const SeqPlan &sq, int M,
                       const axx_run_params *p, int mode, const axx_basis *basis, int nbasis,
                       const double cell[3], axx_plan **out) {
+  if ((p->flags & AXX_FLAG_COMPARTMENTS) && mode != AXX_MODE_LATTICE)
+    return fail(ctx, AXX_ERR_INVALID_ARG, "compartment sums exist for lattice walks only");
+  const int Mo = (p->flags & AXX_FLAG_COMPARTMENTS) ? 2 * M : M;
+  // tables that do not fit the shared-memory budget are read from global
+  // memory (instantiations with 16 channels); only the per-warp sums stay in
+  // shared memory
+  const bool global_tables = walk_smem_bytes(g, Mo) > AXX_SMEM_MAX;
   KernelTables kt;
-  std::string err = make_kernel_tables(g, sq, M, p->steps, mode, p->flags, kt);
+  std::string err =
+      make_kernel_tables(g, sq, M, p->steps, mode, p->flags, kt, global_tables ? AXX_KMAX : 1);
   if (!err.empty()) return fail(ctx, AXX_ERR_UNSUPPORTED, err);
   InitSpec init;
   err = init_spec(g, basis, nbasis, mode, p, init);
   if (!err.empty()) return fail(ctx, AXX_ERR_INVALID_ARG, err);
-  if ((p->flags & AXX_FLAG_COMPARTMENTS) && mode != AXX_MODE_LATTICE)
-    return fail(ctx, AXX_ERR_INVALID_ARG, "compartment sums exist for lattice walks only");
-  const int Mo = (p->flags & AXX_FLAG_COMPARTMENTS) ? 2 * M : M;
-  const size_t smem = walk_smem_bytes(g, Mo);
+  const size_t smem = global_tables ? walk_sums_bytes(Mo) : walk_smem_bytes(g, Mo);
   if (smem > AXX_SMEM_MAX)
     return fail(ctx, AXX_ERR_UNSUPPORTED,
-                "substrate tables and sequence sums exceed the shared-memory budget (" +
-                    std::to_string(smem) + " bytes)");
+                "the sequence sums exceed the shared-memory budget (" + std::to_string(smem) +
+                    " bytes)");
   // one instance, one cell, no compartment sums: the single-instance kernels
   const bool one = g.geo.size() == 1 && g.cstart.size() == 2 && !(p->flags & AXX_FLAG_COMPARTMENTS);
-  const int occ = occupancy_walk(g.geom, kt.km, kt.kmax, false, one, smem);
+  const int occ = occupancy_walk(g.geom, kt.km, kt.kmax, false, one, global_tables, smem);
   if (occ <= 0) return fail(ctx, AXX_ERR_CUDA, "walk kernel cannot be resident (occupancy 0)");
   auto *pl = new axx_plan();
   pl->ctx = ctx;
@@ -132,6 +137,7 @@ axx_status build_plan(axx_ctx *ctx, const GeomPlan &g, const SeqPlan &sq, int M,
     return cuda_fail(ctx, e, "uploading the plan tables");
   }
   fill_walk_params(pl->P, base, L, g, kt, p, mode, M, init, cell, ctx->abort_dev);
+  pl->P.global_tables = global_tables ? 1 : 0;
   pl->out = (double *)(base + L.o_out);
   pl->counters = pl->P.counters;
   pl->walker_steps = p->num_walkers * (long long)(p->steps - 1);

@@ -80,6 +80,7 @@ struct WalkParams {
   float ch_p[AXX_KMAX][3];    // channel projections (0 for padded channels)
   int M;
   int compart;                // also sums over walkers starting in a basis: rows M..2M-1
+  int global_tables;          // substrate tables read from global memory (too big to stage)
   const double *coef;         // [M][kmax]
   double *partials;
   unsigned long long *counters;

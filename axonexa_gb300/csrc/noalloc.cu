@@ -105,19 +105,23 @@ extern "C" axx_status axx_run_lattice_noalloc(axx_ctx *ctx, const axx_lattice *l
   err = plan_sequences(seqs, nseq, p->steps, p->timestep, gamma, sq);
   if (!err.empty()) return fail(ctx, AXX_ERR_INVALID_ARG, err);
   const int M = nseq;
+  const int Mo = (p->flags & AXX_FLAG_COMPARTMENTS) ? 2 * M : M;  // rows of sums
+  // tables beyond the shared-memory budget stay in global memory (16-channel
+  // instantiations)
+  const bool global_tables = walk_smem_bytes(g, Mo) > AXX_SMEM_MAX;
   KernelTables kt;
-  err = make_kernel_tables(g, sq, M, p->steps, AXX_MODE_LATTICE, p->flags, kt);
+  err = make_kernel_tables(g, sq, M, p->steps, AXX_MODE_LATTICE, p->flags, kt,
+                           global_tables ? AXX_KMAX : 1);
   if (!err.empty()) return fail(ctx, AXX_ERR_UNSUPPORTED, err);
   InitSpec init;
   err = init_spec(g, basis, nbasis, AXX_MODE_LATTICE, p, init);
   if (!err.empty()) return fail(ctx, AXX_ERR_INVALID_ARG, err);
-  const int Mo = (p->flags & AXX_FLAG_COMPARTMENTS) ? 2 * M : M;  // rows of sums
-  const size_t smem = walk_smem_bytes(g, Mo);
+  const size_t smem = global_tables ? walk_sums_bytes(Mo) : walk_smem_bytes(g, Mo);
   if (smem > AXX_SMEM_MAX)
-    return fail(ctx, AXX_ERR_UNSUPPORTED, "substrate tables exceed the shared-memory budget");
+    return fail(ctx, AXX_ERR_UNSUPPORTED, "the sequence sums exceed the shared-memory budget");
   // one instance, one cell, no compartment sums: the single-instance kernels
   const bool one = g.geo.size() == 1 && g.cstart.size() == 2 && !(p->flags & AXX_FLAG_COMPARTMENTS);
-  const int occ = occupancy_walk(g.geom, kt.km, kt.kmax, false, one, smem);
+  const int occ = occupancy_walk(g.geom, kt.km, kt.kmax, false, one, global_tables, smem);
   if (occ <= 0) return fail(ctx, AXX_ERR_CUDA, "walk kernel cannot be resident");
   const long long ntask = (p->num_walkers + 31) / 32;
   const long long want = (ntask + AXX_BLOCK / 32 - 1) / (AXX_BLOCK / 32);
@@ -145,6 +149,7 @@ extern "C" axx_status axx_run_lattice_noalloc(axx_ctx *ctx, const axx_lattice *l
   WalkParams P;
   const double cell[3] = {lat->a, lat->b, lat->c};
   fill_walk_params(P, base, Lo, g, kt, p, AXX_MODE_LATTICE, M, init, cell, ctx->abort_dev);
+  P.global_tables = global_tables ? 1 : 0;
   *ctx->abort_host = 0;
   TraceParams T{};
   e = launch_walk(g.geom, kt.km, kt.kmax, false, P, T, (int)grid, smem, s);

@@ -38,6 +38,8 @@ std::string make_kernel_tables(const GeomPlan &g, const SeqPlan &sq, int M, int 
   return "";
 }
 
+size_t walk_sums_bytes(int M) { return (size_t)(AXX_BLOCK / 32) * M * 5 * sizeof(double); }
+
 size_t walk_smem_bytes(const GeomPlan &g, int M) {
   const size_t wsum = (size_t)(AXX_BLOCK / 32) * M * 5 * sizeof(double);  // 160 M, 16-aligned
   const size_t ninst = g.geo.size(), nslot = g.slot_tab.size();

@@ -39,6 +39,8 @@ std::string make_kernel_tables(const GeomPlan &g, const SeqPlan &sq, int M, int 
                                uint32_t flags, KernelTables &kt, int min_kmax = 1);
 // Dynamic shared memory of the walk kernel (per-warp sums + staged tables).
 size_t walk_smem_bytes(const GeomPlan &g, int M);
+// The per-warp sums alone (substrates whose tables stay in global memory).
+size_t walk_sums_bytes(int M);
 ArenaLayout arena_layout(const GeomPlan &g, const KernelTables &kt, int M);
 cudaError_t upload_tables(char *base, const ArenaLayout &L, const GeomPlan &g,
                           const KernelTables &kt, cudaStream_t s);

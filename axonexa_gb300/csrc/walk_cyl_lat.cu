@@ -3,21 +3,21 @@
 
 namespace axx {
 
-cudaError_t launch_walk_cyl_lat(int km, int kmax, bool trace, bool one, const WalkParams &P,
+cudaError_t launch_walk_cyl_lat(int km, int kmax, bool trace, bool one, bool gt, const WalkParams &P,
                            const TraceParams &T, int grid, size_t smem, cudaStream_t s) {
   switch (km) {
-    case 0: return walk_launch_km<AXX_GEOM_CYL, 0>(kmax, trace, one, P, T, grid, smem, s);
-    case 1: return walk_launch_km<AXX_GEOM_CYL, 1>(kmax, trace, one, P, T, grid, smem, s);
-    case 2: return walk_launch_km<AXX_GEOM_CYL, 2>(kmax, trace, one, P, T, grid, smem, s);
+    case 0: return walk_launch_km<AXX_GEOM_CYL, 0>(kmax, trace, one, gt, P, T, grid, smem, s);
+    case 1: return walk_launch_km<AXX_GEOM_CYL, 1>(kmax, trace, one, gt, P, T, grid, smem, s);
+    case 2: return walk_launch_km<AXX_GEOM_CYL, 2>(kmax, trace, one, gt, P, T, grid, smem, s);
   }
   return cudaErrorInvalidValue;
 }
 
-int occupancy_walk_cyl_lat(int km, int kmax, bool trace, bool one, size_t smem) {
+int occupancy_walk_cyl_lat(int km, int kmax, bool trace, bool one, bool gt, size_t smem) {
   switch (km) {
-    case 0: return walk_occ_km<AXX_GEOM_CYL, 0>(kmax, trace, one, smem);
-    case 1: return walk_occ_km<AXX_GEOM_CYL, 1>(kmax, trace, one, smem);
-    case 2: return walk_occ_km<AXX_GEOM_CYL, 2>(kmax, trace, one, smem);
+    case 0: return walk_occ_km<AXX_GEOM_CYL, 0>(kmax, trace, one, gt, smem);
+    case 1: return walk_occ_km<AXX_GEOM_CYL, 1>(kmax, trace, one, gt, smem);
+    case 2: return walk_occ_km<AXX_GEOM_CYL, 2>(kmax, trace, one, gt, smem);
   }
   return 0;
 }

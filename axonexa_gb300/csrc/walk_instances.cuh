@@ -7,10 +7,10 @@
 
 namespace axx {
 
-template <int GEOM, int KMAX, int KM, bool TRACE, bool ONE = false>
+template <int GEOM, int KMAX, int KM, bool TRACE, bool ONE = false, bool GT = false>
 static cudaError_t walk_go(const WalkParams &P, const TraceParams &T, int grid, size_t smem,
                            cudaStream_t s) {
-  auto fn = walk_kernel<GEOM, KMAX, KM, TRACE, ONE>;
+  auto fn = walk_kernel<GEOM, KMAX, KM, TRACE, ONE, GT>;
   if (smem > 48 * 1024) {
     const cudaError_t e =
         cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -20,9 +20,9 @@ static cudaError_t walk_go(const WalkParams &P, const TraceParams &T, int grid, 
   return cudaGetLastError();
 }
 
-template <int GEOM, int KMAX, int KM, bool TRACE, bool ONE = false>
+template <int GEOM, int KMAX, int KM, bool TRACE, bool ONE = false, bool GT = false>
 static int walk_occ(size_t smem) {
-  auto fn = walk_kernel<GEOM, KMAX, KM, TRACE, ONE>;
+  auto fn = walk_kernel<GEOM, KMAX, KM, TRACE, ONE, GT>;
   if (smem > 48 * 1024 &&
       cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
           cudaSuccess)
@@ -42,11 +42,21 @@ constexpr bool walk_one_variant(int kmax, bool trace, bool one) {
          (one && !trace && kmax <= 4 && (GEOM == AXX_GEOM_CYL || GEOM == AXX_GEOM_SPH));
 }
 
+// gt: the plan keeps its tables in global memory; those instantiations exist
+// for lattice walks with 16 channels (the host pads the channels) and traces.
 template <int GEOM, int KM>
-static cudaError_t walk_launch_km(int kmax, bool trace, bool one, const WalkParams &P,
+static cudaError_t walk_launch_km(int kmax, bool trace, bool one, bool gt, const WalkParams &P,
                                   const TraceParams &T, int grid, size_t smem, cudaStream_t s) {
   constexpr bool single = KM >= AXX_KM_SINGLE;
   constexpr bool lat1 = !single && (GEOM == AXX_GEOM_CYL || GEOM == AXX_GEOM_SPH);
+  constexpr bool gt_ok = !single && GEOM != AXX_GEOM_FREE;
+  if constexpr (gt_ok) {
+    if (gt) {
+      if (trace) return walk_go<GEOM, 1, KM, true, false, true>(P, T, grid, smem, s);
+      if (kmax == 16) return walk_go<GEOM, 16, KM, false, false, true>(P, T, grid, smem, s);
+      return cudaErrorInvalidValue;
+    }
+  }
   if constexpr (single) {
     if (trace) return walk_go<GEOM, 1, KM, true, single>(P, T, grid, smem, s);
     switch (kmax) {
@@ -78,9 +88,17 @@ static cudaError_t walk_launch_km(int kmax, bool trace, bool one, const WalkPara
 }
 
 template <int GEOM, int KM>
-static int walk_occ_km(int kmax, bool trace, bool one, size_t smem) {
+static int walk_occ_km(int kmax, bool trace, bool one, bool gt, size_t smem) {
   constexpr bool single = KM >= AXX_KM_SINGLE;
   constexpr bool lat1 = !single && (GEOM == AXX_GEOM_CYL || GEOM == AXX_GEOM_SPH);
+  constexpr bool gt_ok = !single && GEOM != AXX_GEOM_FREE;
+  if constexpr (gt_ok) {
+    if (gt) {
+      if (trace) return walk_occ<GEOM, 1, KM, true, false, true>(smem);
+      if (kmax == 16) return walk_occ<GEOM, 16, KM, false, false, true>(smem);
+      return 0;
+    }
+  }
   if constexpr (single) {
     if (trace) return walk_occ<GEOM, 1, KM, true, single>(smem);
     switch (kmax) {

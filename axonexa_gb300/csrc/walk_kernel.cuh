@@ -795,7 +795,10 @@ __device__ __forceinline__ double warp_sum(double v) {
 // ONEONLY: compiled for substrates of a single instance only (the host checks
 // n_inst == 1 and ncell == 1); the list path is left out, which frees
 // registers for one more resident block per SM.
-template <int GEOM, int KMAX, int KM, bool TRACE, bool ONEONLY = false>
+// GT: the substrate tables stay in global memory (too large to stage in
+// shared memory); a compile-time choice, so that the staged kernels keep
+// their shared-memory loads.
+template <int GEOM, int KMAX, int KM, bool TRACE, bool ONEONLY = false, bool GT = false>
 __global__ void __launch_bounds__(AXX_BLOCK, ONEONLY && KMAX <= 4 ? AXX_MIN_BLOCKS + 1
                                                                  : AXX_MIN_BLOCKS_FOR(KMAX))
     walk_kernel(const __grid_constant__ WalkParams P, const __grid_constant__ TraceParams T) {
@@ -809,31 +812,42 @@ __global__ void __launch_bounds__(AXX_BLOCK, ONEONLY && KMAX <= 4 ? AXX_MIN_BLOC
   const int Mo = (!ONEONLY && P.compart) ? 2 * M : M;
   for (int j = threadIdx.x; j < warps * Mo * 5; j += blockDim.x) wsum[j] = 0.0;
 
-  // stage the substrate tables (layout fixed by the host planner)
-  float4 *sg = reinterpret_cast<float4 *>(smem + (size_t)warps * Mo * 5 * sizeof(double));
-  float4 *sa = sg + P.n_inst;
-  float4 *ss = sa + P.n_inst;
-  uint32_t *sc = reinterpret_cast<uint32_t *>(ss + P.n_slot);
-  int *sr = reinterpret_cast<int *>(sc + P.ncell + 1);
-  uint16_t *sl = reinterpret_cast<uint16_t *>(sr + P.n_slot);
-  for (int j = threadIdx.x; j < P.n_inst; j += blockDim.x) {
-    sg[j] = P.inst_geo[j];
-    sa[j] = P.inst_aux[j];
-  }
-  for (int j = threadIdx.x; j < P.n_slot; j += blockDim.x) {
-    ss[j] = P.slot_tab[j];
-    sr[j] = P.slot_region[j];
-  }
-  for (int j = threadIdx.x; j <= P.ncell; j += blockDim.x) sc[j] = P.cell_start[j];
-  for (int j = threadIdx.x; j < P.n_list; j += blockDim.x) sl[j] = P.cell_list[j];
-  __syncthreads();
   SmemView S;
-  S.geo = sg;
-  S.aux = sa;
-  S.slot = ss;
-  S.cstart = sc;
-  S.region = sr;
-  S.clist = sl;
+  if constexpr (GT) {
+    // tables beyond the shared-memory budget (thousands of bases): read in
+    // place, through L1
+    S.geo = P.inst_geo;
+    S.aux = P.inst_aux;
+    S.slot = P.slot_tab;
+    S.cstart = P.cell_start;
+    S.region = P.slot_region;
+    S.clist = P.cell_list;
+  } else {
+    // stage the substrate tables (layout fixed by the host planner)
+    float4 *sg = reinterpret_cast<float4 *>(smem + (size_t)warps * Mo * 5 * sizeof(double));
+    float4 *sa = sg + P.n_inst;
+    float4 *ss = sa + P.n_inst;
+    uint32_t *sc = reinterpret_cast<uint32_t *>(ss + P.n_slot);
+    int *sr = reinterpret_cast<int *>(sc + P.ncell + 1);
+    uint16_t *sl = reinterpret_cast<uint16_t *>(sr + P.n_slot);
+    for (int j = threadIdx.x; j < P.n_inst; j += blockDim.x) {
+      sg[j] = P.inst_geo[j];
+      sa[j] = P.inst_aux[j];
+    }
+    for (int j = threadIdx.x; j < P.n_slot; j += blockDim.x) {
+      ss[j] = P.slot_tab[j];
+      sr[j] = P.slot_region[j];
+    }
+    for (int j = threadIdx.x; j <= P.ncell; j += blockDim.x) sc[j] = P.cell_start[j];
+    for (int j = threadIdx.x; j < P.n_list; j += blockDim.x) sl[j] = P.cell_list[j];
+    S.geo = sg;
+    S.aux = sa;
+    S.slot = ss;
+    S.cstart = sc;
+    S.region = sr;
+    S.clist = sl;
+  }
+  __syncthreads();
 
   const long long ntask = (P.n_walkers + 31) / 32;
   const long long gwarp = (long long)blockIdx.x * warps + wib;

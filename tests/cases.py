@@ -41,6 +41,15 @@ def sphere_lattice(a_um=10.0, r_um=3.0):
                  for k, (x, y, z) in enumerate(pts)]
 
 
+def cylinder_grid(n=60, spacing_um=1.0, r_um=0.35, kappa=2e-5):
+    """n x n permeable cylinders on a square grid in one periodic cell: more
+    bases than the walk kernel stages in shared memory (3,600 at n = 60)."""
+    s = spacing_um * UM
+    lat = O.Lattice(n * s, n * s, n * s, 60.0, 0.0, D2)
+    return lat, [O.Basis(0, k + 1, (k % n + 0.5) * s, (k // n + 0.5) * s, 0.0, r_um * UM, 1.5e-6,
+                         80.0, 0.0, kappa, 1e-14) for k in range(n * n)]
+
+
 def parallel_plates(l_um=8.0, D=D2, with_cylinder=False):
     """Walls at x = 0 and x = l of an l-wide cubic cell, normals pointing
     into the cell, as the reference's planePhase example sets them up

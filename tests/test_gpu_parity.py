@@ -138,6 +138,26 @@ def test_init_modes_bit_exact(dev, orc):
         np.testing.assert_array_equal(g["words"], o["words"])
 
 
+def test_substrate_beyond_shared_memory(dev, orc):
+    """3,600 bases: the tables stay in global memory; the traces still match
+    the FP32 mirror bit for bit (the mirror scans every instance, so the
+    check stays small)."""
+    import axonexa_gb300 as A
+    lat, bases = cases.cylinder_grid()
+    seqs = cases.seq_mix()[:3]
+    L, B, S = to_product(lat, bases, seqs)
+    g = A.trace_lattice(L, B, 32, 300, 0.001, 21, relaxation=True, permeable=True, device=dev)
+    p = cases.params(32, 300, 21, dt=0.001, flags=3)
+    _, o, _ = orc.walk(lat, bases, [], p, orc.KERN32, ntrace=32, nthreads=8)
+    for k in ("region", "hits", "words"):
+        np.testing.assert_array_equal(g[k], o[k], err_msg=k)
+    np.testing.assert_array_equal(g["pos"].astype(np.float64), o["pos"])
+    assert o["hits"].sum() > 0
+    r = A.run_lattice(L, B, S, 1 << 16, 2000, 0.001, 21, relaxation=True, permeable=True,
+                      device=dev)
+    assert r.cap_hits == 0 and np.all(np.isfinite(r.signal)) and r.signal[0] > 0.5
+
+
 def test_walker_ids_beyond_32_bits(dev, orc):
     """Walker ids above 2^32 (a shard of a very large job): the stream key
     uses the id's high word; traces and sums match the FP32 mirror."""
