@@ -350,6 +350,10 @@ __device__ __forceinline__ MoveOut boundary(const WalkParams &P, const Cands<GEO
   // ONE: the quadratic of the first pass (no instance hit yet, segment L),
   // reused by the nearest-hit loop's first pass
   float bh1 = 0.0f, c01 = 0.0f, c11 = 0.0f;
+  // lists: bit j set when the list's j-th candidate may meet the segment
+  // (candidates past the 32nd are always tested); the first pass skips the
+  // others, whose test would reject them the same way
+  uint32_t mmask = 0u;
   {
     const float aa_c = fma_f(dx, dx, dy * dy);
     const float aa_s = fma_f(dx, dx, fma_f(dy, dy, dz * dz));
@@ -375,7 +379,10 @@ __device__ __forceinline__ MoveOut boundary(const WalkParams &P, const Cands<GEO
     } else {
       for (uint32_t j = C.b; j < C.e; ++j) {
         const int k = C.S.clist[j];
-        maybe |= may(C.S.geo[k], C.S.aux[k]);
+        const bool m = may(C.S.geo[k], C.S.aux[k]);
+        maybe |= m;
+        const uint32_t bit = j - C.b;
+        mmask |= (m || bit >= 32u) ? (1u << (bit & 31u)) : 0u;
       }
     }
   }
@@ -412,6 +419,8 @@ __device__ __forceinline__ MoveOut boundary(const WalkParams &P, const Cands<GEO
       ba = C.a0;
     } else {
       for (uint32_t j = C.b; j < C.e; ++j) {
+        const uint32_t bit = j - C.b;
+        if (last < 0 && bit < 32u && !((mmask >> bit) & 1u)) continue;
         const int k = C.S.clist[j];
         const float4 aux = C.S.aux[k];
         const bool sph = is_sphere<GEOM>(aux);
