@@ -62,6 +62,7 @@ namespace axx {
 struct MeshArgs {
   const float4 *tri;   // [ntri][4]: v0, v1, v2 (outward winding), (n, n.v0)
   const uint32_t *c3s, *c3l;  // 3-D grid: cell starts, triangle lists
+  const float4 *c3n;          // per list entry: the triangle's (n, n.v0), read in list order
   const uint32_t *c2s, *c2l;  // 2-D grid
   float lo[3], hi[3];  // bounding box
   float inv3[3];
@@ -202,15 +203,17 @@ __device__ __forceinline__ float mesh_hit(const MeshArgs &Q, uint32_t b, uint32_
   if (b == e) return best;
   const Shear M = make_shear(dx, dy, dz);
   for (uint32_t j = b; j < e; ++j) {
-    const int k = (int)__ldg(&Q.c3l[j]);
-    if (k == last) continue;
-    const float4 n = __ldg(&Q.tri[4 * k + 3]);
+    // the normal comes with the list entry (consecutive entries share cache
+    // lines); the vertices only for candidates that pass the plane tests
+    const float4 n = __ldg(&Q.c3n[j]);
     const float dn = fma_f(n.x, dx, fma_f(n.y, dy, n.z * dz));
     if (!(dn > 0.0f)) continue;  // only crossings from inside to outside
     const float np = fma_f(n.x, px, fma_f(n.y, py, n.z * pz));
     const float dist = n.w - np;
     if (!(dist > -Q.slack)) continue;        // not beyond the face's plane
     if (!(dist < rem * dn)) continue;        // the plane lies beyond the path
+    const int k = (int)__ldg(&Q.c3l[j]);
+    if (k == last) continue;
     const float s = watertight_hit(M, px, py, pz, __ldg(&Q.tri[4 * k]),
                                    __ldg(&Q.tri[4 * k + 1]), __ldg(&Q.tri[4 * k + 2]));
     if (s < rem && s < best) {
@@ -428,6 +431,7 @@ struct MeshPlan {
   std::vector<float4> tri;
   std::vector<uint8_t> vertical;  // |n_z| tiny: no transversal crossing with a vertical line
   std::vector<uint32_t> c3s, c3l, c2s, c2l;
+  std::vector<float4> c3n;  // (n, n.v0) of each 3-D list entry
   double lo[3], hi[3];
   int g3[3], g2[2];
   float inv3[3], inv2[2];
@@ -592,6 +596,8 @@ std::string plan_mesh(const axx_mesh &m, double step, MeshPlan &o) {
     o.c3l.insert(o.c3l.end(), lists[c].begin(), lists[c].end());
     o.c3s[c + 1] = (uint32_t)o.c3l.size();
   }
+  o.c3n.resize(o.c3l.size());
+  for (size_t j = 0; j < o.c3l.size(); ++j) o.c3n[j] = o.tri[(size_t)o.c3l[j] * 4 + 3];
   // 2-D grid for the parity test (points; no dilation)
   const double h2 = std::sqrt(ext[0] * ext[1] / std::max(1, m.ntri / 4));
   for (int k = 0; k < 2; ++k) {
@@ -617,7 +623,10 @@ std::string plan_mesh(const axx_mesh &m, double step, MeshPlan &o) {
     o.c2l.insert(o.c2l.end(), l2[c].begin(), l2[c].end());
     o.c2s[c + 1] = (uint32_t)o.c2l.size();
   }
-  if (o.c3l.empty()) o.c3l.push_back(0);
+  if (o.c3l.empty()) {
+    o.c3l.push_back(0);
+    o.c3n.push_back(make_float4(0.f, 0.f, 0.f, 0.f));
+  }
   if (o.c2l.empty()) o.c2l.push_back(0);
   return "";
 }
@@ -683,6 +692,8 @@ axx_status mesh_run(axx_ctx *ctx, const axx_mesh *mesh, const axx_sequence *seqs
   off = up(off + mp.c3s.size() * 4);
   const size_t o_c3l = off;
   off = up(off + mp.c3l.size() * 4);
+  const size_t o_c3n = off;
+  off = up(off + mp.c3n.size() * 16);
   const size_t o_c2s = off;
   off = up(off + mp.c2s.size() * 4);
   const size_t o_c2l = off;
@@ -714,6 +725,7 @@ axx_status mesh_run(axx_ctx *ctx, const axx_mesh *mesh, const axx_sequence *seqs
   put(o_tri, mp.tri.data(), mp.tri.size() * 16);
   put(o_c3s, mp.c3s.data(), mp.c3s.size() * 4);
   put(o_c3l, mp.c3l.data(), mp.c3l.size() * 4);
+  put(o_c3n, mp.c3n.data(), mp.c3n.size() * 16);
   put(o_c2s, mp.c2s.data(), mp.c2s.size() * 4);
   put(o_c2l, mp.c2l.data(), mp.c2l.size() * 4);
   if (e == cudaSuccess) e = cudaMemsetAsync(base + o_esc, 0, 8, ctx->stream);
@@ -728,6 +740,7 @@ axx_status mesh_run(axx_ctx *ctx, const axx_mesh *mesh, const axx_sequence *seqs
   Q.tri = (const float4 *)(base + o_tri);
   Q.c3s = (const uint32_t *)(base + o_c3s);
   Q.c3l = (const uint32_t *)(base + o_c3l);
+  Q.c3n = (const float4 *)(base + o_c3n);
   Q.c2s = (const uint32_t *)(base + o_c2s);
   Q.c2l = (const uint32_t *)(base + o_c2l);
   for (int k = 0; k < 3; ++k) {
