@@ -166,13 +166,34 @@ def cpu_sample_baseline(n_walkers: int, threads: int, steps_frac: float = 1.0):
     pg = [O.Sequence(0, 0, g * 1e-6, 10.0, 30.0, 1, 0, 0) for g in np.linspace(0, 200, 32)]
     og = [O.Sequence(1, n, 100e-6, 20.0, 20.0, 1, 0, 0) for n in (1, 2, 4)]
     total_ws, t0 = 0, time.perf_counter()
+    sums = []
     for seqs, steps in ((pg, PGSE_STEPS), (og, OGSE_STEPS)):
         st = max(2, int(steps * steps_frac))
         p = O.Params(n_walkers, st, 0, 0, 1, SEED, DT, 0.0, 0)
-        O.walk(lat, cyl, seqs, p, O.REF64, nthreads=threads)
+        s, _, _ = O.walk(lat, cyl, seqs, p, O.REF64, nthreads=threads)
+        sums.append(s)
         total_ws += n_walkers * (st - 1)
     dt = time.perf_counter() - t0
-    return total_ws / dt, dt, total_ws
+    return total_ws / dt, dt, total_ws, sums
+
+
+def fp64_check(A, dev, n_walkers: int, ref_sums) -> dict:
+    """The GPU walk of the same first walkers (the same Philox streams)
+    against the oracle's FP64 reference-order sums: |dS| per sequence and its
+    ratio to the walk's standard error."""
+    import numpy as np
+    lat, cyl, acqs = workload_records(A)
+    worst_d, worst_r = 0.0, 0.0
+    for (seqs, steps), ref in zip(acqs, ref_sums):
+        r = A.run_lattice(lat, cyl, seqs, n_walkers, steps, DT, SEED, relaxation=True,
+                          device=dev)
+        s_ref = np.hypot(ref[:, 0], ref[:, 1]) / n_walkers
+        d = np.abs(r.signal - s_ref)
+        worst_d = max(worst_d, float(d.max()))
+        worst_r = max(worst_r, float((d / np.maximum(r.stderr, 1e-12)).max()))
+    return {"walkers": n_walkers, "sequences": sum(len(q) for q, _ in acqs),
+            "max_abs_dS": worst_d, "max_dS_over_se": worst_r,
+            "oracle": "FP64 reference-order restatement, the same streams"}
 
 
 def surrogate_section(A, N, L, dev, queries=1000000, reps=10, plain_subs=2):
@@ -322,7 +343,7 @@ def run_reference(args, world, rank):
         cpu_sample_baseline(max(threads, 64), threads, 0.01)
     vals, total_t, total_ws = [], 0.0, 0
     for _ in range(args.steps):
-        v, t, ws = cpu_sample_baseline(n, threads)
+        v, t, ws, _ = cpu_sample_baseline(n, threads)
         vals.append(v)
         total_t += t
         total_ws += ws
@@ -514,10 +535,12 @@ def main():
     if not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         n = int(os.environ.get("AXX_CPU_SAMPLE", "4096"))
-        v, t, wsamp = cpu_sample_baseline(n, threads)
+        v, t, wsamp, ref_sums = cpu_sample_baseline(n, threads)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                                 "sample": "%d walkers x full walks (%.1f s), FP64 reference-"
                                           "order oracle" % (n, t)}
+        # every signal of that sample against the FP64 walk of the same streams
+        line["fp64_check"] = fp64_check(A, dev, n, ref_sums)
     for h, _, _, _ in plans:
         L.axx_plan_destroy(h)
     print(json.dumps(line))
