@@ -44,13 +44,16 @@ __device__ __forceinline__ void mma_bf16(float (&d)[4], uint32_t a0, uint32_t a1
       : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
 }
 
+// blockIdx.z takes K range [z kc, min(K, (z+1) kc)) and writes C + z cz (a
+// split-K partial when gridDim.z > 1).  The operand tiles are read along
+// whichever index has unit stride, so that the loads coalesce.
 __global__ void __launch_bounds__(128) gemm_bf16_kernel(int M, int N, int K,
                                                         const __nv_bfloat16 *__restrict__ A,
                                                         long long sam, long long sak,
                                                         const __nv_bfloat16 *__restrict__ B,
                                                         long long sbk, long long sbn,
                                                         float *__restrict__ C, long long ldc,
-                                                        int accumulate) {
+                                                        int accumulate, int kc, long long cz) {
   __shared__ __align__(16) __nv_bfloat16 As[GT][GK + GPAD];  // [m][k]
   __shared__ __align__(16) __nv_bfloat16 Bs[GT][GK + GPAD];  // [n][k]
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -65,12 +68,16 @@ __global__ void __launch_bounds__(128) gemm_bf16_kernel(int M, int N, int K,
 #pragma unroll
       for (int r = 0; r < 4; ++r) acc[i][j][r] = 0.f;
   const __nv_bfloat16 zero = __float2bfloat16(0.f);
-  for (int k0 = 0; k0 < K; k0 += GK) {
+  const int kb = blockIdx.z * kc, ke = min(K, kb + kc);
+  C += blockIdx.z * cz;
+  const bool a_k = sak == 1, b_k = sbk == 1;  // unit stride along k
+  for (int k0 = kb; k0 < ke; k0 += GK) {
     for (int e = tid; e < GT * GK; e += 128) {
-      const int r = e / GK, k = e % GK;
-      const int gm = m0 + r, gk = k0 + k, gn = n0 + r;
-      As[r][k] = (gm < M && gk < K) ? A[gm * sam + gk * sak] : zero;
-      Bs[r][k] = (gn < N && gk < K) ? B[gk * sbk + gn * sbn] : zero;
+      const int ra = a_k ? e / GK : e % GT, ka = a_k ? e % GK : e / GT;
+      const int rb = b_k ? e / GK : e % GT, kb2 = b_k ? e % GK : e / GT;
+      const int gm = m0 + ra, gka = k0 + ka, gn = n0 + rb, gkb = k0 + kb2;
+      As[ra][ka] = (gm < M && gka < ke) ? A[gm * sam + gka * sak] : zero;
+      Bs[rb][kb2] = (gn < N && gkb < ke) ? B[gkb * sbk + gn * sbn] : zero;
     }
     __syncthreads();
 #pragma unroll
@@ -116,12 +123,38 @@ __global__ void __launch_bounds__(128) gemm_bf16_kernel(int M, int N, int K,
       }
 }
 
+// Sums the split-K partials part[z][m][n] (z ascending: a fixed order) into C.
+__global__ void splitk_sum_kernel(const float *__restrict__ part, int splits, int M, int N,
+                                  float *__restrict__ C, long long ldc) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (long long)M * N) return;
+  const int m = (int)(i / N), n = (int)(i % N);
+  float s = 0.f;
+  for (int z = 0; z < splits; ++z) s += part[(long long)z * M * N + i];
+  C[m * ldc + n] = s;
+}
+
 void gemm_bf16(cudaStream_t s, int M, int N, int K, const __nv_bfloat16 *A, long long sam,
                long long sak, const __nv_bfloat16 *B, long long sbk, long long sbn, float *C,
-               long long ldc, bool accumulate) {
+               long long ldc, bool accumulate, float *part) {
   dim3 grid((N + GT - 1) / GT, (M + GT - 1) / GT);
-  gemm_bf16_kernel<<<grid, 128, 0, s>>>(M, N, K, A, sam, sak, B, sbk, sbn, C, ldc,
-                                        accumulate ? 1 : 0);
+  // a long reduction over few output tiles (the weight gradients: K = batch)
+  // splits K across blocks into partials, summed in a fixed order after
+  const int tiles = (int)(grid.x * grid.y);
+  int splits = 1;
+  if (part && !accumulate)
+    while (splits < kMaxSplitK && tiles * splits < 256 && K / (splits * 2) >= 4 * GK) splits *= 2;
+  if (splits == 1) {
+    gemm_bf16_kernel<<<grid, 128, 0, s>>>(M, N, K, A, sam, sak, B, sbk, sbn, C, ldc,
+                                          accumulate ? 1 : 0, K, 0);
+    return;
+  }
+  const int kc = ((K + splits - 1) / splits + GK - 1) / GK * GK;
+  grid.z = splits;
+  gemm_bf16_kernel<<<grid, 128, 0, s>>>(M, N, K, A, sam, sak, B, sbk, sbn, part, N, 0, kc,
+                                        (long long)M * N);
+  splitk_sum_kernel<<<(int)(((long long)M * N + 255) / 256), 256, 0, s>>>(part, splits, M, N, C,
+                                                                          ldc);
 }
 
 // ---- elementwise kernels ----------------------------------------------------
@@ -324,7 +357,8 @@ static cudaError_t mlp_reserve(axx_mlp *m, int B) {
                oY = take((size_t)B * 4), oDy = take((size_t)B * 4), oC = take((size_t)B * W * 4),
                oZ = take((size_t)L * B * W * 4), oH = take((size_t)L * B * W * 2),
                oDH = take((size_t)B * W * 4), oDZ = take((size_t)B * W * 4),
-               oDZb = take((size_t)B * W * 2), oLoss = take(16);
+               oDZb = take((size_t)B * W * 2), oLoss = take(16),
+               oKp = take((size_t)kMaxSplitK * W * W * 4);
   cudaError_t e = cudaMalloc(&m->work, off);
   if (e != cudaSuccess) return e;
   char *b = (char *)m->work;
@@ -333,6 +367,7 @@ static cudaError_t mlp_reserve(axx_mlp *m, int B) {
   m->yb = (float *)(b + oY);
   m->dy = (float *)(b + oDy);
   m->Cb = (float *)(b + oC);
+  m->kpart = (float *)(b + oKp);
   m->Z = (float *)(b + oZ);
   m->H = (__nv_bfloat16 *)(b + oH);
   m->dH = (float *)(b + oDH);
@@ -374,7 +409,8 @@ void mlp_backward(axx_mlp *m, int B) {
     colsum_kernel<<<W, 256, 0, s>>>(m->dZ, m->grad_bias(l), B, W);
     // dW_l[n][k] = sum_b dZ[b][n] A[b][k]  (M = W rows n, N = in_true columns k, K = B)
     const __nv_bfloat16 *A = l == 0 ? m->Xb : m->H + (size_t)(l - 1) * B * W;
-    gemm_bf16(s, W, in_true, B, m->dZb, 1, W, A, in, 1, m->grad_weight(l), in_true, false);
+    gemm_bf16(s, W, in_true, B, m->dZb, 1, W, A, in, 1, m->grad_weight(l), in_true, false,
+              m->kpart);
     if (l > 0) {
       // dH_{l-1}[b][k] = sum_n dZ[b][n] W_l[n][k]
       gemm_bf16(s, B, W, W, m->dZb, W, 1, m->Wb[l], W, 1, m->dH, W, false);

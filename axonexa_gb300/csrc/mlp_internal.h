@@ -25,6 +25,7 @@ struct axx_mlp {
   __nv_bfloat16 *Xb = nullptr, *H = nullptr, *dZb = nullptr;
   float *tb = nullptr, *yb = nullptr, *dy = nullptr, *Cb = nullptr, *Z = nullptr, *dH = nullptr,
         *dZ = nullptr, *loss = nullptr;
+  float *kpart = nullptr;  // split-K partials of the weight-gradient GEMMs
   float *weight(int l) const { return params + w_off[l]; }
   float *bias(int l) const { return params + b_off[l]; }
   float *grad_weight(int l) const { return grad + w_off[l]; }
@@ -32,9 +33,11 @@ struct axx_mlp {
 };
 
 namespace axx {
+constexpr int kMaxSplitK = 16;
+// part: scratch for split-K partials (kMaxSplitK * M * N floats), or null.
 void gemm_bf16(cudaStream_t s, int M, int N, int K, const __nv_bfloat16 *A, long long sam,
                long long sak, const __nv_bfloat16 *B, long long sbk, long long sbn, float *C,
-               long long ldc, bool accumulate);
+               long long ldc, bool accumulate, float *part = nullptr);
 }  // namespace axx
 
 // tensor-core inference (mlp_tc.cu)
