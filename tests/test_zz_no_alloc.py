@@ -74,3 +74,26 @@ def test_noalloc_refuses_walks_that_do_not_fit():
         _call(N.lib().axx_run_lattice_noalloc, dev.h, lat, basis, srec, len(seqs), params)
     assert e.value.status == 1
     assert "no-allocation scratch" in str(e.value)
+
+
+def test_noalloc_compartment_sums_match_allocating_call():
+    import axonexa_gb300 as A
+    from axonexa_gb300 import _native as N
+    dev = A.default_device()
+    L = N.lib()
+    lat, basis, srec, m = _records()
+    n = 20000
+    params = N.RunParams(n, 2000, 0, 0, N.FLAG_RELAXATION | N.FLAG_COMPARTMENTS, 77, 0.002, 0.0,
+                         0)
+    res = []
+    for fn in (L.axx_run_lattice, L.axx_run_lattice_noalloc):
+        out = [np.zeros(m) for _ in range(4)]
+        ptr = [o.ctypes.data_as(C.POINTER(C.c_double)) for o in out]
+        st = N.Stats(None, None, None, 0, 0, 0, ptr[2], ptr[3], 0)
+        N.check(fn(dev.h, C.byref(lat), basis, 1, srec, m, C.byref(params), ptr[0], ptr[1],
+                   C.byref(st)), dev.h)
+        res.append((out, st.walkers_in))
+    (a, na), (b, nb) = res
+    assert na == nb and 0 < na < n
+    for x, y in zip(a, b):
+        np.testing.assert_allclose(x, y, rtol=0, atol=1e-9 * n)
