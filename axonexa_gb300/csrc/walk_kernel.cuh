@@ -567,6 +567,7 @@ __device__ __forceinline__ void do_move(const WalkParams &P, const SmemView &S,
     res.caps += o.capped ? 1u : 0u;
   }
   float px, py, pz;  // position seen by the phase
+  bool wrapped = false;
   if (single) {
     px = fx;
     py = fy;
@@ -578,9 +579,11 @@ __device__ __forceinline__ void do_move(const WalkParams &P, const SmemView &S,
     px = W.ux;
     py = W.uy;
     pz = W.uz;
+    const float ox = fx, oy = fy, oz = fz;
     fx = wrap_sel(fx, P.a);
     fy = wrap_sel(fy, P.b);
     fz = wrap_sel(fz, P.c);
+    wrapped = (fx != ox) || (fy != oy) || (fz != oz);
   }
   // phase channels: s_c(i) is wave_il[i*KMAX + c]; padded channels carry
   // zero waveforms and zero projections
@@ -608,7 +611,22 @@ __device__ __forceinline__ void do_move(const WalkParams &P, const SmemView &S,
     else
       kahan_add(W.acc[c], W.cmp[c], wv[c] * d);
   }
-  if (!single) {
+  // Behind impermeable specular walls a walker stays in its region: it is
+  // looked up again only when the move wraps across the cell edge (into
+  // another listed image, whose region id may differ), never with a single
+  // instance, whose T2 sum is then formed at the end.  (The FP32 lookup of a
+  // position a rounding error from a wall could name the other side; the
+  // FP64 reference's hardly ever does.)  Permeable and rejection walks look
+  // the region up after every move.
+  constexpr bool tracked = KM == AXX_KM_LAT_IMP;
+  if (!single && tracked && !ONE) {
+    kahan_add(W.t2s, W.t2c, s4.z);
+    if (GEOM != AXX_GEOM_FREE && wrapped) {
+      const int cell = cell_of<GEOM>(P, fx, fy, fz);
+      W.slot = lookup_list<GEOM>(S, S.cstart[cell], S.cstart[cell + 1], P.ecs_slot, fx, fy, fz);
+    }
+  }
+  if (!single && !tracked) {
     int new_slot = P.ecs_slot;
     if (GEOM != AXX_GEOM_FREE) {
       if (ONE) {
@@ -768,7 +786,11 @@ __device__ __forceinline__ WalkResult walk_one(const WalkParams &P, const SmemVi
     st.next2(P, u1, u2);
     do_move<GEOM, KMAX, KM, TRACE, ONE>(P, S, T, wid, i, u1, u2, st, W, res, g0, a0);
   }
-  if (ONE && !single) {  // the T2 sum from the move counts of the two regions
+  if (!single && KM == AXX_KM_LAT_IMP && ONE) {  // the T2 sum of the walker's one region
+    const double t = (double)(i - 1) * (double)S.slot[W.slot].z;
+    W.t2s = (float)t;
+    W.t2c = (float)((double)W.t2s - t);
+  } else if (ONE && !single) {  // the T2 sum from the move counts of the two regions
     const float tin = S.slot[aux_slot(a0)].z, tout = S.slot[P.ecs_slot].z;
     const double t = (double)W.nin * (double)tin + (double)(i - 1 - W.nin) * (double)tout;
     W.t2s = (float)t;

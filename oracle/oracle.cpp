@@ -880,6 +880,7 @@ void walk_kern(const WalkIn &in, const KGeom<T> &G, int64_t w, WalkOut &out, Tra
       out.caps += o.capped ? 1 : 0;
     }
     V3 pp;
+    bool wrapped = false;
     if (in.single) {
       pp = {(double)fx, (double)fy, (double)fz};
     } else {
@@ -887,13 +888,19 @@ void walk_kern(const WalkIn &in, const KGeom<T> &G, int64_t w, WalkOut &out, Tra
       uy = uy + (fy - y);
       uz = uz + (fz - z);
       pp = {(double)ux, (double)uy, (double)uz};
+      const T ox = fx, oy = fy, oz = fz;
       fx = k_wrap(fx, G.a);
       fy = k_wrap(fy, G.b);
       fz = k_wrap(fz, G.c);
+      wrapped = fx != ox || fy != oy || fz != oz;
     }
     for (int j = 0; j < in.nseq; ++j) out.phase[j] += in.gamma * dot(gfunc(in.seqs[j], dt * i), pp) * dt;
+    // impermeable specular lattice walks keep their region, looked up again
+    // only after a move that wraps across the cell edge (the kernel's
+    // formulation; the reference looks it up every move)
+    const bool tracked = !in.single && !in.perm && !in.reject;
     int new_slot = slot;
-    if (!in.single && geom) new_slot = k_lookup(G, fx, fy, fz);
+    if (!in.single && geom && (!tracked || wrapped)) new_slot = k_lookup(G, fx, fy, fz);
     if (in.relax) {
       const T y2 = G.t2term[in.perm ? new_slot : slot];
       const T yy = y2 - t2c;
