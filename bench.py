@@ -53,8 +53,8 @@ SEED = 1234
 PGSE_STEPS, OGSE_STEPS = 25000, 30000
 # from one ncu --set full capture of the PGSE walk launch (262,144 walkers):
 # DRAM bytes read + written per walker, and smsp__issue_active
-WALK_DRAM_BYTES_PER_WALKER = 162816.0 / 262144
-WALK_ISSUE_ACTIVE_NCU = 0.756
+WALK_DRAM_BYTES_PER_WALKER = 159488.0 / 262144
+WALK_ISSUE_ACTIVE_NCU = 0.789
 
 
 def workload_records(A):
