@@ -219,12 +219,14 @@ def main(argv=None):
     import json
     ap = argparse.ArgumentParser(description="time one seeded workload on the GPU")
     ap.add_argument("workload", choices=["free_box", "one_cylinder", "gamma_pack", "mag_lowfield",
-                                         "wc_sphere", "mesh_sphere"])
+                                         "wc_sphere", "mesh_sphere", "batch_256"])
     ap.add_argument("--steps", type=int, default=0, help="cut every walk to this many steps")
     ap.add_argument("--walkers", type=int, default=0)
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--cpu-sample", type=int, default=0,
                     help="mag_lowfield: also time the CPU oracle on this many walkers")
+    ap.add_argument("--walker-scale", type=float, default=0.25,
+                    help="batch_256: scale of every job's walker count")
     a = ap.parse_args(argv)
     if a.workload == "mag_lowfield":
         print(json.dumps(measure_mag(a.walkers, a.steps, a.reps, a.cpu_sample)))
@@ -232,6 +234,8 @@ def main(argv=None):
         print(json.dumps(measure_wc(a.walkers or 32768, a.steps or 22000, a.reps)))
     elif a.workload == "mesh_sphere":
         print(json.dumps(measure_mesh(a.walkers or (1 << 20), a.steps or 6001, a.reps)))
+    elif a.workload == "batch_256":
+        print(json.dumps(measure_batch(a.walker_scale, a.steps or 3000, a.reps)))
     else:
         print(json.dumps(measure(a.workload, a.steps, a.walkers, a.reps)))
 
@@ -337,6 +341,27 @@ def measure_mesh(walkers: int = 1 << 20, steps: int = 6001, reps: int = 3, devic
             "mesh_seconds": t_m, "escaped": r.escaped,
             "hits_per_move": r.hits / r.walker_steps,
             "sphere_walker_steps_per_s": walkers * (steps - 1) / t_s}
+
+
+def measure_batch(walker_scale: float = 0.25, max_steps: int = 3000, reps: int = 3,
+                  device=None) -> dict:
+    """The uneven 256-substrate batch as one persistent launch replayed from a
+    CUDA graph (the autotuned tile): walker-steps/s and signals/s."""
+    from .acquisition import default_device
+    from .batch import Batch
+    dev = device or default_device()
+    jobs = batch_256(walker_scale=walker_scale, max_steps=max_steps)
+    b = Batch(jobs, device=dev)
+    b.launch()
+    b.read()
+    t = min(_timed(lambda: (b.launch(), b.read())) for _ in range(reps))
+    info = b.info()
+    b.close()
+    ws = sum(j.num_walkers * (j.steps - 1) for j in jobs)
+    return {"workload": "batch_256", "jobs": len(jobs), "walker_scale": walker_scale,
+            "max_steps": max_steps, "walker_steps": ws, "seconds": t,
+            "walker_steps_per_s": ws / t, "signals_per_s": sum(len(j.seqs) for j in jobs) / t,
+            "info": {k: v for k, v in info.items() if isinstance(v, (int, float, str))}}
 
 
 def _timed(fn):
