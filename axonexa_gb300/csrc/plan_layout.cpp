@@ -176,6 +176,10 @@ void fill_walk_params(WalkParams &P, char *base, const ArenaLayout &L, const Geo
   P.wave_il = (const float *)(base + L.o_wave);
   for (int c = 0; c < AXX_KMAX; ++c)
     for (int k = 0; k < 3; ++k) P.ch_p[c][k] = kt.ch_p[c][k];
+  P.one_dir = 1;
+  for (int c = 1; c < kt.K; ++c)
+    for (int k = 0; k < 3; ++k)
+      if (kt.ch_p[c][k] != kt.ch_p[0][k]) P.one_dir = 0;
   P.M = M;
   P.compart = (mode == AXX_MODE_LATTICE && (p->flags & AXX_FLAG_COMPARTMENTS)) ? 1 : 0;
   P.coef = (const double *)(base + L.o_coef);

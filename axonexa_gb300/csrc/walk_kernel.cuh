@@ -604,12 +604,21 @@ __device__ __forceinline__ void do_move(const WalkParams &P, const SmemView &S,
     for (int c = 0; c < KMAX; ++c) wv[c] = __ldg(&wrow[c]);
   }
 #pragma unroll
-  for (int c = 0; c < KMAX; ++c) {
-    const float d = fma_f(P.ch_p[c][2], pz, fma_f(P.ch_p[c][1], py, P.ch_p[c][0] * px));
-    if (DEFER)
-      W.part[c] = fma_f(wv[c], d, W.part[c]);
-    else
-      kahan_add(W.acc[c], W.cmp[c], wv[c] * d);
+  if (DEFER && KMAX > 1 && P.one_dir) {
+    // every channel projects on the same direction (padded channels carry
+    // zero waveforms): one projection serves all, the same bits as each
+    const float d = fma_f(P.ch_p[0][2], pz, fma_f(P.ch_p[0][1], py, P.ch_p[0][0] * px));
+#pragma unroll
+    for (int c = 0; c < KMAX; ++c) W.part[c] = fma_f(wv[c], d, W.part[c]);
+  } else {
+#pragma unroll
+    for (int c = 0; c < KMAX; ++c) {
+      const float d = fma_f(P.ch_p[c][2], pz, fma_f(P.ch_p[c][1], py, P.ch_p[c][0] * px));
+      if (DEFER)
+        W.part[c] = fma_f(wv[c], d, W.part[c]);
+      else
+        kahan_add(W.acc[c], W.cmp[c], wv[c] * d);
+    }
   }
   // Behind impermeable specular walls a walker stays in its region: it is
   // looked up again only when the move wraps across the cell edge (into
