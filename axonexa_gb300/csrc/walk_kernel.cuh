@@ -198,6 +198,7 @@ __device__ __forceinline__ float seg_root(float bh, float c0, float c1, float ep
     if (disc <= 0.0f) return AXX_INF;
     s = div_f(c0, sqrt_f(disc) - bh);
   } else {  // on the surface: the far root
+    if (fma_f(rem, aa, 2.0f * bh) < 0.0f) return AXX_INF;  // beyond rem (see surface_hit)
     s = div_f(-2.0f * bh, aa);
   }
   if (!(s > 0.0f && s < rem && s >= eps)) return AXX_INF;
@@ -222,6 +223,12 @@ __device__ __forceinline__ float surface_hit(const float4 &g, float eps, bool sp
   const float pz = sph ? (sz - g.z) : 0.0f;
   const float bh = sph ? fma_f(px, dx, fma_f(py, dy, pz * dz)) : fma_f(px, dx, py * dy);
   if (bh >= 0.0f) return AXX_INF;
+  // The far root -2 bh / aa is at least rem when rem aa + 2 bh < 0: a
+  // correctly rounded fma keeps the sign of the exact value (2 bh is exact),
+  // and rounding is monotone, so the rounded quotient then fails s < rem
+  // exactly as below; the usual case (a chord across the pore far longer than
+  // the step) skips the division.
+  if (fma_f(rem, aa, 2.0f * bh) < 0.0f) return AXX_INF;
   const float s = div_f(-2.0f * bh, aa);
   if (!(s > 0.0f && s < rem && s >= eps)) return AXX_INF;
   return s;
@@ -510,7 +517,10 @@ __device__ __forceinline__ float wrap_sel(float x, float a) {
 // DEFER: the move's phase terms go to W.part (FP32 sums over a block of
 // moves, folded into the compensated sums by the caller) instead of the
 // compensated sums directly.
-template <int GEOM, int KMAX, int KM, bool TRACE, bool ONE, bool PICK = false, bool DEFER = false>
+// NOZ (cylinders along z, no channel projecting on z): z enters neither a
+// boundary test, a region lookup nor a phase term, so the walk keeps none.
+template <int GEOM, int KMAX, int KM, bool TRACE, bool ONE, bool PICK = false, bool DEFER = false,
+          bool NOZ = false>
 __device__ __forceinline__ void do_move(const WalkParams &P, const SmemView &S,
                                         const TraceParams &T, long long wid, int i, float u1,
                                         float u2, DevStream &st, Walker<KMAX> &W,
@@ -561,7 +571,7 @@ __device__ __forceinline__ void do_move(const WalkParams &P, const SmemView &S,
     const MoveOut o = boundary<GEOM, perm, ONE>(P, C, W.x, W.y, W.z, dx, dy, dz, L, v, st, Lb);
     fx = o.fx;
     fy = o.fy;
-    fz = o.fz;
+    fz = NOZ ? W.z : o.fz;
     hits = o.hits;
     res.hits += (unsigned)o.hits;
     res.caps += o.capped ? 1u : 0u;
@@ -575,14 +585,14 @@ __device__ __forceinline__ void do_move(const WalkParams &P, const SmemView &S,
   } else {
     W.ux = W.ux + (fx - W.x);
     W.uy = W.uy + (fy - W.y);
-    W.uz = W.uz + (fz - W.z);
+    if (!NOZ) W.uz = W.uz + (fz - W.z);
     px = W.ux;
     py = W.uy;
     pz = W.uz;
     const float ox = fx, oy = fy, oz = fz;
     fx = wrap_sel(fx, P.a);
     fy = wrap_sel(fy, P.b);
-    fz = wrap_sel(fz, P.c);
+    if (!NOZ) fz = wrap_sel(fz, P.c);
     wrapped = (fx != ox) || (fy != oy) || (fz != oz);
   }
   // phase channels: s_c(i) is wave_il[i*KMAX + c]; padded channels carry
@@ -607,13 +617,16 @@ __device__ __forceinline__ void do_move(const WalkParams &P, const SmemView &S,
   if (DEFER && KMAX > 1 && P.one_dir) {
     // every channel projects on the same direction (padded channels carry
     // zero waveforms): one projection serves all, the same bits as each
-    const float d = fma_f(P.ch_p[0][2], pz, fma_f(P.ch_p[0][1], py, P.ch_p[0][0] * px));
+    const float dxy = fma_f(P.ch_p[0][1], py, P.ch_p[0][0] * px);
+    const float d = NOZ ? dxy : fma_f(P.ch_p[0][2], pz, dxy);
 #pragma unroll
     for (int c = 0; c < KMAX; ++c) W.part[c] = fma_f(wv[c], d, W.part[c]);
   } else {
 #pragma unroll
     for (int c = 0; c < KMAX; ++c) {
-      const float d = fma_f(P.ch_p[c][2], pz, fma_f(P.ch_p[c][1], py, P.ch_p[c][0] * px));
+      // (NOZ: the z term fma(0, pz, dxy) is dxy)
+      const float dxy = fma_f(P.ch_p[c][1], py, P.ch_p[c][0] * px);
+      const float d = NOZ ? dxy : fma_f(P.ch_p[c][2], pz, dxy);
       if (DEFER)
         W.part[c] = fma_f(wv[c], d, W.part[c]);
       else
@@ -675,7 +688,7 @@ __device__ __forceinline__ void do_move(const WalkParams &P, const SmemView &S,
 // One walker.  On return W holds the channel sums (value, Kahan
 // compensation) and the T2 sum.  TRACE records every move of the walker when
 // wid < ntrace.
-template <int GEOM, int KMAX, int KM, bool TRACE, bool ONE>
+template <int GEOM, int KMAX, int KM, bool TRACE, bool ONE, bool NOZ = false>
 __device__ __forceinline__ WalkResult walk_one(const WalkParams &P, const SmemView &S,
                                                const TraceParams &T, long long wid,
                                                Walker<KMAX> &W) {
@@ -776,10 +789,10 @@ __device__ __forceinline__ WalkResult walk_one(const WalkParams &P, const SmemVi
         st.load(P);
         const uint32_t w0 = st.b0, w1 = st.b1, w2 = st.b2, w3 = st.b3;
         st.pos = 2;
-        do_move<GEOM, KMAX, KM, TRACE, ONE, false, defer>(
+        do_move<GEOM, KMAX, KM, TRACE, ONE, false, defer, NOZ>(
             P, S, T, wid, i, word_to_uniform(w0), word_to_uniform(w1), st, W, res, g0, a0);
         st.pos = 4;
-        do_move<GEOM, KMAX, KM, TRACE, ONE, false, defer>(
+        do_move<GEOM, KMAX, KM, TRACE, ONE, false, defer, NOZ>(
             P, S, T, wid, i + 1, word_to_uniform(w2), word_to_uniform(w3), st, W, res, g0, a0);
       }
 #pragma unroll
@@ -793,7 +806,8 @@ __device__ __forceinline__ WalkResult walk_one(const WalkParams &P, const SmemVi
     }
     float u1, u2;
     st.next2(P, u1, u2);
-    do_move<GEOM, KMAX, KM, TRACE, ONE>(P, S, T, wid, i, u1, u2, st, W, res, g0, a0);
+    do_move<GEOM, KMAX, KM, TRACE, ONE, false, false, NOZ>(P, S, T, wid, i, u1, u2, st, W, res,
+                                                          g0, a0);
   }
   if (!single && KM == AXX_KM_LAT_IMP && ONE) {  // the T2 sum of the walker's one region
     const double t = (double)(i - 1) * (double)S.slot[W.slot].z;
@@ -838,10 +852,15 @@ __device__ __forceinline__ double warp_sum(double v) {
 // GT: the substrate tables stay in global memory (too large to stage in
 // shared memory); a compile-time choice, so that the staged kernels keep
 // their shared-memory loads.
-template <int GEOM, int KMAX, int KM, bool TRACE, bool ONEONLY = false, bool GT = false>
+// NOZ: single-instance walks of a cylinder along z whose channels carry no
+// z projection (the host checks both); z is not walked.
+template <int GEOM, int KMAX, int KM, bool TRACE, bool ONEONLY = false, bool GT = false,
+          bool NOZ = false>
 __global__ void __launch_bounds__(AXX_BLOCK, ONEONLY && KMAX <= 4 ? AXX_MIN_BLOCKS + 1
                                                                  : AXX_MIN_BLOCKS_FOR(KMAX))
     walk_kernel(const __grid_constant__ WalkParams P, const __grid_constant__ TraceParams T) {
+  static_assert(!NOZ || (GEOM == AXX_GEOM_CYL && ONEONLY && !TRACE),
+                "z is dropped only from single-cylinder walks without traces");
   extern __shared__ __align__(16) unsigned char smem[];
   constexpr int warps = AXX_BLOCK / 32;
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -907,7 +926,7 @@ __global__ void __launch_bounds__(AXX_BLOCK, ONEONLY && KMAX <= 4 ? AXX_MIN_BLOC
     if (active) {
       WalkResult r;
       if constexpr (ONEONLY)
-        r = walk_one<GEOM, KMAX, KM, TRACE, true>(P, S, T, wid, W);
+        r = walk_one<GEOM, KMAX, KM, TRACE, true, NOZ>(P, S, T, wid, W);
       else if constexpr (KMAX > 4)  // (the list path serves one instance too)
         r = walk_one<GEOM, KMAX, KM, TRACE, false>(P, S, T, wid, W);
       else

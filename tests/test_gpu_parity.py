@@ -274,6 +274,33 @@ def test_signals_against_oracle(dev, orc, name, make, flags, dt, steps):
             assert abs(v - k32[j, c]) <= 2e-5 * n, (j, c, v, k32[j, c])
 
 
+def test_z_free_cylinder_walk(dev, orc):
+    """A cylinder along z with gradients in the xy plane runs the instantiation
+    that walks no z.  Its sums equal those of the same sequences run beside a
+    z-gradient sequence (the instantiation that walks z), and the FP32
+    mirror's trajectories (which walk z) give the same hit count and sums
+    (the mirror sums each sequence's phase in FP64, hence the wider bound)."""
+    import os
+    import axonexa_gb300 as A
+    lat, bases = cases.one_cylinder()
+    xy = [cases.pgse(0), cases.pgse(150), cases.cos_ogse(100, 2, g=(0.6, 0.8, 0.0)),
+          cases.cos_ogse(80, 1, kind=2, g=(0.0, 1.0, 0.0))]
+    zseq = cases.cos_ogse(60, 1, kind=2, g=(0.0, 0.0, 1.0))
+    n, steps, dt, seed = 4096, 2500, 0.002, 31
+    L, B, S = to_product(lat, bases, xy)
+    _, _, Sz = to_product(lat, bases, xy + [zseq])
+    a = A.run_lattice(L, B, S, n, steps, dt, seed, relaxation=True, device=dev)
+    b = A.run_lattice(L, B, Sz, n, steps, dt, seed, relaxation=True, device=dev)
+    k = len(xy)
+    np.testing.assert_allclose(a.mx, b.mx[:k], rtol=0, atol=1e-9)
+    np.testing.assert_allclose(a.my, b.my[:k], rtol=0, atol=1e-9)
+    assert a.hits == b.hits
+    p = cases.params(n, steps, seed, dt=dt, flags=1)
+    k32, _, _ = orc.walk(lat, bases, xy, p, orc.KERN32, nthreads=os.cpu_count() or 1)
+    np.testing.assert_allclose(a.mx, k32[:, 0], rtol=0, atol=2e-5 * n)
+    np.testing.assert_allclose(a.my, k32[:, 1], rtol=0, atol=2e-5 * n)
+
+
 def test_free_diffusion_exp_minus_bD_full_size(dev):
     """Config: empty periodic 50 um box, 65,536 walkers, dt 5 us, 6,000 steps,
     PGSE delta 5 ms, Delta 20 ms, 16 G values 0-300 mT/m: S = exp(-b D)."""
