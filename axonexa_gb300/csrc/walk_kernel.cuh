@@ -503,6 +503,92 @@ __device__ __forceinline__ MoveOut boundary(const WalkParams &P, const Cands<GEO
   return o;
 }
 
+// seg_root for a segment that passes its first rejections (seg_may holds),
+// with selects in place of the early returns: the same operations on the
+// same operands, so the same value, and one square root and one division
+// whatever the case.
+__device__ __forceinline__ float seg_root_may(float bh, float c0, float eps, float aa,
+                                              float rem) {
+  const bool in = c0 < 0.0f, out = c0 > 0.0f, lo = bh <= 0.0f;
+  const float disc = fma_f(bh, bh, -(aa * c0));  // > 0 inside (aa > 0)
+  const float sq = sqrt_f(disc > 0.0f ? disc : 0.0f);
+  const float num = in ? (lo ? sq - bh : -c0) : (out ? c0 : -2.0f * bh);
+  const float den = in ? (lo ? aa : bh + sq) : (out ? sq - bh : aa);
+  const float s = div_f(num, den);
+  const bool ok = !(out && disc <= 0.0f) && s > 0.0f && s < rem && s >= eps;
+  return ok ? s : AXX_INF;
+}
+
+// boundary() for a single cylinder or sphere held in registers: the same
+// passes, the first from the pre-filter's quadratic (seg_root_may), the later
+// ones from the surface (surface_hit), with the loop test on the pass's result.
+template <int GEOM, bool PERM>
+__device__ __forceinline__ MoveOut boundary_one(const WalkParams &P, const Cands<GEOM, true> &C,
+                                                float sx, float sy, float sz, float dx, float dy,
+                                                float dz, float L, float v, DevStream &st,
+                                                float Lb) {
+  static_assert(GEOM == AXX_GEOM_CYL || GEOM == AXX_GEOM_SPH, "one cylinder or sphere");
+  constexpr bool sph = GEOM == AXX_GEOM_SPH;
+  const float4 g = C.g0, a = C.a0;
+  float aa = sph ? fma_f(dx, dx, fma_f(dy, dy, dz * dz)) : fma_f(dx, dx, dy * dy);
+  float bh, c0, c1;
+  seg_coef(g, sph, sx, sy, sz, dx, dy, dz, L, bh, c0, c1);
+  const bool maybe = seg_may(bh, c0, c1, aa, L);
+  MoveOut o;
+  o.hits = 0;
+  o.capped = false;
+  o.fx = fma_f(L, dx, sx);
+  o.fy = fma_f(L, dy, sy);
+  o.fz = fma_f(L, dz, sz);
+  if (!__any_sync(__activemask(), maybe) || !maybe) return o;
+  float rem = L;
+  float best = seg_root_may(bh, c0, a.y, aa, rem);
+  while (best < AXX_INF) {
+    if (o.hits == AXX_REFL_CAP) {
+      o.capped = true;
+      o.fx = sx;
+      o.fy = sy;
+      o.fz = sz;
+      return o;
+    }
+    const float hx = fma_f(best, dx, sx), hy = fma_f(best, dy, sy), hz = fma_f(best, dz, sz);
+    const float rem_before = rem;
+    rem = (o.hits == 0 ? Lb : rem) - best;
+    ++o.hits;
+    if (PERM) {
+      const float u = st.next(P);
+      const float ptr = div_f(C.S.slot[aux_slot(a)].w, v);
+      if (!(u > ptr)) {  // transmitted: continue with the speed of the far side
+        const float tx = fma_f(rem_before, dx, sx), ty = fma_f(rem_before, dy, sy),
+                    tz = fma_f(rem_before, dz, sz);
+        const int ts = C.lookup(P.ecs_slot, tx, ty, tz);
+        const float vn = C.S.slot[ts].x;
+        const float remt = div_f(rem * vn, v);
+        o.fx = fma_f(remt, dx, hx);
+        o.fy = fma_f(remt, dy, hy);
+        o.fz = fma_f(remt, dz, hz);
+        return o;
+      }
+    }
+    const float nx = (hx - g.x) * a.x, ny = (hy - g.y) * a.x;
+    const float nz = sph ? (hz - g.z) * a.x : 0.0f;
+    const float dn = sph ? fma_f(dx, nx, fma_f(dy, ny, dz * nz)) : fma_f(dx, nx, dy * ny);
+    const float t = -2.0f * dn;
+    dx = fma_f(t, nx, dx);
+    dy = fma_f(t, ny, dy);
+    if (sph) dz = fma_f(t, nz, dz);
+    sx = hx;
+    sy = hy;
+    sz = hz;
+    aa = sph ? fma_f(dx, dx, fma_f(dy, dy, dz * dz)) : fma_f(dx, dx, dy * dy);
+    best = surface_hit(g, a.y, sph, sx, sy, sz, dx, dy, dz, aa, rem);
+  }
+  o.fx = fma_f(rem, dx, sx);
+  o.fy = fma_f(rem, dy, sy);
+  o.fz = fma_f(rem, dz, sz);
+  return o;
+}
+
 // Branch-free periodic wrap (Lattice::lmod for a displacement below one cell).
 __device__ __forceinline__ float wrap_sel(float x, float a) {
   const float hi = x - a, lo = x + a;
@@ -568,7 +654,11 @@ __device__ __forceinline__ void do_move(const WalkParams &P, const SmemView &S,
     fy = back ? W.y : fy;
     fz = back ? W.z : fz;
   } else {
-    const MoveOut o = boundary<GEOM, perm, ONE>(P, C, W.x, W.y, W.z, dx, dy, dz, L, v, st, Lb);
+    MoveOut o;
+    if constexpr (ONE && (GEOM == AXX_GEOM_CYL || GEOM == AXX_GEOM_SPH))
+      o = boundary_one<GEOM, perm>(P, C, W.x, W.y, W.z, dx, dy, dz, L, v, st, Lb);
+    else
+      o = boundary<GEOM, perm, ONE>(P, C, W.x, W.y, W.z, dx, dy, dz, L, v, st, Lb);
     fx = o.fx;
     fy = o.fy;
     fz = NOZ ? W.z : o.fz;
