@@ -79,7 +79,7 @@ struct WalkParams {
   const float *wave_il;       // [steps][kmax]
   float ch_p[AXX_KMAX][3];    // channel projections (0 for padded channels)
   int one_dir;                // every channel in use has the same projection
-  int no_z_phase;             // no channel projects on z
+  int phase_axes;             // axes some channel projects on (bits x, y, z)
   int M;
   int compart;                // also sums over walkers starting in a basis: rows M..2M-1
   int global_tables;          // substrate tables read from global memory (too big to stage)

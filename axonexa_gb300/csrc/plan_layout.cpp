@@ -180,9 +180,10 @@ void fill_walk_params(WalkParams &P, char *base, const ArenaLayout &L, const Geo
   for (int c = 1; c < kt.K; ++c)
     for (int k = 0; k < 3; ++k)
       if (kt.ch_p[c][k] != kt.ch_p[0][k]) P.one_dir = 0;
-  P.no_z_phase = 1;
+  P.phase_axes = 0;
   for (int c = 0; c < AXX_KMAX; ++c)
-    if (kt.ch_p[c][2] != 0.0f) P.no_z_phase = 0;
+    for (int k = 0; k < 3; ++k)
+      if (kt.ch_p[c][k] != 0.0f) P.phase_axes |= 1 << k;
   P.M = M;
   P.compart = (mode == AXX_MODE_LATTICE && (p->flags & AXX_FLAG_COMPARTMENTS)) ? 1 : 0;
   P.coef = (const double *)(base + L.o_coef);

@@ -8,10 +8,10 @@
 namespace axx {
 
 template <int GEOM, int KMAX, int KM, bool TRACE, bool ONE = false, bool GT = false,
-          bool NOZ = false>
+          int PAX = 7>
 static cudaError_t walk_go(const WalkParams &P, const TraceParams &T, int grid, size_t smem,
                            cudaStream_t s) {
-  auto fn = walk_kernel<GEOM, KMAX, KM, TRACE, ONE, GT, NOZ>;
+  auto fn = walk_kernel<GEOM, KMAX, KM, TRACE, ONE, GT, PAX>;
   if (smem > 48 * 1024) {
     const cudaError_t e =
         cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -70,15 +70,22 @@ static cudaError_t walk_launch_km(int kmax, bool trace, bool one, bool gt, const
     return cudaErrorInvalidValue;
   } else {
   if (lat1 && walk_one_variant<GEOM, KM>(kmax, trace, one)) {
-    // impermeable single cylinders without z phase: the z-free instantiation
-    // (its occupancy is that of the instantiation below: same bounds, no
-    // more registers)
+    // impermeable single cylinders without z phase: the instantiations that
+    // walk no z, and no unbounded y when only x carries phase (their
+    // occupancy is that of the instantiation below: the same launch bounds,
+    // which every one of them meets without spilling)
     if constexpr (GEOM == AXX_GEOM_CYL && KM == AXX_KM_LAT_IMP) {
-      if (P.no_z_phase) {
+      if (!(P.phase_axes & 4) && !(P.phase_axes & 2)) {
         switch (kmax) {
-          case 1: return walk_go<GEOM, 1, KM, false, true, false, true>(P, T, grid, smem, s);
-          case 2: return walk_go<GEOM, 2, KM, false, true, false, true>(P, T, grid, smem, s);
-          case 4: return walk_go<GEOM, 4, KM, false, true, false, true>(P, T, grid, smem, s);
+          case 1: return walk_go<GEOM, 1, KM, false, true, false, 1>(P, T, grid, smem, s);
+          case 2: return walk_go<GEOM, 2, KM, false, true, false, 1>(P, T, grid, smem, s);
+          case 4: return walk_go<GEOM, 4, KM, false, true, false, 1>(P, T, grid, smem, s);
+        }
+      } else if (!(P.phase_axes & 4)) {
+        switch (kmax) {
+          case 1: return walk_go<GEOM, 1, KM, false, true, false, 3>(P, T, grid, smem, s);
+          case 2: return walk_go<GEOM, 2, KM, false, true, false, 3>(P, T, grid, smem, s);
+          case 4: return walk_go<GEOM, 4, KM, false, true, false, 3>(P, T, grid, smem, s);
         }
       }
     }

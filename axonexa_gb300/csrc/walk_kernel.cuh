@@ -503,6 +503,23 @@ __device__ __forceinline__ MoveOut boundary(const WalkParams &P, const Cands<GEO
   return o;
 }
 
+// A channel's projection p . r, fma(p_z, z, fma(p_y, y, p_x x)), over the
+// axes in PAX: a term of a zero coefficient adds a zero, so leaving it out
+// gives the same value (up to the sign of a zero sum).
+template <int PAX>
+__device__ __forceinline__ float project(const float p[3], float x, float y, float z) {
+  float d;
+  if ((PAX & 3) == 3)
+    d = fma_f(p[1], y, p[0] * x);
+  else if (PAX & 1)
+    d = p[0] * x;
+  else if (PAX & 2)
+    d = p[1] * y;
+  else
+    d = 0.0f;
+  return (PAX & 4) ? fma_f(p[2], z, d) : d;
+}
+
 // seg_root for a segment that passes its first rejections (seg_may holds),
 // with selects in place of the early returns: the same operations on the
 // same operands, so the same value, and one square root and one division
@@ -603,10 +620,12 @@ __device__ __forceinline__ float wrap_sel(float x, float a) {
 // DEFER: the move's phase terms go to W.part (FP32 sums over a block of
 // moves, folded into the compensated sums by the caller) instead of the
 // compensated sums directly.
-// NOZ (cylinders along z, no channel projecting on z): z enters neither a
-// boundary test, a region lookup nor a phase term, so the walk keeps none.
+// PAX: the axes some channel projects on (bits x, y, z); the unbounded
+// coordinate of any other axis feeds nothing and is not kept.  Without z
+// (cylinders along z only) z enters neither a boundary test, a region lookup
+// nor a phase term, so the walk keeps no z at all.
 template <int GEOM, int KMAX, int KM, bool TRACE, bool ONE, bool PICK = false, bool DEFER = false,
-          bool NOZ = false>
+          int PAX = 7>
 __device__ __forceinline__ void do_move(const WalkParams &P, const SmemView &S,
                                         const TraceParams &T, long long wid, int i, float u1,
                                         float u2, DevStream &st, Walker<KMAX> &W,
@@ -615,6 +634,7 @@ __device__ __forceinline__ void do_move(const WalkParams &P, const SmemView &S,
   constexpr bool single = KM >= AXX_KM_SINGLE;
   constexpr bool perm = KM == AXX_KM_LAT_PERM;
   constexpr bool reject = KM == AXX_KM_LAT_REJ || KM == AXX_KM_SINGLE_REJ;
+  constexpr bool PX = PAX & 1, PY = PAX & 2, NOZ = !(PAX & 4);
   const float4 s4 = S.slot[W.slot];
   const float v = s4.x, Lb = s4.y;
   float dx, dy, dz, L = Lb;
@@ -673,8 +693,8 @@ __device__ __forceinline__ void do_move(const WalkParams &P, const SmemView &S,
     py = fy;
     pz = fz;
   } else {
-    W.ux = W.ux + (fx - W.x);
-    W.uy = W.uy + (fy - W.y);
+    if (PX) W.ux = W.ux + (fx - W.x);
+    if (PY) W.uy = W.uy + (fy - W.y);
     if (!NOZ) W.uz = W.uz + (fz - W.z);
     px = W.ux;
     py = W.uy;
@@ -707,16 +727,13 @@ __device__ __forceinline__ void do_move(const WalkParams &P, const SmemView &S,
   if (DEFER && KMAX > 1 && P.one_dir) {
     // every channel projects on the same direction (padded channels carry
     // zero waveforms): one projection serves all, the same bits as each
-    const float dxy = fma_f(P.ch_p[0][1], py, P.ch_p[0][0] * px);
-    const float d = NOZ ? dxy : fma_f(P.ch_p[0][2], pz, dxy);
+    const float d = project<PAX>(P.ch_p[0], px, py, pz);
 #pragma unroll
     for (int c = 0; c < KMAX; ++c) W.part[c] = fma_f(wv[c], d, W.part[c]);
   } else {
 #pragma unroll
     for (int c = 0; c < KMAX; ++c) {
-      // (NOZ: the z term fma(0, pz, dxy) is dxy)
-      const float dxy = fma_f(P.ch_p[c][1], py, P.ch_p[c][0] * px);
-      const float d = NOZ ? dxy : fma_f(P.ch_p[c][2], pz, dxy);
+      const float d = project<PAX>(P.ch_p[c], px, py, pz);
       if (DEFER)
         W.part[c] = fma_f(wv[c], d, W.part[c]);
       else
@@ -778,7 +795,7 @@ __device__ __forceinline__ void do_move(const WalkParams &P, const SmemView &S,
 // One walker.  On return W holds the channel sums (value, Kahan
 // compensation) and the T2 sum.  TRACE records every move of the walker when
 // wid < ntrace.
-template <int GEOM, int KMAX, int KM, bool TRACE, bool ONE, bool NOZ = false>
+template <int GEOM, int KMAX, int KM, bool TRACE, bool ONE, int PAX = 7>
 __device__ __forceinline__ WalkResult walk_one(const WalkParams &P, const SmemView &S,
                                                const TraceParams &T, long long wid,
                                                Walker<KMAX> &W) {
@@ -874,15 +891,16 @@ __device__ __forceinline__ WalkResult walk_one(const WalkParams &P, const SmemVi
       }
 #pragma unroll
       for (int c = 0; c < KMAX; ++c) W.part[c] = 0.0f;
-      for (int q = 0; q < 16 && i + 1 < P.steps; ++q, i += 2) {
+      const int stop = min(i + 32, P.steps - 1);  // 16 pairs, or up to the last pair
+      for (; i < stop; i += 2) {
         ++st.blk;
         st.load(P);
         const uint32_t w0 = st.b0, w1 = st.b1, w2 = st.b2, w3 = st.b3;
         st.pos = 2;
-        do_move<GEOM, KMAX, KM, TRACE, ONE, false, defer, NOZ>(
+        do_move<GEOM, KMAX, KM, TRACE, ONE, false, defer, PAX>(
             P, S, T, wid, i, word_to_uniform(w0), word_to_uniform(w1), st, W, res, g0, a0);
         st.pos = 4;
-        do_move<GEOM, KMAX, KM, TRACE, ONE, false, defer, NOZ>(
+        do_move<GEOM, KMAX, KM, TRACE, ONE, false, defer, PAX>(
             P, S, T, wid, i + 1, word_to_uniform(w2), word_to_uniform(w3), st, W, res, g0, a0);
       }
 #pragma unroll
@@ -896,7 +914,7 @@ __device__ __forceinline__ WalkResult walk_one(const WalkParams &P, const SmemVi
     }
     float u1, u2;
     st.next2(P, u1, u2);
-    do_move<GEOM, KMAX, KM, TRACE, ONE, false, false, NOZ>(P, S, T, wid, i, u1, u2, st, W, res,
+    do_move<GEOM, KMAX, KM, TRACE, ONE, false, false, PAX>(P, S, T, wid, i, u1, u2, st, W, res,
                                                           g0, a0);
   }
   if (!single && KM == AXX_KM_LAT_IMP && ONE) {  // the T2 sum of the walker's one region
@@ -942,15 +960,16 @@ __device__ __forceinline__ double warp_sum(double v) {
 // GT: the substrate tables stay in global memory (too large to stage in
 // shared memory); a compile-time choice, so that the staged kernels keep
 // their shared-memory loads.
-// NOZ: single-instance walks of a cylinder along z whose channels carry no
-// z projection (the host checks both); z is not walked.
+// PAX: the axes the channels project on (bits x, y, z; the host checks that
+// no channel has a component on another axis); an instantiation without z
+// serves single-instance walks of a cylinder along z, which then walk no z.
 template <int GEOM, int KMAX, int KM, bool TRACE, bool ONEONLY = false, bool GT = false,
-          bool NOZ = false>
+          int PAX = 7>
 __global__ void __launch_bounds__(AXX_BLOCK, ONEONLY && KMAX <= 4 ? AXX_MIN_BLOCKS + 1
                                                                  : AXX_MIN_BLOCKS_FOR(KMAX))
     walk_kernel(const __grid_constant__ WalkParams P, const __grid_constant__ TraceParams T) {
-  static_assert(!NOZ || (GEOM == AXX_GEOM_CYL && ONEONLY && !TRACE),
-                "z is dropped only from single-cylinder walks without traces");
+  static_assert(PAX == 7 || (GEOM == AXX_GEOM_CYL && ONEONLY && !TRACE),
+                "axes are dropped only from single-cylinder walks without traces");
   extern __shared__ __align__(16) unsigned char smem[];
   constexpr int warps = AXX_BLOCK / 32;
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1016,7 +1035,7 @@ __global__ void __launch_bounds__(AXX_BLOCK, ONEONLY && KMAX <= 4 ? AXX_MIN_BLOC
     if (active) {
       WalkResult r;
       if constexpr (ONEONLY)
-        r = walk_one<GEOM, KMAX, KM, TRACE, true, NOZ>(P, S, T, wid, W);
+        r = walk_one<GEOM, KMAX, KM, TRACE, true, PAX>(P, S, T, wid, W);
       else if constexpr (KMAX > 4)  // (the list path serves one instance too)
         r = walk_one<GEOM, KMAX, KM, TRACE, false>(P, S, T, wid, W);
       else

@@ -274,17 +274,26 @@ def test_signals_against_oracle(dev, orc, name, make, flags, dt, steps):
             assert abs(v - k32[j, c]) <= 2e-5 * n, (j, c, v, k32[j, c])
 
 
-def test_z_free_cylinder_walk(dev, orc):
-    """A cylinder along z with gradients in the xy plane runs the instantiation
-    that walks no z.  Its sums equal those of the same sequences run beside a
-    z-gradient sequence (the instantiation that walks z), and the FP32
-    mirror's trajectories (which walk z) give the same hit count and sums
-    (the mirror sums each sequence's phase in FP64, hence the wider bound)."""
+XY_SEQS = {
+    "xy": lambda: [cases.pgse(0), cases.pgse(150), cases.cos_ogse(100, 2, g=(0.6, 0.8, 0.0)),
+                   cases.cos_ogse(80, 1, kind=2, g=(0.0, 1.0, 0.0))],
+    "x": lambda: [cases.pgse(0), cases.pgse(150), cases.cos_ogse(100, 2),
+                  cases.cos_ogse(80, 1, kind=3)],
+}
+
+
+@pytest.mark.parametrize("axes", sorted(XY_SEQS))
+def test_z_free_cylinder_walk(dev, orc, axes):
+    """A cylinder along z with gradients in the xy plane (or along x) runs the
+    instantiation that walks no z (and no unbounded y).  Its sums equal those
+    of the same sequences run beside a z-gradient sequence (the
+    instantiation that walks every axis), and the FP32 mirror's trajectories
+    (which walk z) give the same sums (the mirror sums each sequence's phase
+    in FP64, hence the wider bound)."""
     import os
     import axonexa_gb300 as A
     lat, bases = cases.one_cylinder()
-    xy = [cases.pgse(0), cases.pgse(150), cases.cos_ogse(100, 2, g=(0.6, 0.8, 0.0)),
-          cases.cos_ogse(80, 1, kind=2, g=(0.0, 1.0, 0.0))]
+    xy = XY_SEQS[axes]()
     zseq = cases.cos_ogse(60, 1, kind=2, g=(0.0, 0.0, 1.0))
     n, steps, dt, seed = 4096, 2500, 0.002, 31
     L, B, S = to_product(lat, bases, xy)
