@@ -325,6 +325,7 @@ struct Walker {
   float part[KMAX];  // phase of the current block of moves (DEFER)
   float t2s, t2c;
   int nin;  // ONE: moves weighted by the instance's region (T2 by counts)
+  float v0, L0;  // speed and step of the slot, where it never changes
 };
 
 // The instances and the list a move may test: either the cell list of the
@@ -635,7 +636,11 @@ __device__ __forceinline__ void do_move(const WalkParams &P, const SmemView &S,
   constexpr bool perm = KM == AXX_KM_LAT_PERM;
   constexpr bool reject = KM == AXX_KM_LAT_REJ || KM == AXX_KM_SINGLE_REJ;
   constexpr bool PX = PAX & 1, PY = PAX & 2, NOZ = !(PAX & 4);
-  const float4 s4 = S.slot[W.slot];
+  // a single pore, or one instance behind impermeable walls: the walker's
+  // slot never changes, and its speed and step stay in registers (the T2
+  // term, .z, is then not read per move)
+  constexpr bool fixed_slot = ONE && (single || KM == AXX_KM_LAT_IMP);
+  const float4 s4 = fixed_slot ? make_float4(W.v0, W.L0, 0.0f, 0.0f) : S.slot[W.slot];
   const float v = s4.x, Lb = s4.y;
   float dx, dy, dz, L = Lb;
   if (PICK) {
@@ -839,6 +844,11 @@ __device__ __forceinline__ WalkResult walk_one(const WalkParams &P, const SmemVi
       const int cell = cell_of<GEOM>(P, x, y, z);
       W.slot = lookup_list<GEOM>(S, S.cstart[cell], S.cstart[cell + 1], P.ecs_slot, x, y, z);
     }
+  }
+  {
+    const float4 s = S.slot[W.slot];
+    W.v0 = s.x;
+    W.L0 = s.y;
   }
   int i = 1;
   if constexpr (single) {
