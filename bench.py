@@ -54,7 +54,7 @@ PGSE_STEPS, OGSE_STEPS = 25000, 30000
 # from one ncu --set full capture of the PGSE walk launch (262,144 walkers):
 # DRAM bytes read + written per walker, and smsp__issue_active
 WALK_DRAM_BYTES_PER_WALKER = 159488.0 / 262144
-WALK_ISSUE_ACTIVE_NCU = 0.789
+WALK_ISSUE_ACTIVE_NCU = 0.776
 
 
 def workload_records(A):
