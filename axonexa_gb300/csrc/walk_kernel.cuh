@@ -238,6 +238,7 @@ struct MoveOut {
   float fx, fy, fz;
   int hits;
   bool capped;
+  bool crossed;  // transmitted through a permeable wall
 };
 
 __device__ __forceinline__ void kahan_add(float &s, float &c, float y) {
@@ -397,6 +398,7 @@ __device__ __forceinline__ MoveOut boundary(const WalkParams &P, const Cands<GEO
   MoveOut o;
   o.hits = 0;
   o.capped = false;
+  o.crossed = false;
   if (!__any_sync(__activemask(), maybe) || !maybe) {
     o.fx = fma_f(L, dx, sx);
     o.fy = fma_f(L, dy, sy);
@@ -471,6 +473,7 @@ __device__ __forceinline__ MoveOut boundary(const WalkParams &P, const Cands<GEO
         o.fx = fma_f(remt, dx, hx);
         o.fy = fma_f(remt, dy, hy);
         o.fz = fma_f(remt, dz, hz);
+        o.crossed = true;
         return o;
       }
     }
@@ -555,6 +558,7 @@ __device__ __forceinline__ MoveOut boundary_one(const WalkParams &P, const Cands
   MoveOut o;
   o.hits = 0;
   o.capped = false;
+  o.crossed = false;
   o.fx = fma_f(L, dx, sx);
   o.fy = fma_f(L, dy, sy);
   o.fz = fma_f(L, dz, sz);
@@ -585,6 +589,7 @@ __device__ __forceinline__ MoveOut boundary_one(const WalkParams &P, const Cands
         o.fx = fma_f(remt, dx, hx);
         o.fy = fma_f(remt, dy, hy);
         o.fz = fma_f(remt, dz, hz);
+        o.crossed = true;
         return o;
       }
     }
@@ -660,6 +665,7 @@ __device__ __forceinline__ void do_move(const WalkParams &P, const SmemView &S,
   }
   float fx, fy, fz;
   int hits = 0;
+  bool crossed = false;
   if (GEOM == AXX_GEOM_FREE) {
     fx = fma_f(L, dx, W.x);
     fy = fma_f(L, dy, W.y);
@@ -688,6 +694,7 @@ __device__ __forceinline__ void do_move(const WalkParams &P, const SmemView &S,
     fy = o.fy;
     fz = NOZ ? W.z : o.fz;
     hits = o.hits;
+    crossed = o.crossed;
     res.hits += (unsigned)o.hits;
     res.caps += o.capped ? 1u : 0u;
   }
@@ -745,22 +752,36 @@ __device__ __forceinline__ void do_move(const WalkParams &P, const SmemView &S,
         kahan_add(W.acc[c], W.cmp[c], wv[c] * d);
     }
   }
-  // Behind impermeable specular walls a walker stays in its region: it is
-  // looked up again only when the move wraps across the cell edge (into
-  // another listed image, whose region id may differ), never with a single
-  // instance, whose T2 sum is then formed at the end.  (The FP32 lookup of a
-  // position a rounding error from a wall could name the other side; the
-  // FP64 reference's hardly ever does.)  Permeable and rejection walks look
-  // the region up after every move.
-  constexpr bool tracked = KM == AXX_KM_LAT_IMP;
-  if (!single && tracked && !ONE) {
-    kahan_add(W.t2s, W.t2c, s4.z);
-    if (GEOM != AXX_GEOM_FREE && wrapped) {
-      const int cell = cell_of<GEOM>(P, fx, fy, fz);
-      W.slot = lookup_list<GEOM>(S, S.cstart[cell], S.cstart[cell + 1], P.ecs_slot, fx, fy, fz);
+  // Behind specular walls a walker stays in its region: it is looked up
+  // again only when the move wraps across the cell edge (into another listed
+  // image, whose region id may differ) or crosses a permeable wall.  With a
+  // single instance (no reachable ghost) a wrap never changes the region: an
+  // impermeable walk then looks up nothing and forms its T2 sum at the end.
+  // (The FP32 lookup of a position a rounding error from a wall could name
+  // the other side; the FP64 reference's hardly ever does.)  Rejection walks
+  // look the region up after every move.
+  constexpr bool tracked = KM == AXX_KM_LAT_IMP || KM == AXX_KM_LAT_PERM;
+  if (!single && tracked && !(ONE && !perm)) {
+    // dt/T2 of the move's region (0 without relaxation); the permeable walk
+    // weights the region after the move (accumtime is always 0)
+    if (!perm) kahan_add(W.t2s, W.t2c, s4.z);
+    if (GEOM != AXX_GEOM_FREE && (ONE ? crossed : (wrapped || crossed))) {
+      if (ONE) {
+        W.slot = C.lookup(P.ecs_slot, fx, fy, fz);
+      } else {
+        const int cell = cell_of<GEOM>(P, fx, fy, fz);
+        W.slot =
+            lookup_list<GEOM>(S, S.cstart[cell], S.cstart[cell + 1], P.ecs_slot, fx, fy, fz);
+      }
+    }
+    if (perm) {
+      if (ONE)
+        W.nin += (W.slot != P.ecs_slot) ? 1 : 0;
+      else
+        kahan_add(W.t2s, W.t2c, S.slot[W.slot].z);
     }
   }
-  if (!single && !tracked) {
+  if (!single && !tracked) {  // rejection walks
     int new_slot = P.ecs_slot;
     if (GEOM != AXX_GEOM_FREE) {
       if (ONE) {
@@ -771,14 +792,13 @@ __device__ __forceinline__ void do_move(const WalkParams &P, const SmemView &S,
             lookup_list<GEOM>(S, S.cstart[cell], S.cstart[cell + 1], P.ecs_slot, fx, fy, fz);
       }
     }
-    // dt/T2 of the move's region (0 without relaxation); the permeable walk
-    // weights the region after the move (accumtime is always 0).  With one
-    // instance there are two regions: count the moves in the instance's and
-    // form the sum at the end.
+    // dt/T2 of the move's region (0 without relaxation).  With one instance
+    // there are two regions: count the moves in the instance's and form the
+    // sum at the end.
     if (ONE)
-      W.nin += ((perm ? new_slot : W.slot) != P.ecs_slot) ? 1 : 0;
+      W.nin += (W.slot != P.ecs_slot) ? 1 : 0;
     else
-      kahan_add(W.t2s, W.t2c, perm ? S.slot[new_slot].z : s4.z);
+      kahan_add(W.t2s, W.t2c, s4.z);
     W.slot = new_slot;
   }
   W.x = fx;

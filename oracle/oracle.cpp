@@ -341,6 +341,7 @@ struct KMove {
   T fx, fy, fz;
   int hits;
   bool capped;
+  bool crossed;  // transmitted through a permeable wall
 };
 
 template <typename T>
@@ -350,7 +351,7 @@ template <typename T>
 // speed * (dt - t_hit)).
 KMove<T> k_boundary(const KGeom<T> &G, T sx, T sy, T sz, T dx, T dy, T dz, T L, T v, bool perm,
                     Stream &st, T Lb) {
-  KMove<T> o{T(0), T(0), T(0), 0, false};
+  KMove<T> o{T(0), T(0), T(0), 0, false, false};
   T rem = L;
   int last = -1;
   for (;;) {
@@ -390,6 +391,7 @@ KMove<T> k_boundary(const KGeom<T> &G, T sx, T sy, T sz, T dx, T dy, T dz, T L, 
         o.fx = fmaT(remt, dx, hx);
         o.fy = fmaT(remt, dy, hy);
         o.fz = fmaT(remt, dz, hz);
+        o.crossed = true;
         return o;
       }
     }
@@ -852,6 +854,7 @@ void walk_kern(const WalkIn &in, const KGeom<T> &G, int64_t w, WalkOut &out, Tra
     }
     T fx, fy, fz;
     int hits = 0;
+    bool crossed = false;
     if (!geom) {
       fx = fmaT(Lseg, dx, x);
       fy = fmaT(Lseg, dy, y);
@@ -877,6 +880,7 @@ void walk_kern(const WalkIn &in, const KGeom<T> &G, int64_t w, WalkOut &out, Tra
       fy = o.fy;
       fz = o.fz;
       hits = o.hits;
+      crossed = o.crossed;
       out.caps += o.capped ? 1 : 0;
     }
     V3 pp;
@@ -895,12 +899,12 @@ void walk_kern(const WalkIn &in, const KGeom<T> &G, int64_t w, WalkOut &out, Tra
       wrapped = fx != ox || fy != oy || fz != oz;
     }
     for (int j = 0; j < in.nseq; ++j) out.phase[j] += in.gamma * dot(gfunc(in.seqs[j], dt * i), pp) * dt;
-    // impermeable specular lattice walks keep their region, looked up again
-    // only after a move that wraps across the cell edge (the kernel's
-    // formulation; the reference looks it up every move)
-    const bool tracked = !in.single && !in.perm && !in.reject;
+    // specular lattice walks keep their region, looked up again only after a
+    // move that wraps across the cell edge or crosses a permeable wall (the
+    // kernel's formulation; the reference looks it up every move)
+    const bool tracked = !in.single && !in.reject;
     int new_slot = slot;
-    if (!in.single && geom && (!tracked || wrapped)) new_slot = k_lookup(G, fx, fy, fz);
+    if (!in.single && geom && (!tracked || wrapped || crossed)) new_slot = k_lookup(G, fx, fy, fz);
     if (in.relax) {
       const T y2 = G.t2term[in.perm ? new_slot : slot];
       const T yy = y2 - t2c;
