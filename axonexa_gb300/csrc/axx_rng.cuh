@@ -213,22 +213,23 @@ struct DevStream {
   __device__ __forceinline__ float next(const KP &P) {
     return word_to_uniform(next_word(P));
   }
+  // The words at pos and pos + 1 need at most one new block (pos 3: the held
+  // block's last word, then the next block's first; pos 4: the next block's
+  // first two), so a warp whose lanes sit at different positions (permeable
+  // walks draw one word per wall hit) runs at most one block load per move.
   template <class KP>
   __device__ __forceinline__ void next2(const KP &P, float &u1, float &u2) {
-    if ((pos & 1) == 0) {
-      if (pos == 4) {
-        ++blk;
-        load(P);
-        pos = 0;
-      }
-      const bool lo = (pos == 0);
-      u1 = word_to_uniform(lo ? b0 : b2);
-      u2 = word_to_uniform(lo ? b1 : b3);
-      pos += 2;
-    } else {
-      u1 = next(P);
-      u2 = next(P);
+    const int p0 = pos;
+    const uint32_t last = b3;
+    if (p0 >= 3) {
+      ++blk;
+      load(P);
     }
+    const uint32_t w1 = (p0 == 1) ? b1 : (p0 == 2) ? b2 : (p0 == 3) ? last : b0;
+    const uint32_t w2 = (p0 == 1) ? b2 : (p0 == 2) ? b3 : (p0 == 3) ? b0 : b1;
+    u1 = word_to_uniform(w1);
+    u2 = word_to_uniform(w2);
+    pos = (p0 >= 3) ? p0 - 2 : p0 + 2;
   }
   __device__ __forceinline__ uint32_t words_used() const { return blk * 4u + (uint32_t)pos; }
 };
