@@ -29,7 +29,7 @@
 // 16 channels (32 accumulator registers) spill under the 80 registers of 6
 // resident blocks; 5 blocks (102 registers) measured 2 % faster than 6 and
 // 10 % faster than 4 on the 400-cylinder pack.
-#define AXX_MIN_BLOCKS_FOR(kmax) ((kmax) >= 16 ? 5 : AXX_MIN_BLOCKS)
+#define AXX_MIN_BLOCKS_FOR(kmax) ((kmax) >= 12 ? 5 : AXX_MIN_BLOCKS)
 #define AXX_SMEM_MAX (200 * 1024)
 
 enum { AXX_MODE_LATTICE = 0, AXX_MODE_SINGLE = 1 };

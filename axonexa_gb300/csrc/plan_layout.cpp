@@ -24,6 +24,9 @@ std::string make_kernel_tables(const GeomPlan &g, const SeqPlan &sq, int M, int 
   kt.km = walk_mode(mode, g.geom, flags);
   kt.kmax = 1;
   while (kt.kmax < kt.K || kt.kmax < min_kmax) kt.kmax <<= 1;
+  // lattice walks of 9-12 channels (four waveforms along three axes): a
+  // 12-channel capacity instead of 16 padded ones
+  if (mode == AXX_MODE_LATTICE && kt.kmax == 16 && kt.K <= 12 && min_kmax <= 12) kt.kmax = 12;
   if (kt.kmax > AXX_KMAX) return "channel capacity above 16";
   const int km = kt.kmax;
   kt.wave_il.assign((size_t)steps * km, 0.f);

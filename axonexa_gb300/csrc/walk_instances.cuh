@@ -101,6 +101,7 @@ static cudaError_t walk_launch_km(int kmax, bool trace, bool one, bool gt, const
     case 2: return walk_go<GEOM, 2, KM, false>(P, T, grid, smem, s);
     case 4: return walk_go<GEOM, 4, KM, false>(P, T, grid, smem, s);
     case 8: return walk_go<GEOM, 8, KM, false>(P, T, grid, smem, s);
+    case 12: return walk_go<GEOM, 12, KM, false>(P, T, grid, smem, s);  // lattice walks only
     case 16: return walk_go<GEOM, 16, KM, false>(P, T, grid, smem, s);
   }
   return cudaErrorInvalidValue;
@@ -143,6 +144,7 @@ static int walk_occ_km(int kmax, bool trace, bool one, bool gt, size_t smem) {
     case 2: return walk_occ<GEOM, 2, KM, false>(smem);
     case 4: return walk_occ<GEOM, 4, KM, false>(smem);
     case 8: return walk_occ<GEOM, 8, KM, false>(smem);
+    case 12: return walk_occ<GEOM, 12, KM, false>(smem);
     case 16: return walk_occ<GEOM, 16, KM, false>(smem);
   }
   return 0;

@@ -310,6 +310,36 @@ def test_z_free_cylinder_walk(dev, orc, axes):
     np.testing.assert_allclose(a.my, k32[:, 1], rtol=0, atol=2e-5 * n)
 
 
+def test_twelve_channel_capacity(dev, orc):
+    """Four waveforms along three axes make 12 phase channels, which a lattice
+    walk runs at a 12-channel capacity; beside a thirteenth channel the same
+    sequences run at 16.  Both give the same sums, and the FP32 mirror's
+    trajectories agree."""
+    import os
+    import axonexa_gb300 as A
+    lat, bases = cases.hex_cylinders(kappa=2e-5)
+    axes = ((1.0, 0.0, 0.0), (0.0, 1.0, 0.0), (0.0, 0.0, 1.0))
+    seqs = []
+    for g in axes:
+        seqs += [cases.pgse(120, g=g), cases.cos_ogse(80, 1, g=g), cases.cos_ogse(80, 2, g=g),
+                 cases.cos_ogse(60, 2, kind=2, g=g)]
+    extra = cases.pgse(90, delta=5.0, Delta=15.0)
+    n, steps, dt, seed = 4096, 2000, 0.001, 17
+    L, B, S = to_product(lat, bases, seqs)
+    _, _, S13 = to_product(lat, bases, seqs + [extra])
+    kw = dict(relaxation=True, permeable=True, device=dev)
+    a = A.run_lattice(L, B, S, n, steps, dt, seed, **kw)
+    b = A.run_lattice(L, B, S13, n, steps, dt, seed, **kw)
+    k = len(seqs)
+    np.testing.assert_allclose(a.mx, b.mx[:k], rtol=0, atol=1e-9)
+    np.testing.assert_allclose(a.my, b.my[:k], rtol=0, atol=1e-9)
+    assert a.hits == b.hits and a.hits > 0
+    p = cases.params(n, steps, seed, dt=dt, flags=3)
+    k32, _, _ = orc.walk(lat, bases, seqs, p, orc.KERN32, nthreads=os.cpu_count() or 1)
+    np.testing.assert_allclose(a.mx, k32[:, 0], rtol=0, atol=2e-5 * n)
+    np.testing.assert_allclose(a.my, k32[:, 1], rtol=0, atol=2e-5 * n)
+
+
 def test_free_diffusion_exp_minus_bD_full_size(dev):
     """Config: empty periodic 50 um box, 65,536 walkers, dt 5 us, 6,000 steps,
     PGSE delta 5 ms, Delta 20 ms, 16 G values 0-300 mT/m: S = exp(-b D)."""
