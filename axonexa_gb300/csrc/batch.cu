@@ -44,6 +44,7 @@ constexpr int kBatchMaxSeq = 64;  // sequences per job (shared-memory sums)
 struct BatchJob {
   WalkParams P;       // tables point into the batch arena
   int one;            // single-instance path
+  int sph;            // a single pore that is a sphere (else a cylinder)
   int M;
   long long part_off; // first partial (in doubles) of this job's items
   long long out_off;  // first output (in doubles) of this job
@@ -68,7 +69,7 @@ __global__ void __launch_bounds__(AXX_BLOCK, AXX_MIN_BLOCKS_FOR(KMAX))
   double *wsum = reinterpret_cast<double *>(smem + p_bytes);
   unsigned char *geo_base = smem + p_bytes + (size_t)warps * kBatchMaxSeq * 5 * sizeof(double);
   __shared__ int s_item;
-  __shared__ int s_one;
+  __shared__ int s_one, s_sph;
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   int cur = -1;
   TraceParams T{};
@@ -84,7 +85,10 @@ __global__ void __launch_bounds__(AXX_BLOCK, AXX_MIN_BLOCKS_FOR(KMAX))
       const int *src = reinterpret_cast<const int *>(&jobs[item.job].P);
       int *dst = reinterpret_cast<int *>(smem);
       for (int j = threadIdx.x; j < (int)(sizeof(WalkParams) / 4); j += blockDim.x) dst[j] = src[j];
-      if (threadIdx.x == 0) s_one = jobs[item.job].one;
+      if (threadIdx.x == 0) {
+        s_one = jobs[item.job].one;
+        s_sph = jobs[item.job].sph;
+      }
       __syncthreads();
       float4 *sg = reinterpret_cast<float4 *>(geo_base);
       float4 *sa = sg + sP.n_inst;
@@ -135,8 +139,9 @@ __global__ void __launch_bounds__(AXX_BLOCK, AXX_MIN_BLOCKS_FOR(KMAX))
             r = one ? walk_one<AXX_GEOM_MIX, KMAX, AXX_KM_LAT_PERM, false, true>(sP, S, T, wid, W)
                     : walk_one<AXX_GEOM_MIX, KMAX, AXX_KM_LAT_PERM, false, false>(sP, S, T, wid, W);
             break;
-          default:
-            r = walk_one<AXX_GEOM_MIX, KMAX, AXX_KM_SINGLE, false, true>(sP, S, T, wid, W);
+          default:  // a single pore: a cylinder or a sphere, compiled for each
+            r = s_sph ? walk_one<AXX_GEOM_SPH, KMAX, AXX_KM_SINGLE, false, true>(sP, S, T, wid, W)
+                      : walk_one<AXX_GEOM_CYL, KMAX, AXX_KM_SINGLE, false, true>(sP, S, T, wid, W);
             break;
         }
         caps += r.caps;
@@ -579,6 +584,7 @@ static axx_status batch_build(axx_ctx *ctx, const axx_job *jobs, int njobs,
                      ctx->abort_dev);
     hj[j].P.counters = b->d_counters + (size_t)AXX_CNT_N * j;
     hj[j].one = (q.g.geom != AXX_GEOM_FREE && q.g.geo.size() == 1 && q.g.cstart.size() == 2) ? 1 : 0;
+    hj[j].sph = (q.mode == AXX_MODE_SINGLE && q.g.geom == AXX_GEOM_SPH) ? 1 : 0;
     hj[j].M = jobs[j].nseq;
     hj[j].part_off = part_off[j];
     hj[j].out_off = out_off[j];
