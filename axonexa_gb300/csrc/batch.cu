@@ -45,6 +45,7 @@ struct BatchJob {
   WalkParams P;       // tables point into the batch arena
   int one;            // single-instance path
   int sph;            // a single pore that is a sphere (else a cylinder)
+  int cyl;            // a lattice of cylinders along z only
   int M;
   long long part_off; // first partial (in doubles) of this job's items
   long long out_off;  // first output (in doubles) of this job
@@ -69,7 +70,7 @@ __global__ void __launch_bounds__(AXX_BLOCK, AXX_MIN_BLOCKS_FOR(KMAX))
   double *wsum = reinterpret_cast<double *>(smem + p_bytes);
   unsigned char *geo_base = smem + p_bytes + (size_t)warps * kBatchMaxSeq * 5 * sizeof(double);
   __shared__ int s_item;
-  __shared__ int s_one, s_sph;
+  __shared__ int s_one, s_sph, s_cyl;
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   int cur = -1;
   TraceParams T{};
@@ -88,6 +89,7 @@ __global__ void __launch_bounds__(AXX_BLOCK, AXX_MIN_BLOCKS_FOR(KMAX))
       if (threadIdx.x == 0) {
         s_one = jobs[item.job].one;
         s_sph = jobs[item.job].sph;
+        s_cyl = jobs[item.job].cyl;
       }
       __syncthreads();
       float4 *sg = reinterpret_cast<float4 *>(geo_base);
@@ -131,13 +133,17 @@ __global__ void __launch_bounds__(AXX_BLOCK, AXX_MIN_BLOCKS_FOR(KMAX))
       if (active) {
         WalkResult r{0u, 0u, false, false};
         switch (sP.km) {
+          // lattices: the list walk compiled for cylinders when every instance
+          // is one (no per-candidate type tests), else the mixed-type walk
           case AXX_KM_LAT_IMP:
-            r = one ? walk_one<AXX_GEOM_MIX, KMAX, AXX_KM_LAT_IMP, false, true>(sP, S, T, wid, W)
-                    : walk_one<AXX_GEOM_MIX, KMAX, AXX_KM_LAT_IMP, false, false>(sP, S, T, wid, W);
+            r = one     ? walk_one<AXX_GEOM_MIX, KMAX, AXX_KM_LAT_IMP, false, true>(sP, S, T, wid, W)
+                : s_cyl ? walk_one<AXX_GEOM_CYL, KMAX, AXX_KM_LAT_IMP, false, false>(sP, S, T, wid, W)
+                        : walk_one<AXX_GEOM_MIX, KMAX, AXX_KM_LAT_IMP, false, false>(sP, S, T, wid, W);
             break;
           case AXX_KM_LAT_PERM:
-            r = one ? walk_one<AXX_GEOM_MIX, KMAX, AXX_KM_LAT_PERM, false, true>(sP, S, T, wid, W)
-                    : walk_one<AXX_GEOM_MIX, KMAX, AXX_KM_LAT_PERM, false, false>(sP, S, T, wid, W);
+            r = one     ? walk_one<AXX_GEOM_MIX, KMAX, AXX_KM_LAT_PERM, false, true>(sP, S, T, wid, W)
+                : s_cyl ? walk_one<AXX_GEOM_CYL, KMAX, AXX_KM_LAT_PERM, false, false>(sP, S, T, wid, W)
+                        : walk_one<AXX_GEOM_MIX, KMAX, AXX_KM_LAT_PERM, false, false>(sP, S, T, wid, W);
             break;
           default:  // a single pore: a cylinder or a sphere, compiled for each
             r = s_sph ? walk_one<AXX_GEOM_SPH, KMAX, AXX_KM_SINGLE, false, true>(sP, S, T, wid, W)
@@ -585,6 +591,7 @@ static axx_status batch_build(axx_ctx *ctx, const axx_job *jobs, int njobs,
     hj[j].P.counters = b->d_counters + (size_t)AXX_CNT_N * j;
     hj[j].one = (q.g.geom != AXX_GEOM_FREE && q.g.geo.size() == 1 && q.g.cstart.size() == 2) ? 1 : 0;
     hj[j].sph = (q.mode == AXX_MODE_SINGLE && q.g.geom == AXX_GEOM_SPH) ? 1 : 0;
+    hj[j].cyl = (q.mode == AXX_MODE_LATTICE && q.g.geom == AXX_GEOM_CYL) ? 1 : 0;
     hj[j].M = jobs[j].nseq;
     hj[j].part_off = part_off[j];
     hj[j].out_off = out_off[j];
