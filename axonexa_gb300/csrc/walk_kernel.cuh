@@ -735,13 +735,17 @@ __device__ __forceinline__ void do_move(const WalkParams &P, const SmemView &S,
 #pragma unroll
     for (int c = 0; c < KMAX; ++c) wv[c] = __ldg(&wrow[c]);
   }
-#pragma unroll
-  if (DEFER && KMAX > 1 && P.one_dir) {
+  if (KMAX > 1 && P.one_dir) {
     // every channel projects on the same direction (padded channels carry
     // zero waveforms): one projection serves all, the same bits as each
     const float d = project<PAX>(P.ch_p[0], px, py, pz);
 #pragma unroll
-    for (int c = 0; c < KMAX; ++c) W.part[c] = fma_f(wv[c], d, W.part[c]);
+    for (int c = 0; c < KMAX; ++c) {
+      if (DEFER)
+        W.part[c] = fma_f(wv[c], d, W.part[c]);
+      else
+        kahan_add(W.acc[c], W.cmp[c], wv[c] * d);
+    }
   } else {
 #pragma unroll
     for (int c = 0; c < KMAX; ++c) {

@@ -340,6 +340,28 @@ def test_twelve_channel_capacity(dev, orc):
     np.testing.assert_allclose(a.my, k32[:, 1], rtol=0, atol=2e-5 * n)
 
 
+def test_shared_projection_many_channels(dev):
+    """Six waveforms along x (an eight-channel capacity, per-move compensated
+    sums) share one projection; beside a y-gradient sequence the channels no
+    longer share a direction.  The x sequences' sums agree, in a single pore
+    and on a lattice."""
+    import axonexa_gb300 as A
+    lat, bases = cases.one_cylinder()
+    xs = [cases.pgse(100), cases.pgse(80, delta=5.0, Delta=15.0), cases.cos_ogse(80, 1),
+          cases.cos_ogse(80, 2), cases.cos_ogse(60, 2, kind=2), cases.cos_ogse(60, 1, kind=3)]
+    ys = cases.pgse(100, g=(0.0, 1.0, 0.0))
+    L, B, S = to_product(lat, bases, xs)
+    _, _, Sy = to_product(lat, bases, xs + [ys])
+    n, steps, dt, seed = 4096, 2000, 0.002, 5
+    k = len(xs)
+    for run in (lambda q: A.run_lattice(L, B, q, n, steps, dt, seed, relaxation=True, device=dev),
+                lambda q: A.run_single(B[0], q, n, steps, dt, seed, device=dev)):
+        a, b = run(S), run(Sy)
+        np.testing.assert_allclose(a.mx, b.mx[:k], rtol=0, atol=1e-9)
+        np.testing.assert_allclose(a.my, b.my[:k], rtol=0, atol=1e-9)
+        assert a.hits == b.hits and a.hits > 0
+
+
 def test_free_diffusion_exp_minus_bD_full_size(dev):
     """Config: empty periodic 50 um box, 65,536 walkers, dt 5 us, 6,000 steps,
     PGSE delta 5 ms, Delta 20 ms, 16 G values 0-300 mT/m: S = exp(-b D)."""
