@@ -190,7 +190,11 @@ extern "C" axx_status axx_substrate_pack(uint64_t seed, int n, const double *rad
     b.T2 = T2_in;
     b.T1 = 0.0;
     b.permeability = permeability;
-    b.eps = 1e-14 * L;
+    // the reference's initializer default-constructs its cylinders, whose
+    // minimum hit distance is cylEPS = 1e-14 (cylinderXY.cuh:26); a smaller
+    // one lets the reference's expanded quadratic accept the rounding-level
+    // root of the surface a walker was just reflected from
+    b.eps = 1e-14;
     b.nx = b.ny = b.nz = 0.0;
     return true;
   };
