@@ -98,6 +98,8 @@ def test_gamma_packing_statistics():
     for c in cyl:
         orig.setdefault(c.region, c)
     assert len(orig) == 400
+    # the reference's initializer default-constructs its cylinders: cylEPS 1e-14
+    assert all(c.eps == 1e-14 for c in cyl)
     r = np.array([orig[k].radius for k in sorted(orig)])
     x = np.array([orig[k].centerX for k in sorted(orig)])
     y = np.array([orig[k].centerY for k in sorted(orig)])
