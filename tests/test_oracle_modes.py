@@ -32,6 +32,27 @@ def test_kernel_formulation_packs(orc):
         np.testing.assert_array_equal(_events(tr), _events(tk))
 
 
+@pytest.mark.parametrize("name", ["cyl", "hex", "plates_cyl"])
+def test_kernel_formulation_highly_permeable(orc, name):
+    """kappa 0.01 mm/ms: a transmission every few hits, thousands of region
+    changes.  The kernel formulation looks the region up only after a
+    transmission or a wrap; the reference after every move; the events agree
+    move for move."""
+    kappa = 1e-2
+    if name == "cyl":
+        lat, bases = cases.one_cylinder(D_in=1.7e-6, kappa=kappa)
+    elif name == "hex":
+        lat, bases = cases.hex_cylinders(kappa=kappa)
+    else:
+        lat, bases = cases.parallel_plates(with_cylinder=True)
+        bases[2].permeability = kappa
+    p = cases.params(64, 2000, 13, dt=0.002, flags=3)
+    _, tr, _ = orc.walk(lat, bases, [], p, orc.REF64, ntrace=64)
+    _, tk, _ = orc.walk(lat, bases, [], p, orc.KERN64, ntrace=64)
+    np.testing.assert_array_equal(_events(tr), _events(tk))
+    assert (np.diff(tr["region"], axis=1) != 0).sum() > 500
+
+
 def test_kernel_formulation_dense_permeable_pack(orc):
     """The 100-cylinder gamma packing at area fraction 0.6, permeable: the
     kernel formulation keeps a walker's region between transmissions and
