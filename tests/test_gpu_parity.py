@@ -59,6 +59,7 @@ LATTICE_CASES = [
     ("cyl_perm", lambda: cases.one_cylinder(D_in=1.7e-6, kappa=5e-5), 3, 0.002),
     ("cyl_reject", lambda: cases.one_cylinder(), 5, 0.002),
     ("hex_perm", lambda: cases.hex_cylinders(kappa=2e-5), 3, 0.001),
+    ("hex_perm_high", lambda: cases.hex_cylinders(kappa=1e-2), 3, 0.001),
     ("spheres", lambda: cases.sphere_lattice(), 1, 0.002),
     ("gamma_perm", lambda: cases.gamma_packing(), 3, 0.001),
     ("plates", lambda: cases.parallel_plates(), 1, 0.002),
