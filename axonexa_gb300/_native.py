@@ -131,7 +131,9 @@ _SIGS = {
                        C.POINTER(Stats)], C.c_int),
     "axx_plan_info": ([C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
                        C.POINTER(C.c_int64)], C.c_int),
+    "axx_plan_candidates": ([C.c_void_p, C.POINTER(C.c_double)], C.c_int),
     "axx_plan_destroy": ([C.c_void_p], C.c_int),
+    "axx_transfer_bytes": ([C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)], C.c_int),
     "axx_event_record": ([C.c_void_p, C.c_int], C.c_int),
     "axx_event_elapsed": ([C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_float)], C.c_int),
     "axx_sync": ([C.c_void_p], C.c_int),

@@ -539,10 +539,14 @@ def linear_regression(y, x) -> float:
     if len(y) != len(x):
         raise ValueError("linear_regression: y.size != x.size")
     n = float(len(y))
-    t2 = sum(a * b for a, b in zip(x, y))
-    t3 = sum(x)
-    t4 = sum(y)
-    t5 = sum(a * a for a in x)
+    # plain left-to-right sums, as the reference's loop (Python's sum() of
+    # floats is compensated and would round differently)
+    t2 = t3 = t4 = t5 = 0.0
+    for a, b in zip(x, y):
+        t2 = t2 + a * b
+        t3 = t3 + a
+        t4 = t4 + b
+        t5 = t5 + a * a
     delta = n * t5 - t3 * t3
     return (1.0 / delta) * (n * t2 - t3 * t4)
 
@@ -592,7 +596,7 @@ class phaseAcquisition:
         """ADC from ln|M| against b with running mean over repeats (:54-77)."""
         self.points += 1
         b = [f.getB() for f in self.gradientFunctors]
-        ln = [math.log(math.sqrt(self.mx[i] ** 2 + self.my[i] ** 2))
+        ln = [math.log(math.sqrt(self.mx[i] * self.mx[i] + self.my[i] * self.my[i]))
               for i in range(self.numOfMeasurements)]
         adc = -1.0 * linear_regression(ln, b)
         if self.points == 1:

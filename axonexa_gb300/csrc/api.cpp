@@ -34,6 +34,9 @@ struct axx_plan {
   int Mo = 0;  // rows of sums: M, or 2M with the start-compartment sums
   size_t smem = 0;
   size_t upload_bytes = 0;
+  // boundary candidates a move tests, averaged over the cell (walkers are
+  // uniform in it): the cell lists' entries per grid cell
+  double cand_per_move = 0.0;
   void *arena = nullptr;
   double *out = nullptr;  // [M*5]
   unsigned long long *counters = nullptr;
@@ -136,6 +139,10 @@ axx_status build_plan(axx_ctx *ctx, const GeomPlan &g, const SeqPlan &sq, int M,
     delete pl;
     return cuda_fail(ctx, e, "uploading the plan tables");
   }
+  ctx->h2d_bytes += L.upload;
+  pl->cand_per_move = g.geom == AXX_GEOM_FREE || g.cstart.size() < 2
+                          ? 0.0
+                          : (double)g.cstart.back() / (double)(g.cstart.size() - 1);
   fill_walk_params(pl->P, base, L, g, kt, p, mode, M, init, cell, ctx->abort_dev);
   pl->P.global_tables = global_tables ? 1 : 0;
   pl->out = (double *)(base + L.o_out);
@@ -204,6 +211,7 @@ axx_status read_results(axx_plan *pl, double *mx, double *my, axx_stats *stats) 
   if (pl->Mo > 0)
     AXX_CUDA(ctx, cudaMemcpy(h.data(), pl->out, h.size() * 8, cudaMemcpyDeviceToHost));
   AXX_CUDA(ctx, cudaMemcpy(cnt, pl->counters, sizeof(cnt), cudaMemcpyDeviceToHost));
+  ctx->d2h_bytes += (pl->Mo > 0 ? h.size() * 8 : 0) + sizeof(cnt);
   for (int m = 0; m < pl->M; ++m) {
     if (mx) mx[m] = h[m * 5 + 0];
     if (my) my[m] = h[m * 5 + 1];
@@ -364,6 +372,19 @@ axx_status axx_plan_info(const axx_plan *pl, int *channels, int *instances, int 
   if (instances) *instances = pl->n_inst;
   if (kernel_launches) *kernel_launches = 2;
   if (walker_steps) *walker_steps = pl->walker_steps;
+  return AXX_OK;
+}
+
+axx_status axx_plan_candidates(const axx_plan *pl, double *per_move) {
+  if (!pl || !per_move) return AXX_ERR_INVALID_ARG;
+  *per_move = pl->cand_per_move;
+  return AXX_OK;
+}
+
+axx_status axx_transfer_bytes(axx_ctx *ctx, int64_t *h2d, int64_t *d2h) {
+  if (!ctx) return AXX_ERR_INVALID_ARG;
+  if (h2d) *h2d = (int64_t)ctx->h2d_bytes;
+  if (d2h) *d2h = (int64_t)ctx->d2h_bytes;
   return AXX_OK;
 }
 

@@ -13,4 +13,7 @@ struct axx_ctx {
   size_t gmem = 0;
   volatile int *abort_host = nullptr;
   int *abort_dev = nullptr;
+  // bytes the walk entry points copied between host and device on this
+  // context (plan tables up, sums and counters down)
+  unsigned long long h2d_bytes = 0, d2h_bytes = 0;
 };

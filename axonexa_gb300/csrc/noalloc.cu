@@ -11,16 +11,24 @@
 // is part of the library image.  Nothing is allocated on the device; the
 // host-side planning uses ordinary host memory.
 //
-// Every GPU that loads this library holds the array until the process exits.
-// Host code cannot use g_scratch's name as a device address: the address is
-// obtained once per device with cudaGetSymbolAddress (with that device
-// current) on the first call on that device, so that first call should come
-// before any stream capture.  All calls on a device share the array and it
-// keeps the previous call's contents: the counters are cleared at the start
-// of every call, everything else is fully rewritten.  Calls whose work
-// overlaps on the GPU (two host threads, or two contexts on one device) race
-// on the array and must be serialised by the caller.
+// Every GPU that loads this library holds the array until the process exits
+// (with lazy module loading the memory is committed when the module first
+// loads on that device: at the first call, or at any earlier use of the
+// library's kernels).  Host code cannot use g_scratch's name as a device
+// address: the address is looked up with cudaGetSymbolAddress, with the
+// device current, at the first call in each device context, so that first
+// call should come before any stream capture.  A device reset (by the
+// caller or by another library) destroys the context and reloads the module,
+// which may move the array; the lookup is keyed on the context's id, which
+// CUDA never reuses, so the first call after a reset looks the address up
+// again.  All calls on a device share the array and it keeps the previous
+// call's contents: the counters are cleared at the start of every call,
+// everything else is fully rewritten.  Calls whose work overlaps on the GPU
+// (two host threads, or two contexts on one device) race on the array and
+// must be serialised by the caller.
+#include <cuda.h>
 #include <cuda_runtime.h>
+#include <cudaTypedefs.h>
 
 #include <algorithm>
 #include <cmath>
@@ -45,19 +53,52 @@ static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
 
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
-void *g_addr[kMaxDevices] = {};
+struct ScratchAddr {
+  unsigned long long ctx_id = 0;  // 0: not looked up yet
+  void *addr = nullptr;
+};
+ScratchAddr g_addr[kMaxDevices];
 
-// Device address of g_scratch on `device` (current on the calling thread).
+// Id of the context current on this thread (cuCtxGetId, reached through the
+// runtime's driver entry points so that the library does not link libcuda).
+cudaError_t current_context_id(unsigned long long *id) {
+  static PFN_cuCtxGetCurrent_v4000 get_current = nullptr;
+  static PFN_cuCtxGetId_v12000 get_id = nullptr;
+  if (!get_current || !get_id) {
+    cudaDriverEntryPointQueryResult q1, q2;
+    void *f1 = nullptr, *f2 = nullptr;
+    cudaError_t e = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 4000,
+                                                     cudaEnableDefault, &q1);
+    if (e == cudaSuccess)
+      e = cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2);
+    if (e != cudaSuccess) return e;
+    if (q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+      return cudaErrorNotSupported;
+    get_current = (PFN_cuCtxGetCurrent_v4000)f1;
+    get_id = (PFN_cuCtxGetId_v12000)f2;
+  }
+  CUcontext c = nullptr;
+  if (get_current(&c) != CUDA_SUCCESS || !c) return cudaErrorInvalidResourceHandle;
+  if (get_id(c, id) != CUDA_SUCCESS) return cudaErrorInvalidResourceHandle;
+  return cudaSuccess;
+}
+
+// Device address of g_scratch on `device` (current on the calling thread),
+// looked up once per device context.
 cudaError_t scratch_address(int device, void **out) {
   if (device < 0 || device >= kMaxDevices) return cudaErrorInvalidDevice;
   std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_addr[device]) {
+  unsigned long long id = 0;
+  cudaError_t e = current_context_id(&id);
+  if (e != cudaSuccess) return e;
+  if (g_addr[device].ctx_id != id) {
     void *p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
+    e = cudaGetSymbolAddress(&p, g_scratch);
     if (e != cudaSuccess) return e;
-    g_addr[device] = p;
+    g_addr[device].addr = p;
+    g_addr[device].ctx_id = id;
   }
-  *out = g_addr[device];
+  *out = g_addr[device].addr;
   return cudaSuccess;
 }
 
@@ -143,6 +184,7 @@ extern "C" axx_status axx_run_lattice_noalloc(axx_ctx *ctx, const axx_lattice *l
   cudaStream_t s = ctx->stream;
   e = upload_tables(base, Lo, g, kt, s);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMemcpyAsync(no-allocation tables)");
+  ctx->h2d_bytes += Lo.upload;
   // counters start at zero on every call (the array keeps the last call's values)
   e = cudaMemsetAsync(base + Lo.o_cnt, 0, AXX_CNT_N * 8, s);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMemsetAsync(counters)");
@@ -164,6 +206,7 @@ extern "C" axx_status axx_run_lattice_noalloc(axx_ctx *ctx, const axx_lattice *l
   if (e == cudaSuccess) e = cudaMemcpyAsync(cnt, base + o_cnt, sizeof(cnt), cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "reading the no-allocation results");
+  ctx->d2h_bytes += (Mo > 0 ? h.size() * 8 : 0) + sizeof(cnt);
   for (int m = 0; m < M; ++m) {
     if (mx) mx[m] = h[m * 5 + 0];
     if (my) my[m] = h[m * 5 + 1];

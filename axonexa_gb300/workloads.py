@@ -223,13 +223,11 @@ def main(argv=None):
     ap.add_argument("--steps", type=int, default=0, help="cut every walk to this many steps")
     ap.add_argument("--walkers", type=int, default=0)
     ap.add_argument("--reps", type=int, default=3)
-    ap.add_argument("--cpu-sample", type=int, default=0,
-                    help="mag_lowfield: also time the CPU oracle on this many walkers")
     ap.add_argument("--walker-scale", type=float, default=0.25,
                     help="batch_256: scale of every job's walker count")
     a = ap.parse_args(argv)
     if a.workload == "mag_lowfield":
-        print(json.dumps(measure_mag(a.walkers, a.steps, a.reps, a.cpu_sample)))
+        print(json.dumps(measure_mag(a.walkers, a.steps, a.reps)))
     elif a.workload == "wc_sphere":
         print(json.dumps(measure_wc(a.walkers or 32768, a.steps or 22000, a.reps)))
     elif a.workload == "mesh_sphere":
@@ -255,12 +253,9 @@ def mag_lowfield(n_fields=16, walkers=57344, gd=1.0, gs=1.0):
                 timestep=0.001, gamma=-203789.0, seed=1234)
 
 
-def measure_mag(walkers: int = 0, steps: int = 0, reps: int = 3, cpu_sample: int = 0,
-                device=None) -> dict:
+def measure_mag(walkers: int = 0, steps: int = 0, reps: int = 3, device=None) -> dict:
     """Walker-steps/s of the magnetisation walk (axx_run_mag, host records in,
-    host sums out, best of reps after one warm-up), and optionally the CPU
-    oracle's reference-order walk on a bounded walker sample."""
-    import os
+    host sums out, best of reps after one warm-up)."""
     import time
 
     from .magnetization import run_mag
@@ -280,19 +275,6 @@ def measure_mag(walkers: int = 0, steps: int = 0, reps: int = 3, cpu_sample: int
            "seconds": best, "walker_steps_per_s": ws / best,
            "field_updates_per_s": n * st * len(w["fields"]) / best,
            "signal": [float(x) for x in r.signal]}
-    if cpu_sample:
-        from oracle import oracle as O
-        O.lib()
-        pore = O.Basis(0, 0, 0.0, 0.0, 0.0, 24.2, 20.0, 0.0, 0.0, 0.0, 1e-14)
-        F = [O.Field(0, 0, f.B0, f.G, 0, 0, 0, f.gradientDuration, f.gradientSpacing, 0, 0, 0, 0,
-                     0, 0) for f in w["fields"]]
-        p = O.mag_params(cpu_sample, st, w["seed"], w["timestep"], gamma=w["gamma"])
-        th = os.cpu_count() or 1
-        t0 = time.perf_counter()
-        O.mag_walk(pore, F, p, nthreads=th)
-        tc = time.perf_counter() - t0
-        out["cpu_oracle"] = {"walker_steps_per_s": cpu_sample * (st - 1) / tc, "cores": th,
-                             "sample_walkers": cpu_sample, "seconds": tc}
     return out
 
 

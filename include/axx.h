@@ -222,12 +222,19 @@ axx_status axx_run_single(axx_ctx *ctx, const axx_basis *basis, const axx_sequen
  * reference: it exists for callers that cannot call cudaMalloc when they run
  * a walk (a memory pool or budget that owns all device memory, a framework
  * that forbids allocation after start-up, a thread that must not trigger the
- * synchronisation cudaMalloc/cudaFree can cause).  Same inputs, outputs and
- * results as axx_run_lattice; every device-side buffer of the call lives in
- * one static array of AXX_NOALLOC_SCRATCH_BYTES that each GPU loading the
- * library holds until the process exits.  A walk whose tables and per-block
- * partials do not fit is rejected with AXX_ERR_INVALID_ARG.  The first call on
- * a device looks up the array's device address, so make it before any stream
+ * synchronisation cudaMalloc/cudaFree can cause).  Same inputs and outputs as
+ * axx_run_lattice and the same kernels; every device-side buffer of the call
+ * lives in one static array of AXX_NOALLOC_SCRATCH_BYTES that each GPU
+ * loading the library holds until the process exits (with lazy module
+ * loading it is committed when the module first loads on the device: at the
+ * first call, or at any earlier use of the library's kernels).  A walk whose
+ * tables and per-block partials do not fit even one block per SM is rejected
+ * with AXX_ERR_INVALID_ARG; when the partials of the full grid do not fit,
+ * the grid shrinks, and the results then equal axx_run_lattice's up to the
+ * grouping of the per-block FP64 partial sums (rounding only).  The call is
+ * synchronous: it returns after the results are on the host.  The array's
+ * device address is looked up at the first call in each device context (and
+ * again after a device reset), so make the first call before any stream
  * capture.  All calls on a device share the array: calls whose GPU work
  * overlaps race and must be serialised by the caller.  The context must have
  * been created beforehand (axx_create). */
@@ -255,7 +262,20 @@ axx_status axx_plan_read(axx_plan *plan, double *mx, double *my, axx_stats *stat
  * kernel_launches = kernels one axx_plan_launch enqueues. */
 axx_status axx_plan_info(const axx_plan *plan, int *channels, int *instances,
                          int *kernel_launches, int64_t *walker_steps);
+/* Boundary candidates one move tests, averaged over the cell: the entries of
+ * the grid-cell lists per cell (walkers are uniform in the cell), 1 for a
+ * single pore, 0 for free diffusion.  The n_cand of the walk's op count;
+ * the reference tests every basis each move (Lattice::intersectionCheck*,
+ * src/substrate/lattice.cuh:184-246). */
+axx_status axx_plan_candidates(const axx_plan *plan, double *per_move);
 axx_status axx_plan_destroy(axx_plan *plan);
+
+/* Bytes the walk entry points (plans and one-shot runs) copied host to
+ * device (tables) and device to host (sums, counters) on this context since
+ * it was created: what an end-to-end call moves across the host link.  The
+ * reference copies the per-walker phases instead
+ * (src/acquisition/phaseAcquisitionStream.cuh:139-189). */
+axx_status axx_transfer_bytes(axx_ctx *ctx, int64_t *h2d_bytes, int64_t *d2h_bytes);
 
 /* Timing on the context stream: record event `slot` (0..7), and read the
  * elapsed milliseconds between two recorded slots after a sync. */

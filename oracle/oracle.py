@@ -15,7 +15,11 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liboracle.so")
 REFLIB = os.path.join(HERE, "_ref", "libaxxref.so")
-REF_SRC = "/root/reference"
+REFLIB_ACQ = os.path.join(HERE, "_ref", "libaxxref_acq.so")
+# The reference's source tree (for building its walker for the host): the
+# AXX_REFERENCE_SRC environment variable, or the path given to build().
+REF_SRC = os.environ.get("AXX_REFERENCE_SRC", "")
+REF_SRC_RECORD = os.path.join(HERE, "_ref", "ref_src.txt")
 
 REF64, KERN64, KERN32 = 0, 1, 2
 REF_VARIANTS = ("spec_imp", "spec_imp_t2", "spec_perm", "spec_perm_t2", "rej", "rej_t2",
@@ -54,11 +58,27 @@ class Trace(C.Structure):
                 ("hits", C.POINTER(C.c_int32)), ("words", C.POINTER(C.c_int32))]
 
 
-def build(ref: bool = True) -> None:
-    """Builds liboracle.so, and _ref/libaxxref.so when the reference tree exists."""
+def build(ref: bool = True, ref_src: str = None) -> None:
+    """Builds liboracle.so, and _ref/libaxxref.so + _ref/libaxxref_acq.so when
+    the reference tree (`ref_src`, else AXX_REFERENCE_SRC) exists."""
     subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
-    if ref and os.path.isdir(os.path.join(REF_SRC, "src")):
-        subprocess.run(["make", "-s", "-j8", "-C", HERE, "ref", "REF=" + REF_SRC], check=True)
+    src = ref_src or REF_SRC
+    if ref and src and os.path.isdir(os.path.join(src, "src")):
+        subprocess.run(["make", "-s", "-j8", "-C", HERE, "ref", "REF=" + src], check=True)
+        with open(REF_SRC_RECORD, "w") as f:
+            f.write(os.path.abspath(src))
+
+
+def reference_src():
+    """The reference source tree _ref/ was built from, or None."""
+    if REF_SRC and os.path.isdir(os.path.join(REF_SRC, "src")):
+        return REF_SRC
+    try:
+        with open(REF_SRC_RECORD) as f:
+            p = f.read().strip()
+    except OSError:
+        return None
+    return p if os.path.isdir(os.path.join(p, "src")) else None
 
 
 _lib = None
@@ -83,6 +103,22 @@ def reflib():
     if _ref is None and os.path.exists(REFLIB):
         _ref = C.CDLL(REFLIB)
     return _ref
+
+
+_ref_acq = None
+
+
+def reflib_acq():
+    """The reference's acquisition post-processing (linear_regression,
+    phaseAcquisition::calcADC), or None when it was not built here."""
+    global _ref_acq
+    if _ref_acq is None and os.path.exists(REFLIB_ACQ):
+        L = C.CDLL(REFLIB_ACQ)
+        L.ref_linear_regression.restype = C.c_double
+        L.ref_linear_regression.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int]
+        L.ref_calc_adc.restype = C.c_int
+        _ref_acq = L
+    return _ref_acq
 
 
 def _arr(seq, cls):
