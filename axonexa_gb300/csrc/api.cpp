@@ -32,6 +32,7 @@ struct axx_plan {
   WalkParams P{};
   int geom = 0, km = 0, kmax = 1, grid = 0, M = 0, K = 0, n_inst = 0;
   int Mo = 0;  // rows of sums: M, or 2M with the start-compartment sums
+  bool rows = false;  // partials per warp instead of per block
   size_t smem = 0;
   size_t upload_bytes = 0;
   // boundary candidates a move tests, averaged over the cell (walkers are
@@ -90,10 +91,12 @@ axx_status build_plan(axx_ctx *ctx, const GeomPlan &g, const SeqPlan &sq, int M,
   if ((p->flags & AXX_FLAG_COMPARTMENTS) && mode != AXX_MODE_LATTICE)
     return fail(ctx, AXX_ERR_INVALID_ARG, "compartment sums exist for lattice walks only");
   const int Mo = (p->flags & AXX_FLAG_COMPARTMENTS) ? 2 * M : M;
-  // tables that do not fit the shared-memory budget are read from global
-  // memory (instantiations with 16 channels); only the per-warp sums stay in
-  // shared memory
-  const bool global_tables = walk_smem_bytes(g, Mo) > AXX_SMEM_MAX;
+  // the sums go to per-warp rows of the partials in global memory, which
+  // leaves the shared memory to the substrate tables; tables that do not fit
+  // the shared-memory budget are read from global memory (instantiations with
+  // 16 channels)
+  const bool rows = true;
+  const bool global_tables = walk_smem_bytes(g, Mo, rows) > AXX_SMEM_MAX;
   KernelTables kt;
   std::string err =
       make_kernel_tables(g, sq, M, p->steps, mode, p->flags, kt, global_tables ? AXX_KMAX : 1);
@@ -101,7 +104,7 @@ axx_status build_plan(axx_ctx *ctx, const GeomPlan &g, const SeqPlan &sq, int M,
   InitSpec init;
   err = init_spec(g, basis, nbasis, mode, p, init);
   if (!err.empty()) return fail(ctx, AXX_ERR_INVALID_ARG, err);
-  const size_t smem = global_tables ? walk_sums_bytes(Mo) : walk_smem_bytes(g, Mo);
+  const size_t smem = global_tables ? walk_sums_bytes(Mo, rows) : walk_smem_bytes(g, Mo, rows);
   if (smem > AXX_SMEM_MAX)
     return fail(ctx, AXX_ERR_UNSUPPORTED,
                 "the sequence sums exceed the shared-memory budget (" + std::to_string(smem) +
@@ -124,7 +127,8 @@ axx_status build_plan(axx_ctx *ctx, const GeomPlan &g, const SeqPlan &sq, int M,
   const long long ntask = (p->num_walkers + 31) / 32;
   const long long want = (ntask + AXX_BLOCK / 32 - 1) / (AXX_BLOCK / 32);
   pl->grid = (int)std::min<long long>(want, (long long)occ * ctx->nsm);
-  const ArenaLayout L = arena_layout(g, kt, Mo);
+  pl->rows = rows;
+  const ArenaLayout L = arena_layout(g, kt, Mo, rows);
   pl->upload_bytes = L.upload;
   cudaError_t e = cudaMalloc(&pl->arena, L.fixed + L.per_block * pl->grid);
   if (e != cudaSuccess) {
@@ -143,7 +147,7 @@ axx_status build_plan(axx_ctx *ctx, const GeomPlan &g, const SeqPlan &sq, int M,
   pl->cand_per_move = g.geom == AXX_GEOM_FREE || g.cstart.size() < 2
                           ? 0.0
                           : (double)g.cstart.back() / (double)(g.cstart.size() - 1);
-  fill_walk_params(pl->P, base, L, g, kt, p, mode, M, init, cell, ctx->abort_dev);
+  fill_walk_params(pl->P, base, L, g, kt, p, mode, M, init, cell, ctx->abort_dev, rows);
   pl->P.global_tables = global_tables ? 1 : 0;
   pl->out = (double *)(base + L.o_out);
   pl->counters = pl->P.counters;
@@ -168,10 +172,11 @@ axx_status make_lattice_plan(axx_ctx *ctx, const axx_lattice *lat, const axx_bas
   Frame fr;
   std::string e = frame_lattice(lat, basis, nbasis, seqs, nseq, fr);
   if (!e.empty()) return fail(ctx, AXX_ERR_INVALID_ARG, e);
-  e = plan_lattice(fr.lat_p, fr.basis_p, nbasis, params->timestep, params->flags, g);
-  if (!e.empty()) return fail(ctx, AXX_ERR_INVALID_ARG, e);
   SeqPlan sq;
   e = plan_sequences(fr.seqs_p, nseq, params->steps, params->timestep, gamma, sq);
+  if (!e.empty()) return fail(ctx, AXX_ERR_INVALID_ARG, e);
+  e = plan_lattice(fr.lat_p, fr.basis_p, nbasis, params->timestep, params->flags, g,
+                   list_table_budget((int)sq.channels.size()));
   if (!e.empty()) return fail(ctx, AXX_ERR_INVALID_ARG, e);
   const double cell[3] = {fr.lat_p->a, fr.lat_p->b, fr.lat_p->c};
   s = build_plan(ctx, g, sq, nseq, params, AXX_MODE_LATTICE, fr.basis_p, nbasis, cell, out);
@@ -354,7 +359,8 @@ axx_status axx_plan_launch(axx_plan *pl) {
   TraceParams T{};
   AXX_CUDA(ctx, launch_walk(pl->geom, pl->km, pl->kmax, false, pl->P, T, pl->grid, pl->smem,
                             ctx->stream));
-  AXX_CUDA(ctx, launch_reduce_partials(pl->P.partials, pl->grid, pl->Mo * 5, pl->out, ctx->stream));
+  const int nrows = pl->grid * (pl->rows ? AXX_BLOCK / 32 : 1);
+  AXX_CUDA(ctx, launch_reduce_partials(pl->P.partials, nrows, pl->Mo * 5, pl->out, ctx->stream));
   pl->launched = true;
   return AXX_OK;
 }
@@ -505,7 +511,8 @@ static axx_status run_trace(axx_ctx *ctx, axx_plan *pl, int ntrace, float *init_
   b += align256(nrec * 4);
   T.words = (int32_t *)b;
   cudaError_t e = cudaMemsetAsync(pl->counters, 0, AXX_CNT_N * 8, ctx->stream);
-  const int grid = (ntrace + AXX_BLOCK - 1) / AXX_BLOCK;
+  // the plan's grid (its partial rows); warps stride over the walkers
+  const int grid = std::min(pl->grid, (ntrace + AXX_BLOCK - 1) / AXX_BLOCK);
   if (e == cudaSuccess)
     e = launch_walk(pl->geom, pl->km, 1, true, pl->P, T, grid, pl->smem, ctx->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);

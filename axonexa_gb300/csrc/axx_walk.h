@@ -12,10 +12,13 @@
 //                      slot is the extracellular space
 //   wave_il[steps*KMAX] FP32 unit waveform of each phase channel, step-major
 //                      (one row of KMAX values per step; padded channels 0)
+//   wave4[steps]       float4: axis-channel plans (channel 3w + a is waveform
+//                      w along axis a, w < 4): the four waveforms per step
 //   coef[M*KMAX]       FP64 gamma*dt*G_m*alpha_mc: phase of sequence m from
 //                      the channel accumulators (0 for padded channels)
-//   partials[grid*Mo*5] FP64 per-block sums (x, y, x^2, y^2, xy) of the Mo = M
-//                      rows (2M with compartment sums), scratch
+//   partials[rows*Mo*5] FP64 sums (x, y, x^2, y^2, xy) of the Mo = M rows (2M
+//                      with compartment sums), one row set per block, or per
+//                      warp (warp_rows: the shared memory holds no sums), scratch
 #pragma once
 #include <stdint.h>
 
@@ -77,12 +80,15 @@ struct WalkParams {
   float init_R, init_cx, init_cy, init_cz;
   int K, kmax;                // channels in use, channel capacity (padded)
   const float *wave_il;       // [steps][kmax]
+  const float4 *wave4;        // axis channels: [steps] the four waveforms' values
   float ch_p[AXX_KMAX][3];    // channel projections (0 for padded channels)
   int one_dir;                // every channel in use has the same projection
   int phase_axes;             // axes some channel projects on (bits x, y, z)
+  int axis_channels;          // channel 3w + a is waveform w along axis a (w < 4)
   int M;
   int compart;                // also sums over walkers starting in a basis: rows M..2M-1
   int global_tables;          // substrate tables read from global memory (too big to stage)
+  int warp_rows;              // partials: one row per warp (gwarp) instead of per block
   const double *coef;         // [M][kmax]
   double *partials;
   unsigned long long *counters;

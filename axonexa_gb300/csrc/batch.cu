@@ -491,7 +491,7 @@ static axx_status batch_build(axx_ctx *ctx, const axx_job *jobs, int njobs,
                                          q.kt, kmax);
     if (err.empty()) err = init_spec(q.g, q.f.basis_p, jobs[j].nbasis, q.mode, &q.p, q.init);
     if (!err.empty()) return bfail(ctx, AXX_ERR_INVALID_ARG, "job " + std::to_string(j) + ": " + err);
-    geo_max = std::max(geo_max, walk_smem_bytes(q.g, 0));
+    geo_max = std::max(geo_max, batch_table_bytes(q.g));
     job_off[j] = off;
     off = up256(off + arena_layout(q.g, q.kt, jobs[j].nseq).fixed);
   }

@@ -243,8 +243,96 @@ static float4 aux_of(const axx_basis &b, int slot) {
   return a;
 }
 
+// One basis instance (a basis or a periodic ghost of it) during planning.
+struct Inst {
+  int k;
+  double cx, cy, cz, R;
+  int type;
+  double n[3];  // unit normal of a plane
+};
+
+// A plane meets a box when the signed distances n.(x - c) of the box's
+// corners do not all have one sign.
+static bool plane_meets(const Inst &q, double x0, double x1, double y0, double y1, double z0,
+                        double z1) {
+  double lo = 0.0, hi = 0.0;
+  const double xs[2] = {x0, x1}, ys[2] = {y0, y1}, zs[2] = {z0, z1};
+  for (int i = 0; i < 8; ++i) {
+    const double d = q.n[0] * (xs[i & 1] - q.cx) + q.n[1] * (ys[(i >> 1) & 1] - q.cy) +
+                     q.n[2] * (zs[i >> 2] - q.cz);
+    lo = i ? std::min(lo, d) : d;
+    hi = i ? std::max(hi, d) : d;
+  }
+  return lo <= 0.0 && hi >= 0.0;
+}
+
+// Uniform gx x gy x gz grid over the a x b x c cell: per grid cell, the
+// instances that can be met from inside it within one step (the cell box
+// dilated by dil, plus a slack for the FP32 rounding of the cell index), in
+// ascending instance (basis) order.  The outer cells reach beyond the cell
+// edge (positions are clamped into the grid).  Each instance is tested only
+// against the cells its dilated bounding box can reach.
+static void build_grid(GeomPlan &g, const std::vector<Inst> &inst, double A, double B, double C,
+                       double dil, int gx, int gy, int gz) {
+  g.gx = gx;
+  g.gy = gy;
+  g.gz = gz;
+  g.inv_hx = (float)((double)gx / A);
+  g.inv_hy = (float)((double)gy / B);
+  g.inv_hz = (float)((double)gz / C);
+  const int ncell = gx * gy * gz;
+  const double sx = 1e-5 * A / gx, sy = 1e-5 * B / gy, sz = 1e-5 * C / gz;
+  auto lo_of = [](int i, double side, int n) { return i == 0 ? -1e300 : side * i / n; };
+  auto hi_of = [](int i, double side, int n) { return i == n - 1 ? 1e300 : side * (i + 1) / n; };
+  auto range = [](double lo, double hi, double side, int n, int &i0, int &i1) {
+    const double hh = side / n;
+    i0 = (int)std::max(0.0, std::min((double)n - 1, std::floor(lo / hh) - 1));
+    i1 = (int)std::max(0.0, std::min((double)n - 1, std::floor(hi / hh) + 1));
+  };
+  std::vector<std::vector<uint16_t>> lists(ncell);
+  for (size_t n = 0; n < inst.size(); ++n) {
+    const Inst &q = inst[n];
+    int x0 = 0, x1 = gx - 1, y0 = 0, y1 = gy - 1, z0 = 0, z1 = gz - 1;
+    if (q.type != AXX_PRIM_PLANE) {
+      const double r = q.R + dil;
+      range(q.cx - r, q.cx + r, A, gx, x0, x1);
+      range(q.cy - r, q.cy + r, B, gy, y0, y1);
+      if (q.type == AXX_PRIM_SPHERE) range(q.cz - r, q.cz + r, C, gz, z0, z1);
+    }
+    for (int iz = z0; iz <= z1; ++iz)
+      for (int iy = y0; iy <= y1; ++iy)
+        for (int ix = x0; ix <= x1; ++ix) {
+          const double bx0 = lo_of(ix, A, gx) - dil - sx, bx1 = hi_of(ix, A, gx) + dil + sx;
+          const double by0 = lo_of(iy, B, gy) - dil - sy, by1 = hi_of(iy, B, gy) + dil + sy;
+          const double bz0 = lo_of(iz, C, gz) - dil - sz, bz1 = hi_of(iz, C, gz) + dil + sz;
+          bool meets;
+          if (q.type == AXX_PRIM_PLANE) {
+            meets = plane_meets(q, bx0, bx1, by0, by1, bz0, bz1);
+          } else {
+            auto axis = [](double c, double lo, double hi) {
+              return c < lo ? lo - c : (c > hi ? c - hi : 0.0);
+            };
+            const double ex = axis(q.cx, bx0, bx1), ey = axis(q.cy, by0, by1);
+            double d2 = ex * ex + ey * ey;
+            if (q.type == AXX_PRIM_SPHERE) {
+              const double ez = axis(q.cz, bz0, bz1);
+              d2 += ez * ez;
+            }
+            meets = d2 < q.R * q.R;
+          }
+          if (meets) lists[(iz * gy + iy) * gx + ix].push_back((uint16_t)n);
+        }
+  }
+  g.cstart.assign(ncell + 1, 0);
+  g.clist.clear();
+  for (int c = 0; c < ncell; ++c) {
+    g.clist.insert(g.clist.end(), lists[c].begin(), lists[c].end());
+    g.cstart[c + 1] = (uint32_t)g.clist.size();
+  }
+}
+
 std::string plan_lattice(const axx_lattice *lat, const axx_basis *basis, int nbasis, double dt,
-                         uint32_t flags, GeomPlan &g) {
+                         uint32_t flags, GeomPlan &g, size_t list_budget) {
   g = GeomPlan();
   if (!lat) return "lattice is NULL";
   if (!(lat->a > 0.0) || !(lat->b > 0.0) || !(lat->c > 0.0)) return "cell sides must be > 0";
@@ -301,27 +389,7 @@ std::string plan_lattice(const axx_lattice *lat, const axx_basis *basis, int nba
   // the cell within one step and do not coincide with a listed basis
   const double dil = (double)lmax * 1.01 + 1e-7 * std::max(A, std::max(B, C));
   const double tol = 1e-9 * std::max(A, std::max(B, C));
-  struct Inst {
-    int k;
-    double cx, cy, cz, R;
-    int type;
-    double n[3];  // unit normal of a plane
-  };
   std::vector<Inst> inst;
-  // a plane meets a box when the signed distances n.(x - c) of the box's
-  // corners do not all have one sign
-  auto plane_meets = [](const Inst &q, double x0, double x1, double y0, double y1, double z0,
-                        double z1) {
-    double lo = 0.0, hi = 0.0;
-    const double xs[2] = {x0, x1}, ys[2] = {y0, y1}, zs[2] = {z0, z1};
-    for (int i = 0; i < 8; ++i) {
-      const double d = q.n[0] * (xs[i & 1] - q.cx) + q.n[1] * (ys[(i >> 1) & 1] - q.cy) +
-                       q.n[2] * (zs[i >> 2] - q.cz);
-      lo = i ? std::min(lo, d) : d;
-      hi = i ? std::max(hi, d) : d;
-    }
-    return lo <= 0.0 && hi >= 0.0;
-  };
   auto reach = [&](const Inst &q) {
     if (q.type == AXX_PRIM_PLANE)
       return plane_meets(q, -dil, A + dil, -dil, B + dil, -dil, C + dil);
@@ -383,49 +451,32 @@ std::string plan_lattice(const axx_lattice *lat, const axx_basis *basis, int nba
                                              : geo_of(q.cx, q.cy, q.cz, q.R));
     g.aux.push_back(aux_of(basis[q.k], q.k));
   }
-  // grid over the cell
+  // grid over the cell: about one basis per grid cell's area
   const double h = std::max(2.0 * (double)lmax, std::sqrt(A * B / (double)nbasis));
-  g.gx = (int)std::min(64.0, std::max(1.0, std::floor(A / h)));
-  g.gy = (int)std::min(64.0, std::max(1.0, std::floor(B / h)));
-  g.gz = (any_sph || any_plane) ? (int)std::min(64.0, std::max(1.0, std::floor(C / h))) : 1;
-  g.inv_hx = (float)((double)g.gx / A);
-  g.inv_hy = (float)((double)g.gy / B);
-  g.inv_hz = (float)((double)g.gz / C);
-  const int ncell = g.gx * g.gy * g.gz;
-  g.cstart.assign(ncell + 1, 0);
-  for (int iz = 0; iz < g.gz; ++iz)
-    for (int iy = 0; iy < g.gy; ++iy)
-      for (int ix = 0; ix < g.gx; ++ix) {
-        const int cell = (iz * g.gy + iy) * g.gx + ix;
-        // cell box; the outer cells reach the cell edge and beyond (positions
-        // are clamped into the grid)
-        const double x0 = ix == 0 ? -1e300 : A * ix / g.gx, x1 = ix == g.gx - 1 ? 1e300 : A * (ix + 1) / g.gx;
-        const double y0 = iy == 0 ? -1e300 : B * iy / g.gy, y1 = iy == g.gy - 1 ? 1e300 : B * (iy + 1) / g.gy;
-        const double z0 = iz == 0 ? -1e300 : C * iz / g.gz, z1 = iz == g.gz - 1 ? 1e300 : C * (iz + 1) / g.gz;
-        // slack for FP32 rounding of the cell index
-        const double sx = 1e-5 * A / g.gx, sy = 1e-5 * B / g.gy, sz = 1e-5 * C / g.gz;
-        for (size_t n = 0; n < inst.size(); ++n) {
-          const Inst &q = inst[n];
-          if (q.type == AXX_PRIM_PLANE) {
-            if (plane_meets(q, x0 - dil - sx, x1 + dil + sx, y0 - dil - sy, y1 + dil + sy,
-                            z0 - dil - sz, z1 + dil + sz))
-              g.clist.push_back((uint16_t)n);
-            continue;
-          }
-          auto axis = [](double c, double lo, double hi) {
-            return c < lo ? lo - c : (c > hi ? c - hi : 0.0);
-          };
-          const double ex = axis(q.cx, x0 - dil - sx, x1 + dil + sx);
-          const double ey = axis(q.cy, y0 - dil - sy, y1 + dil + sy);
-          double d2 = ex * ex + ey * ey;
-          if (q.type == AXX_PRIM_SPHERE) {
-            const double ez = axis(q.cz, z0 - dil - sz, z1 + dil + sz);
-            d2 += ez * ez;
-          }
-          if (d2 < q.R * q.R) g.clist.push_back((uint16_t)n);
-        }
-        g.cstart[cell + 1] = (uint32_t)g.clist.size();
+  auto cells_along = [&](double side, double hh, int cap) {
+    return (int)std::min((double)cap, std::max(1.0, std::floor(side / hh)));
+  };
+  const bool flat = !(any_sph || any_plane);  // z-cylinders only: a 2-D grid
+  build_grid(g, inst, A, B, C, dil, cells_along(A, h, 64), cells_along(B, h, 64),
+             flat ? 1 : cells_along(C, h, 64));
+  // Finer 2-D grids leave fewer candidates per move (a grid cell about a
+  // third of a basis across lists about 1.3 cylinders, against 3.3 at one
+  // basis per cell), as long as the staged tables stay within the budget.
+  if (list_budget > 0 && flat && inst.size() > 1) {
+    const size_t fixed = inst.size() * 32;
+    for (double f : {4.0, 3.5, 3.0, 2.5, 2.0, 1.5}) {
+      const int gx = cells_along(A, h / f, 256), gy = cells_along(B, h / f, 256);
+      if (gx <= g.gx && gy <= g.gy) break;
+      // a cheap lower bound first: the cell starts alone
+      if (fixed + ((size_t)gx * gy + 1) * 4 > list_budget) continue;
+      GeomPlan t = g;
+      build_grid(t, inst, A, B, C, dil, gx, gy, 1);
+      if (fixed + t.cstart.size() * 4 + t.clist.size() * 2 <= list_budget) {
+        g = t;
+        break;
       }
+    }
+  }
   return "";
 }
 

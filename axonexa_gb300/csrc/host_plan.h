@@ -48,8 +48,11 @@ struct GeomPlan {
 // Returns "" on success or an error message.
 std::string plan_sequences(const axx_sequence *seqs, int nseq, int steps, double dt,
                            double gamma, SeqPlan &out);
+// list_budget > 0: a lattice of z-cylinders (a 2-D grid) may take a finer
+// grid, whose staged tables (instances, cell starts and lists) stay within
+// list_budget bytes.
 std::string plan_lattice(const axx_lattice *lat, const axx_basis *basis, int nbasis,
-                         double dt, uint32_t flags, GeomPlan &out);
+                         double dt, uint32_t flags, GeomPlan &out, size_t list_budget = 0);
 std::string plan_single(const axx_basis *basis, double dt, GeomPlan &out, float &speed,
                         float &step);
 

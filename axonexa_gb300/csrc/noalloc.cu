@@ -140,16 +140,19 @@ extern "C" axx_status axx_run_lattice_noalloc(axx_ctx *ctx, const axx_lattice *l
   lat = fr.lat_p;
   basis = fr.basis_p;
   seqs = fr.seqs_p;
-  err = plan_lattice(lat, basis, nbasis, p->timestep, p->flags, g);
-  if (!err.empty()) return fail(ctx, AXX_ERR_INVALID_ARG, err);
   SeqPlan sq;
   err = plan_sequences(seqs, nseq, p->steps, p->timestep, gamma, sq);
   if (!err.empty()) return fail(ctx, AXX_ERR_INVALID_ARG, err);
+  err = plan_lattice(lat, basis, nbasis, p->timestep, p->flags, g,
+                     list_table_budget((int)sq.channels.size()));
+  if (!err.empty()) return fail(ctx, AXX_ERR_INVALID_ARG, err);
   const int M = nseq;
   const int Mo = (p->flags & AXX_FLAG_COMPARTMENTS) ? 2 * M : M;  // rows of sums
-  // tables beyond the shared-memory budget stay in global memory (16-channel
+  // the same layout as axx_run_lattice: per-warp rows of partials, tables
+  // beyond the shared-memory budget in global memory (16-channel
   // instantiations)
-  const bool global_tables = walk_smem_bytes(g, Mo) > AXX_SMEM_MAX;
+  const bool rows = true;
+  const bool global_tables = walk_smem_bytes(g, Mo, rows) > AXX_SMEM_MAX;
   KernelTables kt;
   err = make_kernel_tables(g, sq, M, p->steps, AXX_MODE_LATTICE, p->flags, kt,
                            global_tables ? AXX_KMAX : 1);
@@ -157,7 +160,7 @@ extern "C" axx_status axx_run_lattice_noalloc(axx_ctx *ctx, const axx_lattice *l
   InitSpec init;
   err = init_spec(g, basis, nbasis, AXX_MODE_LATTICE, p, init);
   if (!err.empty()) return fail(ctx, AXX_ERR_INVALID_ARG, err);
-  const size_t smem = global_tables ? walk_sums_bytes(Mo) : walk_smem_bytes(g, Mo);
+  const size_t smem = global_tables ? walk_sums_bytes(Mo, rows) : walk_smem_bytes(g, Mo, rows);
   if (smem > AXX_SMEM_MAX)
     return fail(ctx, AXX_ERR_UNSUPPORTED, "the sequence sums exceed the shared-memory budget");
   // one instance, one cell, no compartment sums: the single-instance kernels
@@ -169,7 +172,7 @@ extern "C" axx_status axx_run_lattice_noalloc(axx_ctx *ctx, const axx_lattice *l
   long long grid = std::min<long long>(want, (long long)occ * ctx->nsm);
 
   // layout inside the scratch array; the partials shrink the grid if needed
-  const ArenaLayout Lo = arena_layout(g, kt, Mo);
+  const ArenaLayout Lo = arena_layout(g, kt, Mo, rows);
   if (Lo.fixed > kScratchBytes ||
       (Lo.per_block > 0 &&
        Lo.fixed + Lo.per_block * std::min<long long>(grid, ctx->nsm) > kScratchBytes)) {
@@ -190,13 +193,14 @@ extern "C" axx_status axx_run_lattice_noalloc(axx_ctx *ctx, const axx_lattice *l
   if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMemsetAsync(counters)");
   WalkParams P;
   const double cell[3] = {lat->a, lat->b, lat->c};
-  fill_walk_params(P, base, Lo, g, kt, p, AXX_MODE_LATTICE, M, init, cell, ctx->abort_dev);
+  fill_walk_params(P, base, Lo, g, kt, p, AXX_MODE_LATTICE, M, init, cell, ctx->abort_dev, rows);
   P.global_tables = global_tables ? 1 : 0;
   *ctx->abort_host = 0;
   TraceParams T{};
   e = launch_walk(g.geom, kt.km, kt.kmax, false, P, T, (int)grid, smem, s);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "walk kernel launch");
-  e = launch_reduce_partials(P.partials, (int)grid, Mo * 5, (double *)(base + Lo.o_out), s);
+  e = launch_reduce_partials(P.partials, (int)grid * (AXX_BLOCK / 32), Mo * 5,
+                             (double *)(base + Lo.o_out), s);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "reduction launch");
   const size_t o_out = Lo.o_out, o_cnt = Lo.o_cnt;
 

@@ -35,22 +35,57 @@ std::string make_kernel_tables(const GeomPlan &g, const SeqPlan &sq, int M, int 
     for (int i = 0; i < steps; ++i) kt.wave_il[(size_t)i * km + c] = src[i];
     for (int k = 0; k < 3; ++k) kt.ch_p[c][k] = sq.channels[c].p[k];
   }
+  // axis channels: every waveform carries the three axis vectors in order
+  // (plan_sequences chooses the axes when a waveform's directions span
+  // space), lattice walks with the 12-channel capacity
+  kt.axis_channels = mode == AXX_MODE_LATTICE && km == 12 && kt.K % 3 == 0;
+  for (int c = 0; c < kt.K && kt.axis_channels; ++c) {
+    const Channel &ch = sq.channels[c];
+    if (ch.wave != sq.channels[c - c % 3].wave || (c % 3 == 0 && c > 0 &&
+                                                   ch.wave == sq.channels[c - 1].wave))
+      kt.axis_channels = false;
+    for (int k = 0; k < 3; ++k)
+      if (ch.p[k] != (k == c % 3 ? 1.0f : 0.0f)) kt.axis_channels = false;
+  }
+  if (kt.axis_channels) {
+    kt.wave4.assign((size_t)steps * 4, 0.f);
+    for (int w = 0; w < kt.K / 3; ++w) {
+      const float *src = &sq.wave[(size_t)sq.channels[3 * w].wave * steps];
+      for (int i = 0; i < steps; ++i) kt.wave4[(size_t)i * 4 + w] = src[i];
+    }
+  }
   kt.coef.assign((size_t)M * km, 0.0);
   for (int m = 0; m < M; ++m)
     for (int c = 0; c < kt.K; ++c) kt.coef[(size_t)m * km + c] = sq.coef[(size_t)m * kt.K + c];
   return "";
 }
 
-size_t walk_sums_bytes(int M) { return (size_t)(AXX_BLOCK / 32) * M * 5 * sizeof(double); }
-
-size_t walk_smem_bytes(const GeomPlan &g, int M) {
-  const size_t wsum = (size_t)(AXX_BLOCK / 32) * M * 5 * sizeof(double);  // 160 M, 16-aligned
-  const size_t ninst = g.geo.size(), nslot = g.slot_tab.size();
-  const size_t ncell = g.cstart.size() - 1;
-  return wsum + ninst * 32 + nslot * 16 + (ncell + 1) * 4 + nslot * 4 + g.clist.size() * 2;
+size_t walk_sums_bytes(int M, bool warp_rows) {
+  return warp_rows ? 0 : (size_t)(AXX_BLOCK / 32) * M * 5 * sizeof(double);  // 160 M
 }
 
-ArenaLayout arena_layout(const GeomPlan &g, const KernelTables &kt, int M) {
+size_t walk_table_bytes(const GeomPlan &g) {
+  return g.geo.size() * 32 + g.cstart.size() * 4 + g.clist.size() * 2;
+}
+
+size_t walk_smem_bytes(const GeomPlan &g, int M, bool warp_rows) {
+  return walk_sums_bytes(M, warp_rows) + walk_table_bytes(g);
+}
+
+size_t list_table_budget(int K) {
+  int kmax = 1;
+  while (kmax < K) kmax <<= 1;
+  if (kmax == 16 && K <= 12) kmax = 12;
+  // 228 KB of shared memory per SM, 1 KB of it reserved per resident block
+  const size_t per_sm = 228 * 1024;
+  return per_sm / AXX_MIN_BLOCKS_FOR(kmax) - 1024;
+}
+
+size_t batch_table_bytes(const GeomPlan &g) {
+  return walk_table_bytes(g) + g.slot_tab.size() * 20;
+}
+
+ArenaLayout arena_layout(const GeomPlan &g, const KernelTables &kt, int M, bool warp_rows) {
   ArenaLayout L;
   size_t off = 0;
   auto take = [&](size_t bytes) {
@@ -65,15 +100,16 @@ ArenaLayout arena_layout(const GeomPlan &g, const KernelTables &kt, int M) {
   L.o_slot = take(g.slot_tab.size() * 16);
   L.o_reg = take(g.slot_region.size() * 4);
   L.o_wave = take(kt.wave_il.size() * 4);
+  L.o_wave4 = take(kt.wave4.size() * 4);
   L.o_coef = take(kt.coef.size() * 8);
   L.o_out = take((size_t)M * 5 * 8);
   L.o_cnt = take(AXX_CNT_N * 8);
   L.o_part = off;
   L.fixed = off;
-  L.per_block = (size_t)M * 5 * 8;
+  L.per_block = (size_t)M * 5 * 8 * (warp_rows ? AXX_BLOCK / 32 : 1);
   L.upload = g.geo.size() * 16 + g.aux.size() * 16 + g.cstart.size() * 4 + g.clist.size() * 2 +
              g.slot_tab.size() * 16 + g.slot_region.size() * 4 + kt.wave_il.size() * 4 +
-             kt.coef.size() * 8;
+             kt.wave4.size() * 4 + kt.coef.size() * 8;
   return L;
 }
 
@@ -90,6 +126,7 @@ cudaError_t upload_tables(char *base, const ArenaLayout &L, const GeomPlan &g,
                             up(L.o_slot, g.slot_tab.data(), g.slot_tab.size() * 16),
                             up(L.o_reg, g.slot_region.data(), g.slot_region.size() * 4),
                             up(L.o_wave, kt.wave_il.data(), kt.wave_il.size() * 4),
+                            up(L.o_wave4, kt.wave4.data(), kt.wave4.size() * 4),
                             up(L.o_coef, kt.coef.data(), kt.coef.size() * 8)};
   for (cudaError_t e : es)
     if (e != cudaSuccess) return e;
@@ -130,7 +167,7 @@ std::string init_spec(const GeomPlan &g, const axx_basis *basis, int nbasis, int
 void fill_walk_params(WalkParams &P, char *base, const ArenaLayout &L, const GeomPlan &g,
                       const KernelTables &kt, const axx_run_params *p, int mode, int M,
                       const InitSpec &init, const double cell[3],
-                      const volatile int *abort_flag) {
+                      const volatile int *abort_flag, bool warp_rows) {
   std::memset(&P, 0, sizeof(P));
   P.a = (float)cell[0];
   P.b = (float)cell[1];
@@ -177,6 +214,8 @@ void fill_walk_params(WalkParams &P, char *base, const ArenaLayout &L, const Geo
   P.K = kt.K;
   P.kmax = kt.kmax;
   P.wave_il = (const float *)(base + L.o_wave);
+  P.wave4 = (const float4 *)(base + L.o_wave4);
+  P.axis_channels = kt.axis_channels ? 1 : 0;
   for (int c = 0; c < AXX_KMAX; ++c)
     for (int k = 0; k < 3; ++k) P.ch_p[c][k] = kt.ch_p[c][k];
   P.one_dir = 1;
@@ -193,6 +232,7 @@ void fill_walk_params(WalkParams &P, char *base, const ArenaLayout &L, const Geo
   P.partials = (double *)(base + L.o_part);
   P.counters = (unsigned long long *)(base + L.o_cnt);
   P.abort_flag = abort_flag;
+  P.warp_rows = warp_rows ? 1 : 0;
 }
 
 }  // namespace axx

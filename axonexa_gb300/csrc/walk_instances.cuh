@@ -101,7 +101,13 @@ static cudaError_t walk_launch_km(int kmax, bool trace, bool one, bool gt, const
     case 2: return walk_go<GEOM, 2, KM, false>(P, T, grid, smem, s);
     case 4: return walk_go<GEOM, 4, KM, false>(P, T, grid, smem, s);
     case 8: return walk_go<GEOM, 8, KM, false>(P, T, grid, smem, s);
-    case 12: return walk_go<GEOM, 12, KM, false>(P, T, grid, smem, s);  // lattice walks only
+    case 12:  // lattice walks only; axis channels for permeable cylinder lattices
+      // (the impermeable walk's paired-move loop spills with them)
+      if constexpr (GEOM == AXX_GEOM_CYL && KM == AXX_KM_LAT_PERM) {
+        if (P.axis_channels)
+          return walk_go<GEOM, 12, KM, false, false, false, AXX_PAX_AXES>(P, T, grid, smem, s);
+      }
+      return walk_go<GEOM, 12, KM, false>(P, T, grid, smem, s);
     case 16: return walk_go<GEOM, 16, KM, false>(P, T, grid, smem, s);
   }
   return cudaErrorInvalidValue;

@@ -179,6 +179,13 @@ __device__ __forceinline__ bool seg_may(float bh, float c0, float c1, float aa, 
            (c0 >= 0.0f && (bh >= 0.0f || (c0 > 0.0f && c1 > 0.0f && fma_f(aa, rem, bh) <= 0.0f))));
 }
 
+// seg_may, and for a start outside also the discriminant test of seg_root's
+// entry root (the same operation on the same operands): a line that passes
+// beside the instance is rejected before the nearest-hit loop.
+__device__ __forceinline__ bool seg_may_disc(float bh, float c0, float c1, float aa, float rem) {
+  return seg_may(bh, c0, c1, aa, rem) && !(c0 > 0.0f && !(fma_f(bh, bh, -(aa * c0)) > 0.0f));
+}
+
 // Distance to the first boundary of one instance along the segment
 // start + s*d, 0 < s < rem, or +inf, given its quadratic (c0 = 0 for a start
 // on the instance's surface).
@@ -326,7 +333,10 @@ struct Walker {
   float part[KMAX];  // phase of the current block of moves (DEFER)
   float t2s, t2c;
   int nin;  // ONE: moves weighted by the instance's region (T2 by counts)
-  float v0, L0;  // speed and step of the slot, where it never changes
+  // speed, step and dt/T2 of the walker's slot, held while the slot holds
+  // (walks behind specular or permeable walls, whose slot changes only at a
+  // wrap or a transmission)
+  float v0, L0, t2z;
 };
 
 // The instances and the list a move may test: either the cell list of the
@@ -374,8 +384,9 @@ __device__ __forceinline__ MoveOut boundary(const WalkParams &P, const Cands<GEO
       float bh, c0, c1;
       seg_coef(g, sph, sx, sy, sz, dx, dy, dz, L, bh, c0, c1);
       // the same rejections seg_root applies first (c0 is exact here: no
-      // instance has been hit yet in this move)
-      return seg_may(bh, c0, c1, sph ? aa_s : aa_c, L);
+      // instance has been hit yet in this move), its discriminant test
+      // included
+      return seg_may_disc(bh, c0, c1, sph ? aa_s : aa_c, L);
     };
     if (ONE) {
       if (is_plane<GEOM>(C.a0)) {
@@ -383,7 +394,7 @@ __device__ __forceinline__ MoveOut boundary(const WalkParams &P, const Cands<GEO
       } else {
         const bool sph = is_sphere<GEOM>(C.a0);
         seg_coef(C.g0, sph, sx, sy, sz, dx, dy, dz, L, bh1, c01, c11);
-        maybe = seg_may(bh1, c01, c11, sph ? aa_s : aa_c, L);
+        maybe = seg_may_disc(bh1, c01, c11, sph ? aa_s : aa_c, L);
       }
     } else {
       for (uint32_t j = C.b; j < C.e; ++j) {
@@ -507,6 +518,10 @@ __device__ __forceinline__ MoveOut boundary(const WalkParams &P, const Cands<GEO
   return o;
 }
 
+// PAX value of the axis-channel instantiations (channel 3w + a is waveform w
+// along axis a; every axis carries phase: bits x, y, z set, and bit 3)
+#define AXX_PAX_AXES 15
+
 // A channel's projection p . r, fma(p_z, z, fma(p_y, y, p_x x)), over the
 // axes in PAX: a term of a zero coefficient adds a zero, so leaving it out
 // gives the same value (up to the sign of a zero sum).
@@ -554,7 +569,7 @@ __device__ __forceinline__ MoveOut boundary_one(const WalkParams &P, const Cands
   float aa = sph ? fma_f(dx, dx, fma_f(dy, dy, dz * dz)) : fma_f(dx, dx, dy * dy);
   float bh, c0, c1;
   seg_coef(g, sph, sx, sy, sz, dx, dy, dz, L, bh, c0, c1);
-  const bool maybe = seg_may(bh, c0, c1, aa, L);
+  const bool maybe = seg_may_disc(bh, c0, c1, aa, L);
   MoveOut o;
   o.hits = 0;
   o.capped = false;
@@ -645,7 +660,9 @@ __device__ __forceinline__ void do_move(const WalkParams &P, const SmemView &S,
   // slot never changes, and its speed and step stay in registers (the T2
   // term, .z, is then not read per move)
   constexpr bool fixed_slot = ONE && (single || KM == AXX_KM_LAT_IMP);
-  const float4 s4 = fixed_slot ? make_float4(W.v0, W.L0, 0.0f, 0.0f) : S.slot[W.slot];
+  constexpr bool tracked = KM == AXX_KM_LAT_IMP || KM == AXX_KM_LAT_PERM;
+  const float4 s4 = (fixed_slot || tracked) ? make_float4(W.v0, W.L0, W.t2z, 0.0f)
+                                            : S.slot[W.slot];
   const float v = s4.x, Lb = s4.y;
   float dx, dy, dz, L = Lb;
   if (PICK) {
@@ -721,7 +738,18 @@ __device__ __forceinline__ void do_move(const WalkParams &P, const SmemView &S,
   // zero waveforms and zero projections
   const float *wrow = P.wave_il + (size_t)i * KMAX;
   float wv[KMAX];
-  if (KMAX % 4 == 0) {
+  if constexpr (PAX == AXX_PAX_AXES) {
+    // channel 3w + a: waveform w along axis a; the projection is the
+    // coordinate itself (the same value: fma(0, y, 1 * x) = x)
+    static_assert(KMAX == 12, "axis channels: four waveforms along three axes");
+    const float4 w4 = __ldg(P.wave4 + i);
+    const float wq[4] = {w4.x, w4.y, w4.z, w4.w};
+#pragma unroll
+    for (int c = 0; c < KMAX; ++c) {
+      const float d = (c % 3 == 0) ? px : ((c % 3 == 1) ? py : pz);
+      kahan_add(W.acc[c], W.cmp[c], wq[c / 3] * d);
+    }
+  } else if (KMAX % 4 == 0) {
     // rows of 4k floats start on 16-byte boundaries (the table is 256-aligned)
 #pragma unroll
     for (int q = 0; q < KMAX / 4; ++q) {
@@ -735,7 +763,8 @@ __device__ __forceinline__ void do_move(const WalkParams &P, const SmemView &S,
 #pragma unroll
     for (int c = 0; c < KMAX; ++c) wv[c] = __ldg(&wrow[c]);
   }
-  if (KMAX > 1 && P.one_dir) {
+  if constexpr (PAX == AXX_PAX_AXES) {
+  } else if (KMAX > 1 && P.one_dir) {
     // every channel projects on the same direction (padded channels carry
     // zero waveforms): one projection serves all, the same bits as each
     const float d = project<PAX>(P.ch_p[0], px, py, pz);
@@ -764,7 +793,6 @@ __device__ __forceinline__ void do_move(const WalkParams &P, const SmemView &S,
   // (The FP32 lookup of a position a rounding error from a wall could name
   // the other side; the FP64 reference's hardly ever does.)  Rejection walks
   // look the region up after every move.
-  constexpr bool tracked = KM == AXX_KM_LAT_IMP || KM == AXX_KM_LAT_PERM;
   if (!single && tracked && !(ONE && !perm)) {
     // dt/T2 of the move's region (0 without relaxation); the permeable walk
     // weights the region after the move (accumtime is always 0)
@@ -777,12 +805,16 @@ __device__ __forceinline__ void do_move(const WalkParams &P, const SmemView &S,
         W.slot =
             lookup_list<GEOM>(S, S.cstart[cell], S.cstart[cell + 1], P.ecs_slot, fx, fy, fz);
       }
+      const float4 ns = S.slot[W.slot];
+      W.v0 = ns.x;
+      W.L0 = ns.y;
+      W.t2z = ns.z;
     }
     if (perm) {
       if (ONE)
         W.nin += (W.slot != P.ecs_slot) ? 1 : 0;
       else
-        kahan_add(W.t2s, W.t2c, S.slot[W.slot].z);
+        kahan_add(W.t2s, W.t2c, W.t2z);
     }
   }
   if (!single && !tracked) {  // rejection walks
@@ -873,6 +905,7 @@ __device__ __forceinline__ WalkResult walk_one(const WalkParams &P, const SmemVi
     const float4 s = S.slot[W.slot];
     W.v0 = s.x;
     W.L0 = s.y;
+    W.t2z = s.z;
   }
   int i = 1;
   if constexpr (single) {
@@ -910,11 +943,11 @@ __device__ __forceinline__ WalkResult walk_one(const WalkParams &P, const SmemVi
       st.load(P);
       const uint32_t w0 = st.b0, w1 = st.b1, w2 = st.b2, w3 = st.b3;
       st.pos = 2;
-      do_move<GEOM, KMAX, KM, TRACE, ONE>(P, S, T, wid, i, word_to_uniform(w0),
-                                           word_to_uniform(w1), st, W, res, g0, a0);
+      do_move<GEOM, KMAX, KM, TRACE, ONE, false, false, PAX>(
+          P, S, T, wid, i, word_to_uniform(w0), word_to_uniform(w1), st, W, res, g0, a0);
       st.pos = 4;
-      do_move<GEOM, KMAX, KM, TRACE, ONE>(P, S, T, wid, i + 1, word_to_uniform(w2),
-                                           word_to_uniform(w3), st, W, res, g0, a0);
+      do_move<GEOM, KMAX, KM, TRACE, ONE, false, false, PAX>(
+          P, S, T, wid, i + 1, word_to_uniform(w2), word_to_uniform(w3), st, W, res, g0, a0);
     }
   }
   if (defer && !perm && __all_sync(__activemask(), st.pos == 4)) {
@@ -986,8 +1019,9 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
-// The walk kernel.  Dynamic shared memory: [warps][M][5] FP64 sums, then the
-// instances, slot table, cell starts, slot regions and cell lists.
+// The walk kernel.  Dynamic shared memory: [warps][M][5] FP64 sums (none with
+// per-warp rows in global memory), then the instances, cell starts and cell
+// lists.
 // ONEONLY: compiled for substrates of a single instance only (the host checks
 // n_inst == 1 and ncell == 1); the list path is left out, which frees
 // registers for one more resident block per SM.
@@ -1002,7 +1036,8 @@ template <int GEOM, int KMAX, int KM, bool TRACE, bool ONEONLY = false, bool GT 
 __global__ void __launch_bounds__(AXX_BLOCK, ONEONLY && KMAX <= 4 ? AXX_MIN_BLOCKS + 1
                                                                  : AXX_MIN_BLOCKS_FOR(KMAX))
     walk_kernel(const __grid_constant__ WalkParams P, const __grid_constant__ TraceParams T) {
-  static_assert(PAX == 7 || (GEOM == AXX_GEOM_CYL && ONEONLY && !TRACE),
+  static_assert(PAX == 7 || (GEOM == AXX_GEOM_CYL && ONEONLY && !TRACE) ||
+                    (PAX == AXX_PAX_AXES && KMAX == 12 && !ONEONLY && !TRACE),
                 "axes are dropped only from single-cylinder walks without traces");
   extern __shared__ __align__(16) unsigned char smem[];
   constexpr int warps = AXX_BLOCK / 32;
@@ -1012,7 +1047,17 @@ __global__ void __launch_bounds__(AXX_BLOCK, ONEONLY && KMAX <= 4 ? AXX_MIN_BLOC
   // rows of sums: all walkers, then those starting inside a basis (the
   // compartment sums run in the general instantiations only)
   const int Mo = (!ONEONLY && P.compart) ? 2 * M : M;
-  for (int j = threadIdx.x; j < warps * Mo * 5; j += blockDim.x) wsum[j] = 0.0;
+  const long long gwarp = (long long)blockIdx.x * warps + wib;
+  // the sums of this warp: per-warp rows in shared memory, folded into one
+  // partial per block at the end, or (warp_rows) the warp's own row of the
+  // partials in global memory
+  const bool rows = P.warp_rows != 0;
+  double *wrow = rows ? P.partials + (size_t)gwarp * Mo * 5 : wsum + (size_t)wib * Mo * 5;
+  if (rows) {
+    for (int j = lane; j < Mo * 5; j += 32) wrow[j] = 0.0;
+  } else {
+    for (int j = threadIdx.x; j < warps * Mo * 5; j += blockDim.x) wsum[j] = 0.0;
+  }
 
   SmemView S;
   if constexpr (GT) {
@@ -1025,34 +1070,29 @@ __global__ void __launch_bounds__(AXX_BLOCK, ONEONLY && KMAX <= 4 ? AXX_MIN_BLOC
     S.region = P.slot_region;
     S.clist = P.cell_list;
   } else {
-    // stage the substrate tables (layout fixed by the host planner)
-    float4 *sg = reinterpret_cast<float4 *>(smem + (size_t)warps * Mo * 5 * sizeof(double));
+    // stage the substrate tables (layout fixed by the host planner); the slot
+    // tables, read when a walker's slot changes, stay in global memory
+    float4 *sg = reinterpret_cast<float4 *>(smem + (rows ? 0 : (size_t)warps * Mo * 5 *
+                                                                  sizeof(double)));
     float4 *sa = sg + P.n_inst;
-    float4 *ss = sa + P.n_inst;
-    uint32_t *sc = reinterpret_cast<uint32_t *>(ss + P.n_slot);
-    int *sr = reinterpret_cast<int *>(sc + P.ncell + 1);
-    uint16_t *sl = reinterpret_cast<uint16_t *>(sr + P.n_slot);
+    uint32_t *sc = reinterpret_cast<uint32_t *>(sa + P.n_inst);
+    uint16_t *sl = reinterpret_cast<uint16_t *>(sc + P.ncell + 1);
     for (int j = threadIdx.x; j < P.n_inst; j += blockDim.x) {
       sg[j] = P.inst_geo[j];
       sa[j] = P.inst_aux[j];
-    }
-    for (int j = threadIdx.x; j < P.n_slot; j += blockDim.x) {
-      ss[j] = P.slot_tab[j];
-      sr[j] = P.slot_region[j];
     }
     for (int j = threadIdx.x; j <= P.ncell; j += blockDim.x) sc[j] = P.cell_start[j];
     for (int j = threadIdx.x; j < P.n_list; j += blockDim.x) sl[j] = P.cell_list[j];
     S.geo = sg;
     S.aux = sa;
-    S.slot = ss;
+    S.slot = P.slot_tab;
     S.cstart = sc;
-    S.region = sr;
+    S.region = P.slot_region;
     S.clist = sl;
   }
   __syncthreads();
 
   const long long ntask = (P.n_walkers + 31) / 32;
-  const long long gwarp = (long long)blockIdx.x * warps + wib;
   const long long nwarp = (long long)gridDim.x * warps;
   unsigned caps = 0, hits = 0, init_fail = 0, aborted = 0, start_in = 0;
   // a single instance (one basis without reachable ghosts, or a single pore)
@@ -1071,7 +1111,7 @@ __global__ void __launch_bounds__(AXX_BLOCK, ONEONLY && KMAX <= 4 ? AXX_MIN_BLOC
       if constexpr (ONEONLY)
         r = walk_one<GEOM, KMAX, KM, TRACE, true, PAX>(P, S, T, wid, W);
       else if constexpr (KMAX > 4)  // (the list path serves one instance too)
-        r = walk_one<GEOM, KMAX, KM, TRACE, false>(P, S, T, wid, W);
+        r = walk_one<GEOM, KMAX, KM, TRACE, false, PAX>(P, S, T, wid, W);
       else
         r = one ? walk_one<GEOM, KMAX, KM, TRACE, true>(P, S, T, wid, W)
                 : walk_one<GEOM, KMAX, KM, TRACE, false>(P, S, T, wid, W);
@@ -1100,7 +1140,7 @@ __global__ void __launch_bounds__(AXX_BLOCK, ONEONLY && KMAX <= 4 ? AXX_MIN_BLOC
       const double s0 = warp_sum(xv), s1 = warp_sum(yv), s2 = warp_sum(xv * xv),
                    s3 = warp_sum(yv * yv), s4 = warp_sum(xv * yv);
       if (lane == 0) {
-        double *d = wsum + ((size_t)wib * Mo + m) * 5;
+        double *d = wrow + (size_t)m * 5;
         d[0] += s0;
         d[1] += s1;
         d[2] += s2;
@@ -1111,7 +1151,7 @@ __global__ void __launch_bounds__(AXX_BLOCK, ONEONLY && KMAX <= 4 ? AXX_MIN_BLOC
         // (x and y only: the rows' other entries stay 0)
         const double t0 = warp_sum(in0 ? xv : 0.0), t1 = warp_sum(in0 ? yv : 0.0);
         if (lane == 0) {
-          double *d = wsum + ((size_t)wib * Mo + M + m) * 5;
+          double *d = wrow + (size_t)(M + m) * 5;
           d[0] += t0;
           d[1] += t1;
         }
@@ -1124,6 +1164,7 @@ __global__ void __launch_bounds__(AXX_BLOCK, ONEONLY && KMAX <= 4 ? AXX_MIN_BLOC
   if (aborted) atomicAdd(&P.counters[AXX_CNT_ABORTED], (unsigned long long)aborted);
   if (!ONEONLY && start_in)
     atomicAdd(&P.counters[AXX_CNT_START_IN], (unsigned long long)start_in);
+  if (rows) return;  // each warp's row is its partial
   __syncthreads();
   for (int j = threadIdx.x; j < Mo * 5; j += blockDim.x) {
     double s = 0.0;
