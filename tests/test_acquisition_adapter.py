@@ -113,8 +113,11 @@ def _adapter_adc():
     if "adc" not in _built:
         out = os.path.join(LIBDIR, "_build", "adapter_adc")
         os.makedirs(os.path.dirname(out), exist_ok=True)
-        subprocess.run([_gxx(), "-std=c++17", "-O2", "-I", INC, os.path.join(CPP, "adapter_adc.cpp"),
-                        "-L", LIBDIR, "-laxx", "-Wl,-rpath," + LIBDIR, "-o", out], check=True)
+        # no contraction into fused multiply-adds (aarch64 GCC fuses by
+        # default): the reference's code is built the same way
+        subprocess.run([_gxx(), "-std=c++17", "-O2", "-ffp-contract=off", "-I", INC,
+                        os.path.join(CPP, "adapter_adc.cpp"), "-L", LIBDIR, "-laxx",
+                        "-Wl,-rpath," + LIBDIR, "-o", out], check=True)
         _built["adc"] = out
     return _built["adc"]
 
@@ -123,7 +126,8 @@ def build_adapter_main():
     """tests/cpp/adapter_main.cpp compiled against the adapter and libaxx.so."""
     out = os.path.join(LIBDIR, "_build", "adapter_main")
     os.makedirs(os.path.dirname(out), exist_ok=True)
-    subprocess.run([_gxx(), "-std=c++17", "-O2", "-Wall", "-Werror", "-I", INC, "-I", CPP,
+    subprocess.run([_gxx(), "-std=c++17", "-O2", "-ffp-contract=off", "-Wall", "-Werror",
+                    "-I", INC, "-I", CPP,
                     os.path.join(CPP, "adapter_main.cpp"), "-L", LIBDIR, "-laxx",
                     "-Wl,-rpath," + LIBDIR, "-o", out], check=True)
     return out
