@@ -33,6 +33,7 @@ CUDA_SOURCES = [
     "batch.cu",
     "mlp.cu",
     "mlp_tc.cu",
+    "mlp_gemm_tc.cu",
     "mag.cu",
     "calcf.cu",
     "wc.cu",

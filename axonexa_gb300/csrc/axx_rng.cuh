@@ -231,6 +231,26 @@ struct DevStream {
     u2 = word_to_uniform(w2);
     pos = (p0 >= 3) ? p0 - 2 : p0 + 2;
   }
+  // next2, except that a move whose two words end the held block loads the
+  // next one at once (pos 2: the block's last two words; pos 3: the last
+  // word, then the next block's first; pos 4: the next block's first two):
+  // after the move's draws at least one word is held, so a permeable wall
+  // hit's draw (one word) needs no block load inside the divergent boundary
+  // loop unless the move hits more than once.  Same words, same positions.
+  template <class KP>
+  __device__ __forceinline__ void next2_eager(const KP &P, float &u1, float &u2) {
+    const int p0 = pos;
+    const uint32_t o2 = b2, o3 = b3;
+    if (p0 >= 2) {
+      ++blk;
+      load(P);
+    }
+    const uint32_t w1 = (p0 == 0) ? b0 : (p0 == 1) ? b1 : (p0 == 2) ? o2 : (p0 == 3) ? o3 : b0;
+    const uint32_t w2 = (p0 == 0) ? b1 : (p0 == 1) ? b2 : (p0 == 2) ? o3 : (p0 == 3) ? b0 : b1;
+    u1 = word_to_uniform(w1);
+    u2 = word_to_uniform(w2);
+    pos = (p0 < 2) ? p0 + 2 : p0 - 2;
+  }
   __device__ __forceinline__ uint32_t words_used() const { return blk * 4u + (uint32_t)pos; }
 };
 #endif

@@ -4,6 +4,8 @@
 //
 // Layout in HBM (per plan, uploaded once):
 //   inst_geo[n_inst]   float4 (cx, cy, cz, -R^2)   basis instances: every basis
+//                      (lattices of z-cylinders: cz is (R + h)^2 of the
+//                      annulus test)
 //   inst_aux[n_inst]   float4 (1/R, eps, slot, type) plus its periodic ghosts
 //   cell_start[ncell+1], cell_list[...] uint32/uint16: per grid cell of the
 //                      periodic box, the instances whose bounding box meets the
@@ -63,6 +65,7 @@ struct WalkParams {
   const uint16_t *cell_list;
   int gx, gy, gz;
   float inv_hx, inv_hy, inv_hz;
+  float ann_h2x2;             // cylinder lattices: 2 h^2 of the annulus test (geo.z = (R+h)^2)
   const float4 *slot_tab;
   const int *slot_region;     // region id of each slot (0 for the extracellular slot)
   int ecs_slot;

@@ -451,6 +451,13 @@ std::string plan_lattice(const axx_lattice *lat, const axx_basis *basis, int nba
                                              : geo_of(q.cx, q.cy, q.cz, q.R));
     g.aux.push_back(aux_of(basis[q.k], q.k));
   }
+  if (g.geom == AXX_GEOM_CYL) {
+    // the annulus test of the cylinder lists: (R + h)^2 in the unused cz,
+    // h = half the longest step plus a slack far above FP32 position rounding
+    const double hh = 0.5 * (double)lmax + 0.01 * (double)lmax + 1e-6 * std::max(A, B);
+    for (size_t n = 0; n < inst.size(); ++n) g.geo[n].z = (float)((inst[n].R + hh) * (inst[n].R + hh));
+    g.ann_h2x2 = (float)(2.0 * hh * hh);
+  }
   // grid over the cell: about one basis per grid cell's area
   const double h = std::max(2.0 * (double)lmax, std::sqrt(A * B / (double)nbasis));
   auto cells_along = [&](double side, double hh, int cap) {

@@ -43,6 +43,7 @@ struct GeomPlan {
   std::vector<int> slot_region;
   int ecs_slot = 0;
   float lmax = 0.f;
+  float ann_h2x2 = 0.f;  // z-cylinder lattices: 2 h^2 of the annulus test
 };
 
 // Returns "" on success or an error message.

@@ -1,7 +1,7 @@
 // mlp.cu -- the learned surrogate's network: MLP in -> depth x width (SiLU)
-// -> 1, trained with hand-written BF16 tensor-core kernels (mma.sync
-// m16n8k16, FP32 accumulate) and Adam; inference runs the fused tcgen05
-// kernel of mlp_tc.cu.
+// -> 1, trained with hand-written BF16 tensor-core GEMMs (tcgen05.mma with
+// TMEM accumulators, mlp_gemm_tc.cu) and Adam; inference runs the fused
+// tcgen05 kernel of mlp_tc.cu.
 //
 // Training step for a batch of B rows (weights W_l are [out][in] row-major):
 //   forward   Z_l = A_l W_l^T + b_l, H_l = silu(Z_l) (A_0 = X, A_l = H_{l-1}),
@@ -29,133 +29,6 @@
 #include "mlp_internal.h"
 
 namespace axx {
-
-// ---- generic strided BF16 GEMM on mma.sync ----------------------------------
-// C[m*ldc + n] (+)= sum_k A(m,k) B(k,n), A(m,k) = A[m*sam + k*sak],
-// B(k,n) = B[k*sbk + n*sbn]; out-of-range elements read as zero.
-constexpr int GT = 64, GK = 32, GPAD = 8;
-
-__device__ __forceinline__ void mma_bf16(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2,
-                                        uint32_t a3, uint32_t b0, uint32_t b1) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
-      "{%8,%9}, {%0,%1,%2,%3};\n"
-      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-      : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
-}
-
-// blockIdx.z takes K range [z kc, min(K, (z+1) kc)) and writes C + z cz (a
-// split-K partial when gridDim.z > 1).  The operand tiles are read along
-// whichever index has unit stride, so that the loads coalesce.
-__global__ void __launch_bounds__(128) gemm_bf16_kernel(int M, int N, int K,
-                                                        const __nv_bfloat16 *__restrict__ A,
-                                                        long long sam, long long sak,
-                                                        const __nv_bfloat16 *__restrict__ B,
-                                                        long long sbk, long long sbn,
-                                                        float *__restrict__ C, long long ldc,
-                                                        int accumulate, int kc, long long cz) {
-  __shared__ __align__(16) __nv_bfloat16 As[GT][GK + GPAD];  // [m][k]
-  __shared__ __align__(16) __nv_bfloat16 Bs[GT][GK + GPAD];  // [n][k]
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int wm = warp >> 1, wn = warp & 1;
-  const int m0 = blockIdx.y * GT, n0 = blockIdx.x * GT;
-  const int g = lane >> 2, c = lane & 3;
-  float acc[2][4][4];
-#pragma unroll
-  for (int i = 0; i < 2; ++i)
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-#pragma unroll
-      for (int r = 0; r < 4; ++r) acc[i][j][r] = 0.f;
-  const __nv_bfloat16 zero = __float2bfloat16(0.f);
-  const int kb = blockIdx.z * kc, ke = min(K, kb + kc);
-  C += blockIdx.z * cz;
-  const bool a_k = sak == 1, b_k = sbk == 1;  // unit stride along k
-  for (int k0 = kb; k0 < ke; k0 += GK) {
-    for (int e = tid; e < GT * GK; e += 128) {
-      const int ra = a_k ? e / GK : e % GT, ka = a_k ? e % GK : e / GT;
-      const int rb = b_k ? e / GK : e % GT, kb2 = b_k ? e % GK : e / GT;
-      const int gm = m0 + ra, gka = k0 + ka, gn = n0 + rb, gkb = k0 + kb2;
-      As[ra][ka] = (gm < M && gka < ke) ? A[gm * sam + gka * sak] : zero;
-      Bs[rb][kb2] = (gn < N && gkb < ke) ? B[gkb * sbk + gn * sbn] : zero;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int kk = 0; kk < GK; kk += 16) {
-      uint32_t af[2][4], bfr[4][2];
-#pragma unroll
-      for (int i = 0; i < 2; ++i) {
-        const int r = wm * 32 + i * 16 + g;
-        af[i][0] = *reinterpret_cast<const uint32_t *>(&As[r][kk + 2 * c]);
-        af[i][1] = *reinterpret_cast<const uint32_t *>(&As[r + 8][kk + 2 * c]);
-        af[i][2] = *reinterpret_cast<const uint32_t *>(&As[r][kk + 2 * c + 8]);
-        af[i][3] = *reinterpret_cast<const uint32_t *>(&As[r + 8][kk + 2 * c + 8]);
-      }
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const int n = wn * 32 + j * 8 + g;
-        bfr[j][0] = *reinterpret_cast<const uint32_t *>(&Bs[n][kk + 2 * c]);
-        bfr[j][1] = *reinterpret_cast<const uint32_t *>(&Bs[n][kk + 2 * c + 8]);
-      }
-#pragma unroll
-      for (int i = 0; i < 2; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j)
-          mma_bf16(acc[i][j], af[i][0], af[i][1], af[i][2], af[i][3], bfr[j][0], bfr[j][1]);
-    }
-    __syncthreads();
-  }
-#pragma unroll
-  for (int i = 0; i < 2; ++i)
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-#pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const int m = m0 + wm * 32 + i * 16 + g + h * 8;
-        const int n = n0 + wn * 32 + j * 8 + 2 * c;
-        if (m >= M) continue;
-        for (int q = 0; q < 2; ++q) {
-          if (n + q >= N) continue;
-          float *dst = &C[m * ldc + n + q];
-          const float v = acc[i][j][h * 2 + q];
-          *dst = accumulate ? *dst + v : v;
-        }
-      }
-}
-
-// Sums the split-K partials part[z][m][n] (z ascending: a fixed order) into C.
-__global__ void splitk_sum_kernel(const float *__restrict__ part, int splits, int M, int N,
-                                  float *__restrict__ C, long long ldc) {
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= (long long)M * N) return;
-  const int m = (int)(i / N), n = (int)(i % N);
-  float s = 0.f;
-  for (int z = 0; z < splits; ++z) s += part[(long long)z * M * N + i];
-  C[m * ldc + n] = s;
-}
-
-void gemm_bf16(cudaStream_t s, int M, int N, int K, const __nv_bfloat16 *A, long long sam,
-               long long sak, const __nv_bfloat16 *B, long long sbk, long long sbn, float *C,
-               long long ldc, bool accumulate, float *part) {
-  dim3 grid((N + GT - 1) / GT, (M + GT - 1) / GT);
-  // a long reduction over few output tiles (the weight gradients: K = batch)
-  // splits K across blocks into partials, summed in a fixed order after
-  const int tiles = (int)(grid.x * grid.y);
-  int splits = 1;
-  if (part && !accumulate)
-    while (splits < kMaxSplitK && tiles * splits < 256 && K / (splits * 2) >= 4 * GK) splits *= 2;
-  if (splits == 1) {
-    gemm_bf16_kernel<<<grid, 128, 0, s>>>(M, N, K, A, sam, sak, B, sbk, sbn, C, ldc,
-                                          accumulate ? 1 : 0, K, 0);
-    return;
-  }
-  const int kc = ((K + splits - 1) / splits + GK - 1) / GK * GK;
-  grid.z = splits;
-  gemm_bf16_kernel<<<grid, 128, 0, s>>>(M, N, K, A, sam, sak, B, sbk, sbn, part, N, 0, kc,
-                                        (long long)M * N);
-  splitk_sum_kernel<<<(int)(((long long)M * N + 255) / 256), 256, 0, s>>>(part, splits, M, N, C,
-                                                                          ldc);
-}
 
 // ---- elementwise kernels ----------------------------------------------------
 __device__ __forceinline__ float sigmoid_f(float z) { return 1.0f / (1.0f + __expf(-z)); }
@@ -385,7 +258,7 @@ void mlp_forward_train(axx_mlp *m, int B) {
   for (int l = 0; l < m->depth; ++l) {
     const int in = l == 0 ? m->in_pad : W;
     const __nv_bfloat16 *A = l == 0 ? m->Xb : m->H + (size_t)(l - 1) * B * W;
-    gemm_bf16(s, B, W, in, A, in, 1, m->Wb[l], 1, in, m->Cb, W, false);
+    gemm_bf16(s, B, W, in, A, in, 1, m->Wb[l], 1, in, m->Cb, W, false, nullptr, m->tc_error);
     bias_silu_kernel<<<blocks((long long)B * W), 256, 0, s>>>(
         m->Cb, m->bias(l), m->Z + (size_t)l * B * W, m->H + (size_t)l * B * W, B, W);
   }
@@ -410,10 +283,11 @@ void mlp_backward(axx_mlp *m, int B) {
     // dW_l[n][k] = sum_b dZ[b][n] A[b][k]  (M = W rows n, N = in_true columns k, K = B)
     const __nv_bfloat16 *A = l == 0 ? m->Xb : m->H + (size_t)(l - 1) * B * W;
     gemm_bf16(s, W, in_true, B, m->dZb, 1, W, A, in, 1, m->grad_weight(l), in_true, false,
-              m->kpart);
+              m->kpart, m->tc_error);
     if (l > 0) {
       // dH_{l-1}[b][k] = sum_n dZ[b][n] W_l[n][k]
-      gemm_bf16(s, B, W, W, m->dZb, W, 1, m->Wb[l], W, 1, m->dH, W, false);
+      gemm_bf16(s, B, W, W, m->dZb, W, 1, m->Wb[l], W, 1, m->dH, W, false, nullptr,
+                m->tc_error);
     }
   }
 }
@@ -480,6 +354,7 @@ extern "C" axx_status axx_mlp_create(axx_ctx *ctx, int in_dim, int width, int de
     }
     e = mlp_tc_init(m);
   }
+  if (e == cudaSuccess) e = gemm_tc_init();
   if (e != cudaSuccess) {
     axx_mlp_destroy(m);
     return mcuda(ctx, e, "axx_mlp_create");
@@ -530,6 +405,17 @@ extern "C" axx_status axx_mlp_set_params(axx_mlp *m, const float *params) {
   return AXX_OK;
 }
 
+// AXX_ERR_TIMEOUT (and the flag cleared) when a tensor-core completion wait
+// of the work just synchronised ran out.
+static axx_status tc_status(axx_mlp *m) {
+  int tc_err = 0;
+  const cudaError_t e = cudaMemcpy(&tc_err, m->tc_error, 4, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return mcuda(m->ctx, e, "reading the tensor-core error flag");
+  if (!tc_err) return AXX_OK;
+  cudaMemset(m->tc_error, 0, 4);
+  return mfail(m->ctx, AXX_ERR_TIMEOUT, "a tensor-core completion wait ran out");
+}
+
 static cudaError_t upload_xy(axx_mlp *m, const float *X, const float *y, int n, float **dX,
                              float **dy) {
   cudaError_t e = cudaMalloc(dX, (size_t)n * m->in_dim * 4);
@@ -558,7 +444,7 @@ extern "C" axx_status axx_mlp_gradients(axx_mlp *m, const float *X, const float 
   if (dX) cudaFree(dX);
   if (dY) cudaFree(dY);
   if (e != cudaSuccess) return mcuda(m->ctx, e, "axx_mlp_gradients");
-  return AXX_OK;
+  return tc_status(m);
 }
 
 extern "C" axx_status axx_mlp_train(axx_mlp *m, const float *X, const float *y, int n, int batch,
@@ -591,7 +477,7 @@ extern "C" axx_status axx_mlp_train(axx_mlp *m, const float *X, const float *y, 
   if (dY) cudaFree(dY);
   if (dL) cudaFree(dL);
   if (e != cudaSuccess) return mcuda(m->ctx, e, "axx_mlp_train");
-  return AXX_OK;
+  return tc_status(m);
 }
 
 extern "C" axx_status axx_mlp_predict(axx_mlp *m, const float *X, int n, float *y) {

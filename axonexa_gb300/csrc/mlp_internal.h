@@ -34,10 +34,15 @@ struct axx_mlp {
 
 namespace axx {
 constexpr int kMaxSplitK = 16;
-// part: scratch for split-K partials (kMaxSplitK * M * N floats), or null.
+// C[m*ldc + n] (+)= sum_k A[m*sam + k*sak] B[k*sbk + n*sbn] on the tcgen05
+// tensor cores (mlp_gemm_tc.cu).  part: scratch for split-K partials
+// (kMaxSplitK * M * N floats), or null; err: device flag set by a timed-out
+// completion wait.
 void gemm_bf16(cudaStream_t s, int M, int N, int K, const __nv_bfloat16 *A, long long sam,
                long long sak, const __nv_bfloat16 *B, long long sbk, long long sbn, float *C,
-               long long ldc, bool accumulate, float *part = nullptr);
+               long long ldc, bool accumulate, float *part, int *err);
+// Raises the GEMM kernel's dynamic shared-memory limit (once per process).
+cudaError_t gemm_tc_init();
 }  // namespace axx
 
 // tensor-core inference (mlp_tc.cu)

@@ -188,6 +188,7 @@ void fill_walk_params(WalkParams &P, char *base, const ArenaLayout &L, const Geo
   P.inv_hx = g.inv_hx;
   P.inv_hy = g.inv_hy;
   P.inv_hz = g.inv_hz;
+  P.ann_h2x2 = g.ann_h2x2;
   P.slot_tab = (const float4 *)(base + L.o_slot);
   P.slot_region = (const int *)(base + L.o_reg);
   P.ecs_slot = g.ecs_slot;

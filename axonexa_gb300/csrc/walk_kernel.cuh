@@ -151,6 +151,20 @@ __device__ __forceinline__ float plane_hit(const float4 &g, float eps, bool on_s
   return s;
 }
 
+// The annulus test of a cylinder list: whether a segment whose midpoint is
+// (mx, my), of length at most the plan's longest step, can come near the
+// cylinder's surface.  Cylinder-lattice plans store (R + h)^2 in geo.z, with
+// h half the longest step plus a slack (1 % of it and 1e-6 of the cell)
+// far above the FP32 rounding of positions; h2x2 = 2 h^2.  The segment lies
+// within the ball of its half length around the midpoint, so a centre
+// distance D with D > R + h (outside) or D < R - h (inside, (R - h)^2 =
+// 2 R^2 + 2 h^2 - (R + h)^2) means no root of the exact test.
+__device__ __forceinline__ bool annulus_keeps(const float4 &g, float mx, float my, float h2x2) {
+  const float ex = mx - g.x, ey = my - g.y;
+  const float d2 = fma_f(ex, ex, ey * ey);
+  return !(d2 > g.z || d2 < fma_f(-2.0f, g.w, h2x2 - g.z));
+}
+
 // The quadratic of one instance along the segment start + s*d, s in
 // [0, rem]: half the linear coefficient bh = p.d and |p|^2 - R^2 at both
 // ends (c0 at the start, c1 at s = rem), p = start - centre.
@@ -396,6 +410,29 @@ __device__ __forceinline__ MoveOut boundary(const WalkParams &P, const Cands<GEO
         seg_coef(C.g0, sph, sx, sy, sz, dx, dy, dz, L, bh1, c01, c11);
         maybe = seg_may_disc(bh1, c01, c11, sph ? aa_s : aa_c, L);
       }
+    } else if constexpr (GEOM == AXX_GEOM_CYL && PERM) {
+      // lists of permeable cylinders: the annulus test first (the segment lies within
+      // L/2 of its midpoint; a cylinder whose surface is farther than that,
+      // plus a slack far above FP32 rounding, cannot be met), then the exact
+      // test on the candidates it keeps
+      const float hl = 0.5f * L;
+      const float mx = fma_f(hl, dx, sx), my = fma_f(hl, dy, sy);
+      uint32_t keep = 0u;
+      bool far = false;  // a candidate past the 32nd kept (always tested)
+      for (uint32_t j = C.b; j < C.e; ++j) {
+        const uint32_t bit = j - C.b;
+        const bool k = annulus_keeps(C.S.geo[C.S.clist[j]], mx, my, P.ann_h2x2);
+        keep |= (k && bit < 32u) ? (1u << bit) : 0u;
+        far |= k && bit >= 32u;
+      }
+      while (keep) {
+        const uint32_t bit = (uint32_t)(__ffs(keep) - 1);
+        keep &= keep - 1u;
+        const int k = C.S.clist[C.b + bit];
+        const bool m = may(C.S.geo[k], C.S.aux[k]);
+        mmask |= m ? (1u << bit) : 0u;
+      }
+      maybe = mmask != 0u || far;
     } else {
       for (uint32_t j = C.b; j < C.e; ++j) {
         const int k = C.S.clist[j];
@@ -439,10 +476,17 @@ __device__ __forceinline__ MoveOut boundary(const WalkParams &P, const Cands<GEO
       bg = C.g0;
       ba = C.a0;
     } else {
+      // after a hit: the annulus test of the remaining segment (cylinder
+      // lists; the instance just hit is tested from its surface)
+      const float hl = 0.5f * rem;
+      const float mx = fma_f(hl, dx, sx), my = fma_f(hl, dy, sy);
       for (uint32_t j = C.b; j < C.e; ++j) {
         const uint32_t bit = j - C.b;
         if (last < 0 && bit < 32u && !((mmask >> bit) & 1u)) continue;
         const int k = C.S.clist[j];
+        if (GEOM == AXX_GEOM_CYL && PERM && last >= 0 && k != last &&
+            !annulus_keeps(C.S.geo[k], mx, my, P.ann_h2x2))
+          continue;
         const float4 aux = C.S.aux[k];
         const bool sph = is_sphere<GEOM>(aux);
         const float s =
@@ -661,8 +705,11 @@ __device__ __forceinline__ void do_move(const WalkParams &P, const SmemView &S,
   // term, .z, is then not read per move)
   constexpr bool fixed_slot = ONE && (single || KM == AXX_KM_LAT_IMP);
   constexpr bool tracked = KM == AXX_KM_LAT_IMP || KM == AXX_KM_LAT_PERM;
-  const float4 s4 = (fixed_slot || tracked) ? make_float4(W.v0, W.L0, W.t2z, 0.0f)
-                                            : S.slot[W.slot];
+  // permeable walks hold their slot's values in registers (reloaded when the
+  // slot changes); impermeable list walks read them per move (the registers
+  // would spill there)
+  constexpr bool cached = fixed_slot || perm;
+  const float4 s4 = cached ? make_float4(W.v0, W.L0, W.t2z, 0.0f) : S.slot[W.slot];
   const float v = s4.x, Lb = s4.y;
   float dx, dy, dz, L = Lb;
   if (PICK) {
@@ -805,10 +852,12 @@ __device__ __forceinline__ void do_move(const WalkParams &P, const SmemView &S,
         W.slot =
             lookup_list<GEOM>(S, S.cstart[cell], S.cstart[cell + 1], P.ecs_slot, fx, fy, fz);
       }
-      const float4 ns = S.slot[W.slot];
-      W.v0 = ns.x;
-      W.L0 = ns.y;
-      W.t2z = ns.z;
+      if (perm) {
+        const float4 ns = S.slot[W.slot];
+        W.v0 = ns.x;
+        W.L0 = ns.y;
+        W.t2z = ns.z;
+      }
     }
     if (perm) {
       if (ONE)
@@ -980,7 +1029,10 @@ __device__ __forceinline__ WalkResult walk_one(const WalkParams &P, const SmemVi
       break;
     }
     float u1, u2;
-    st.next2(P, u1, u2);
+    if (perm)
+      st.next2_eager(P, u1, u2);
+    else
+      st.next2(P, u1, u2);
     do_move<GEOM, KMAX, KM, TRACE, ONE, false, false, PAX>(P, S, T, wid, i, u1, u2, st, W, res,
                                                           g0, a0);
   }
@@ -1050,10 +1102,13 @@ __global__ void __launch_bounds__(AXX_BLOCK, ONEONLY && KMAX <= 4 ? AXX_MIN_BLOC
   const long long gwarp = (long long)blockIdx.x * warps + wib;
   // the sums of this warp: per-warp rows in shared memory, folded into one
   // partial per block at the end, or (warp_rows) the warp's own row of the
-  // partials in global memory
-  const bool rows = P.warp_rows != 0;
-  double *wrow = rows ? P.partials + (size_t)gwarp * Mo * 5 : wsum + (size_t)wib * Mo * 5;
-  if (rows) {
+  // partials in global memory (the row's address is formed where it is used,
+  // so that it holds no register during the walk)
+  auto warp_row = [&]() {
+    return P.warp_rows ? P.partials + (size_t)gwarp * Mo * 5 : wsum + (size_t)wib * Mo * 5;
+  };
+  if (P.warp_rows) {
+    double *wrow = warp_row();
     for (int j = lane; j < Mo * 5; j += 32) wrow[j] = 0.0;
   } else {
     for (int j = threadIdx.x; j < warps * Mo * 5; j += blockDim.x) wsum[j] = 0.0;
@@ -1072,8 +1127,8 @@ __global__ void __launch_bounds__(AXX_BLOCK, ONEONLY && KMAX <= 4 ? AXX_MIN_BLOC
   } else {
     // stage the substrate tables (layout fixed by the host planner); the slot
     // tables, read when a walker's slot changes, stay in global memory
-    float4 *sg = reinterpret_cast<float4 *>(smem + (rows ? 0 : (size_t)warps * Mo * 5 *
-                                                                  sizeof(double)));
+    float4 *sg = reinterpret_cast<float4 *>(smem + (P.warp_rows ? 0 : (size_t)warps * Mo * 5 *
+                                                                          sizeof(double)));
     float4 *sa = sg + P.n_inst;
     uint32_t *sc = reinterpret_cast<uint32_t *>(sa + P.n_inst);
     uint16_t *sl = reinterpret_cast<uint16_t *>(sc + P.ncell + 1);
@@ -1130,6 +1185,7 @@ __global__ void __launch_bounds__(AXX_BLOCK, ONEONLY && KMAX <= 4 ? AXX_MIN_BLOC
 #pragma unroll
     for (int c = 0; c < KMAX; ++c) ph[c] = (double)W.acc[c] - (double)W.cmp[c];
     const double w = exp(-((double)W.t2s - (double)W.t2c));
+    double *wrow = warp_row();
     for (int m = 0; m < M; ++m) {
       double ang = 0.0;
 #pragma unroll
@@ -1164,7 +1220,7 @@ __global__ void __launch_bounds__(AXX_BLOCK, ONEONLY && KMAX <= 4 ? AXX_MIN_BLOC
   if (aborted) atomicAdd(&P.counters[AXX_CNT_ABORTED], (unsigned long long)aborted);
   if (!ONEONLY && start_in)
     atomicAdd(&P.counters[AXX_CNT_START_IN], (unsigned long long)start_in);
-  if (rows) return;  // each warp's row is its partial
+  if (P.warp_rows) return;  // each warp's row is its partial
   __syncthreads();
   for (int j = threadIdx.x; j < Mo * 5; j += blockDim.x) {
     double s = 0.0;
