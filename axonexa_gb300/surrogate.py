@@ -10,14 +10,18 @@ past a sequence's own echo with its phase frozen while T2 keeps acting, so a
 common readout time makes the signal a function of the ten inputs alone.
 
 The network (MLP in -> 4 x 256 SiLU -> 1) lives in libaxx.so: BF16 tensor-core
-training (mma.sync GEMMs, FP32 accumulate, Adam) and tcgen05 inference.  Plain
+training (tcgen05 GEMMs with TMEM accumulators, FP32 accumulate, Adam) and
+tcgen05 inference.  The trained parameters of the 400-cylinder configuration,
+with their held-out pairs and Monte Carlo truth, ship in data/ (load()).  Plain
 Monte Carlo stays the fallback: queries outside the training ranges are
 simulated, not predicted.
 """
 from __future__ import annotations
 
 import ctypes as C
+import json
 import math
+import os
 from dataclasses import dataclass
 from typing import Dict, List, Optional, Tuple
 
@@ -173,7 +177,7 @@ def draw_substrates(n, rng) -> List[SubstrateDraw]:
 
 
 def make_jobs(subs: List[SubstrateDraw], rng, walkers: int, timestep: float,
-              n_cyl: int = 100, waves_per_sub: int = 8, g_per_wave: int = 8):
+              n_cyl: int = 400, waves_per_sub: int = 8, g_per_wave: int = 8):
     """One batch job per substrate: `waves_per_sub` waveforms (Delta, delta,
     omega) x `g_per_wave` amplitudes, all read at TE_READ.  Returns (jobs,
     parameter rows)."""
@@ -209,27 +213,80 @@ MAX_CAP_FRACTION = 1e-8
 
 
 def simulate(jobs: List[Job], device: Device = None, chunk: int = 64,
-             counts: Optional[Dict[str, int]] = None) -> np.ndarray:
+             counts: Optional[Dict[str, int]] = None, method: str = "auto",
+             stderr: Optional[list] = None) -> np.ndarray:
     """Normalised signals |M|/N of every sequence of every job (plain MC).
-    `counts`, when given, accumulates walker_steps and cap_hits."""
+    method "batch": persistent batched launches of `chunk` jobs; "plans": one
+    walk per job (axx_run_lattice: the single-job kernels, faster for large
+    dense packings); "auto": plans when a job holds more than 100 bases.
+    `counts`, when given, accumulates walker_steps and cap_hits; `stderr`,
+    when given, receives each signal's standard error."""
+    from .acquisition import run_lattice
+    if method == "auto":
+        method = "plans" if jobs and max(len(j.basis) for j in jobs) > 100 else "batch"
     out = []
-    for i in range(0, len(jobs), chunk):
-        for r in run_batch(jobs[i:i + chunk], device=device, max_cap_fraction=MAX_CAP_FRACTION):
-            out.append(r.signal)
-            if counts is not None:
-                counts["walker_steps"] = counts.get("walker_steps", 0) + int(r.walker_steps)
-                counts["cap_hits"] = counts.get("cap_hits", 0) + int(r.cap_hits)
+
+    def tally(r):
+        out.append(r.signal)
+        if stderr is not None:
+            stderr.append(r.stderr)
+        if counts is not None:
+            counts["walker_steps"] = counts.get("walker_steps", 0) + int(r.walker_steps)
+            counts["cap_hits"] = counts.get("cap_hits", 0) + int(r.cap_hits)
+
+    if method == "plans":
+        for j in jobs:
+            r = run_lattice(j.lattice, j.basis, j.seqs, j.num_walkers, j.steps, j.timestep,
+                            j.seed, relaxation=j.relaxation, permeable=j.permeable,
+                            device=device, allow_cap=True)
+            if r.cap_hits > MAX_CAP_FRACTION * r.walker_steps:
+                raise N.ReflectionCapError(N.AXX_ERR_REFLECTION_CAP,
+                                           "%d reflection-cap moves" % r.cap_hits)
+            tally(r)
+    else:
+        for i in range(0, len(jobs), chunk):
+            for r in run_batch(jobs[i:i + chunk], device=device,
+                               max_cap_fraction=MAX_CAP_FRACTION):
+                tally(r)
     return np.concatenate(out) if out else np.zeros(0)
 
 
-def generate(n_sub: int, seed: int, walkers: int = 262144, timestep: float = 0.005,
-             n_cyl: int = 100, device: Device = None, counts: Optional[Dict[str, int]] = None):
-    """(parameters [n][10], signals [n]) from n_sub substrates x 64 sequences."""
+def generate(n_sub: int, seed: int, walkers: int = 262144, timestep: float = 0.001,
+             n_cyl: int = 400, device: Device = None, counts: Optional[Dict[str, int]] = None,
+             stderr: Optional[list] = None):
+    """(parameters [n][10], signals [n]) from n_sub substrates x 64 sequences:
+    by default the 400-cylinder gamma packings at dt 1 us of the permeable
+    benchmark substrate, 262,144 walkers per packing."""
     rng = np.random.default_rng(seed)
     subs = draw_substrates(n_sub, rng)
     jobs, P = make_jobs(subs, rng, walkers, timestep, n_cyl)
-    S = simulate(jobs, device=device, counts=counts)
+    S = simulate(jobs, device=device, counts=counts, stderr=stderr)
     return P, S
+
+
+WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "surrogate_400cyl.npz")
+
+
+def save(mlp: MLP, path: str, heldout: Optional[dict] = None, meta: Optional[dict] = None):
+    """The trained parameters (FP32, axx_mlp layout), with the held-out pairs
+    and their Monte Carlo truth when given."""
+    d = {"params": mlp.get_params(), "shape": np.array([mlp.in_dim, mlp.width, mlp.depth])}
+    for k, v in (heldout or {}).items():
+        d["heldout_" + k] = np.asarray(v)
+    if meta:
+        d["meta"] = np.array(json.dumps(meta))
+    np.savez_compressed(path, **d)
+
+
+def load(path: str = WEIGHTS, device: Device = None):
+    """(MLP with the saved parameters, held-out dict, meta dict)."""
+    z = np.load(path)
+    in_dim, width, depth = (int(x) for x in z["shape"])
+    mlp = MLP(in_dim, width, depth, device=device)
+    mlp.set_params(z["params"])
+    held = {k[len("heldout_"):]: z[k] for k in z.files if k.startswith("heldout_")}
+    meta = json.loads(str(z["meta"])) if "meta" in z.files else {}
+    return mlp, held, meta
 
 
 class Surrogate:
@@ -258,8 +315,8 @@ class Surrogate:
         s.loss = np.concatenate(losses)
         return s
 
-    def predict(self, P, fallback_walkers: int = 262144, timestep: float = 0.005,
-                device: Device = None) -> Tuple[np.ndarray, np.ndarray]:
+    def predict(self, P, fallback_walkers: int = 262144, timestep: float = 0.001,
+                device: Device = None, n_cyl: int = 400) -> Tuple[np.ndarray, np.ndarray]:
         """Signals for parameter rows; rows outside the training ranges are
         simulated.  Returns (signals, used_fallback mask)."""
         P = np.asarray(P, np.float64)
@@ -272,8 +329,8 @@ class Surrogate:
             for i in np.nonzero(~ok)[0]:
                 p = P[i]
                 sub = SubstrateDraw(*p[:6])
-                jobs, _ = make_jobs([sub], rng, fallback_walkers, timestep, waves_per_sub=1,
-                                    g_per_wave=1)
+                jobs, _ = make_jobs([sub], rng, fallback_walkers, timestep, n_cyl=n_cyl,
+                                    waves_per_sub=1, g_per_wave=1)
                 jobs[0].seqs = [_sequence(p[6], p[7], p[8], p[9])]
                 out[i] = simulate(jobs, device=device)[0]
         return out, ~ok

@@ -328,18 +328,32 @@ def fma_peak(N, L, dev):
 
 
 def surrogate_section(A, N, L, dev, queries=1000000, reps=10, plain_subs=2):
-    """Learned-surrogate throughput: tcgen05 inference of `queries` rows
-    resident on the GPU (CUDA events on the library stream), the same through
-    the host API (host rows in, host signals out), and the plain walk's
-    signals/s on the surrogate's data-generation jobs (100-cylinder gamma
-    packings, 262,144 walkers, 64 sequences each, dt 5 us)."""
-    import ctypes as C
-
+    """Learned surrogate: the trained network of the 400-cylinder
+    configuration (axonexa_gb300/data) against its held-out pairs' plain
+    Monte Carlo truth (|dS|), tcgen05 inference of `queries` rows resident on
+    the GPU (CUDA events on the library stream), the same through the host API
+    (host rows in, host signals out), and the plain walk's signals/s on the
+    surrogate's own data-generation jobs (400-cylinder gamma packings, 262,144
+    walkers, 64 sequences each, dt 1 us, read at 55 ms)."""
     import numpy as np
     import torch
 
     from axonexa_gb300 import surrogate as S
-    m = S.MLP(seed=0, device=dev)
+    out = {}
+    if os.path.exists(S.WEIGHTS):
+        m, held, meta = S.load(device=dev)
+        pred = m.predict(S.normalise(held["P"]))
+        err = np.abs(pred - held["truth"])
+        out.update({"weights": os.path.relpath(S.WEIGHTS, ROOT), "trained_on": meta,
+                    "heldout_pairs": int(len(err)),
+                    "heldout_truth_se_mean": float(np.mean(held["truth_se"])),
+                    "heldout_abs_dS_mean": float(err.mean()),
+                    "heldout_abs_dS_p95": float(np.quantile(err, 0.95)),
+                    "heldout_abs_dS_max": float(err.max()),
+                    "heldout_frac_within_2e-3": float(np.mean(err <= 2e-3))})
+    else:
+        m = S.MLP(seed=0, device=dev)
+        out["weights"] = "untrained (no saved weights): throughput only"
     g = torch.Generator(device="cuda")
     g.manual_seed(SEED2)
     X = torch.rand(queries, 10, device="cuda", generator=g) * 2 - 1
@@ -360,25 +374,25 @@ def surrogate_section(A, N, L, dev, queries=1000000, reps=10, plain_subs=2):
     assert np.array_equal(yh, y.cpu().numpy()), "host and device inference disagree"
     peaks = measured_peaks()
     pk = peaks.get("bf16_tflops")
-    out = {"queries": queries, "signals_per_s": queries / (ms * 1e-3), "ms": ms,
-           "e2e_signals_per_s": queries / e2e_s, "h2d_bytes": int(Xh.nbytes),
-           "d2h_bytes": int(4 * queries), "kernel_launches_per_call": 1,
-           "roofline": {"bound": "tensor", "achieved": flops / (ms * 1e-3) / 1e12,
-                        "peak": pk, "unit": "TFLOP/s",
-                        "frac": (flops / (ms * 1e-3) / 1e12 / pk) if pk else None,
-                        "peak_source": "measured bf16 GEMM burst" if pk else None,
-                        "flops_per_row": m.flops_per_row()}}
+    out.update({"queries": queries, "signals_per_s": queries / (ms * 1e-3), "ms": ms,
+                "e2e_signals_per_s": queries / e2e_s, "h2d_bytes": int(Xh.nbytes),
+                "d2h_bytes": int(4 * queries), "kernel_launches_per_call": 1,
+                "roofline": {"bound": "tensor", "achieved": flops / (ms * 1e-3) / 1e12,
+                             "peak": pk, "unit": "TFLOP/s",
+                             "frac": (flops / (ms * 1e-3) / 1e12 / pk) if pk else None,
+                             "peak_source": "measured bf16 GEMM burst" if pk else None,
+                             "flops_per_row": m.flops_per_row()}})
     m.close()
     if plain_subs > 0:
         rng = np.random.default_rng(SEED2)
         subs = S.draw_substrates(plain_subs, rng)
-        jobs, P = S.make_jobs(subs, rng, 262144, 0.005, 100)
-        S.simulate(jobs, device=dev)  # same batch shape: tunes (cached) and warms up
+        jobs, P = S.make_jobs(subs, rng, 262144, 0.001, 400)
         t0 = time.perf_counter()
         sig = S.simulate(jobs, device=dev)
         t_mc = time.perf_counter() - t0
         out["plain_signals_per_s"] = len(sig) / t_mc
-        out["plain_job"] = "%d gamma packings x 64 sequences x 262,144 walkers, dt 5 us" % plain_subs
+        out["plain_job"] = ("%d 400-cylinder gamma packings x 64 sequences x 262,144 walkers, "
+                            "dt 1 us, 55,001 steps" % plain_subs)
         out["speedup_vs_plain"] = out["signals_per_s"] / out["plain_signals_per_s"]
     return out
 

@@ -132,5 +132,5 @@ def test_surrogate_gain_over_plain_monte_carlo(dev):
     # out-of-range queries are simulated instead of predicted
     out = Ph[:2].copy()
     out[:, 0] = 6.0  # mean radius beyond the training range
-    val, fb = sur.predict(out, fallback_walkers=4096, timestep=dt)
+    val, fb = sur.predict(out, fallback_walkers=4096, timestep=dt, n_cyl=40)
     assert fb.all() and np.all((val > 0) & (val <= 1.0))
