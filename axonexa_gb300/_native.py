@@ -69,6 +69,12 @@ class Stats(C.Structure):
                 ("walkers_in", C.c_int64)]
 
 
+class PackSpec(C.Structure):
+    _fields_ = [("shape", C.c_double), ("mean", C.c_double), ("rmin", C.c_double),
+                ("rmax", C.c_double), ("fraction", C.c_double), ("D", C.c_double),
+                ("T2", C.c_double), ("permeability", C.c_double)]
+
+
 class MeshRec(C.Structure):
     _fields_ = [("vertices", C.POINTER(C.c_double)), ("nvert", C.c_int32),
                 ("triangles", C.POINTER(C.c_int32)), ("ntri", C.c_int32), ("D", C.c_double)]
@@ -184,6 +190,10 @@ _SIGS = {
                             C.c_double, C.c_double, C.c_int, C.POINTER(Basis),
                             C.POINTER(C.c_int), C.POINTER(C.c_double),
                             C.POINTER(C.c_double)], C.c_int),
+    "axx_substrate_rps_gamma_gpu": ([C.c_void_p, C.c_uint64, C.c_int, C.c_int,
+                                     C.POINTER(PackSpec), C.c_int, C.POINTER(Basis),
+                                     C.POINTER(C.c_int), C.POINTER(C.c_double),
+                                     C.POINTER(C.c_double)], C.c_int),
     "axx_volume_fraction": ([C.c_void_p, C.POINTER(LatticeRec), C.POINTER(Basis), C.c_int,
                              C.c_int64, C.c_uint64, C.POINTER(C.c_double),
                              C.POINTER(C.c_int64)], C.c_int),

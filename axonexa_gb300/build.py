@@ -38,6 +38,7 @@ CUDA_SOURCES = [
     "calcf.cu",
     "wc.cu",
     "mesh.cu",
+    "pack.cu",
 ]
 HOST_SOURCES = ["api.cpp", "frame.cpp", "host_plan.cpp", "plan_layout.cpp", "substrate.cpp"]
 

@@ -8,8 +8,10 @@
 // (correctEdges :131-186, circleIntersectsLattice :251-276).  The cell side is
 // chosen so that the cylinders' area fraction is the requested one.  When
 // random sequential addition cannot place every cylinder at that density
-// (its jamming limit is near 0.55 for equal discs), the centres are relaxed
-// by pairwise periodic overlap removal until no two cylinders overlap.  Every
+// (its jamming limit is near 0.55 for equal discs), it places them at a lower
+// fraction and the cell is compressed to the requested one in small steps,
+// each followed by pairwise periodic overlap removal until no two cylinders
+// overlap.  Every
 // pair keeps a gap of 1 % of its radius sum (kGap).
 //
 // Randomness: SplitMix64 (Steele, Lea, Flood, OOPSLA 2014) for uniforms,
@@ -76,7 +78,8 @@ bool overlaps(const std::vector<double> &x, const std::vector<double> &y,
 }
 
 // Pairwise overlap removal: each pair closer than the minimum separation
-// moves apart along its centre line by half the shortfall (plus 0.1 %).
+// moves apart along its centre line by half the shortfall (plus 0.1 % and
+// 1e-9 of the cell).
 // Returns true when every pair is separated.
 bool relax(std::vector<double> &x, std::vector<double> &y, const std::vector<double> &r,
            double L, int iters) {
@@ -97,7 +100,9 @@ bool relax(std::vector<double> &x, std::vector<double> &y, const std::vector<dou
           d = 1.0;
           d2 = 0.0;
         }
-        const double push = 0.5 * (s - std::sqrt(d2)) * 1.001;
+        // plus 1e-9 of the cell: an overlap below the rounding of the
+        // centres would otherwise be pushed by less than one ulp, forever
+        const double push = 0.5 * (s - std::sqrt(d2)) * 1.001 + 1e-9 * L;
         const double ux = dx / d, uy = dy / d;
         x[i] += push * ux;
         y[i] += push * uy;
@@ -140,40 +145,56 @@ extern "C" axx_status axx_substrate_pack(uint64_t seed, int n, const double *rad
   for (double v : r) area += 3.141592653589793 * v * v;
   const double L = std::sqrt(area / fraction);
   std::vector<double> x(n), y(n);
-  // random sequential addition, largest radius first (index n-1 down to 0)
-  bool placed = true;
   std::vector<int> order(n);
   for (int i = 0; i < n; ++i) order[i] = n - 1 - i;
-  std::vector<double> px, py, pr;
-  for (int idx = 0; idx < n && placed; ++idx) {
-    const int i = order[idx];
-    bool ok = false;
-    for (int t = 0; t < 2000 && !ok; ++t) {
-      px.push_back(rng.uniform() * L);
-      py.push_back(rng.uniform() * L);
-      pr.push_back(r[i]);
-      const int me = (int)px.size() - 1;
-      if (!overlaps(px, py, pr, me, me, L)) {
-        ok = true;
-      } else {
-        px.pop_back();
-        py.pop_back();
-        pr.pop_back();
+  // random sequential addition, largest radius first (index n-1 down to 0),
+  // in a cell of side Lc; false when a cylinder finds no place in 2,000 draws
+  auto rsa = [&](double Lc) {
+    std::vector<double> px, py, pr;
+    for (int idx = 0; idx < n; ++idx) {
+      const int i = order[idx];
+      bool ok = false;
+      for (int t = 0; t < 2000 && !ok; ++t) {
+        px.push_back(rng.uniform() * Lc);
+        py.push_back(rng.uniform() * Lc);
+        pr.push_back(r[i]);
+        const int me = (int)px.size() - 1;
+        if (!overlaps(px, py, pr, me, me, Lc)) {
+          ok = true;
+        } else {
+          px.pop_back();
+          py.pop_back();
+          pr.pop_back();
+        }
       }
+      if (!ok) return false;
     }
-    if (!ok) placed = false;
-  }
-  if (placed) {
     for (int idx = 0; idx < n; ++idx) {
       x[order[idx]] = px[idx];
       y[order[idx]] = py[idx];
     }
-  } else {
-    for (int i = 0; i < n; ++i) {
-      x[i] = rng.uniform() * L;
-      y[i] = rng.uniform() * L;
+    return true;
+  };
+  if (!rsa(L)) {
+    // Addition jammed (its limit is near 0.55 for equal discs): add at a
+    // lower fraction, then compress the cell in steps of 0.01 in fraction,
+    // scaling the centres with it and removing the overlaps after each step.
+    double fc = std::min(0.5, fraction);
+    while (!rsa(std::sqrt(area / fc))) {
+      fc -= 0.05;
+      if (fc < 0.1) return AXX_ERR_UNSUPPORTED;
     }
-    if (!relax(x, y, r, L, 20000)) return AXX_ERR_UNSUPPORTED;
+    double Lc = std::sqrt(area / fc);
+    while (fc < fraction) {
+      fc = std::min(fraction, fc + 0.01);
+      const double Ln = fc == fraction ? L : std::sqrt(area / fc);
+      for (int i = 0; i < n; ++i) {
+        x[i] *= Ln / Lc;
+        y[i] *= Ln / Lc;
+      }
+      Lc = Ln;
+      if (!relax(x, y, r, Lc, 20000)) return AXX_ERR_UNSUPPORTED;
+    }
   }
   // originals, then images of the cylinders that cross the cell edge
   int cnt = 0;

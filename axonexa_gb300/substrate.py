@@ -29,6 +29,35 @@ def rps_gamma_pack(seed: int, n: int, shape: float, mean: float, fraction: float
     return _packing(out, nout, side, ach, T2_ex, D_ex)
 
 
+def rps_gamma_pack_gpu(seed: int, n: int, specs, *, T2_ex: float, D_ex: float, device=None):
+    """Many gamma packings at once on the GPU (axx_substrate_rps_gamma_gpu).
+    specs: one dict per packing with shape, mean, fraction, D_in, T2_in and
+    optionally permeability, rmin, rmax (defaults as rps_gamma_pack).
+    Returns [(Lattice, [Cylinder_XY...], achieved_fraction), ...]."""
+    from .acquisition import default_device
+    dev = device or default_device()
+    npack = len(specs)
+    arr = (N.PackSpec * npack)()
+    for i, s in enumerate(specs):
+        mean = s["mean"]
+        arr[i] = N.PackSpec(s["shape"], mean, s.get("rmin", mean * 0.05), s.get("rmax", mean * 4.0),
+                            s["fraction"], s["D_in"], s["T2_in"], s.get("permeability", 0.0))
+    cap = n * 4
+    out = (N.Basis * (cap * npack))()
+    nout = (C.c_int * npack)()
+    side = (C.c_double * npack)()
+    ach = (C.c_double * npack)()
+    N.check(N.lib().axx_substrate_rps_gamma_gpu(dev.h, seed, n, npack, arr, cap, out, nout, side,
+                                                ach), dev.h)
+    res = []
+    base = C.addressof(out)
+    for p in range(npack):
+        view = (N.Basis * cap).from_address(base + p * cap * C.sizeof(N.Basis))
+        res.append(_packing(view, C.c_int(nout[p]), C.c_double(side[p]), C.c_double(ach[p]),
+                            T2_ex, D_ex))
+    return res
+
+
 def pack_radii(seed: int, radii, fraction: float, *, D_in: float, T2_in: float, D_ex: float,
                T2_ex: float, permeability: float = 0.0):
     """The placement step of rps_gamma_pack for given radii

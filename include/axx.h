@@ -419,6 +419,31 @@ axx_status axx_substrate_rps_gamma(uint64_t seed, int n, double shape, double me
                                    int max_out, axx_basis *out, int *nout, double *side,
                                    double *achieved);
 
+/* One packing of axx_substrate_rps_gamma_gpu: n radii from gamma(shape,
+ * mean/shape) truncated to (rmin, rmax); the cell side makes the cylinders'
+ * area `fraction` of the cell; every cylinder gets D, T2 and permeability. */
+typedef struct {
+  double shape, mean;
+  double rmin, rmax;
+  double fraction;
+  double D, T2, permeability;
+} axx_pack_spec;
+
+/* RPSLatticeInitializer (src/substrate/RPSinitializer.h:10-314) on the GPU,
+ * npack packings of n cylinders at once (n <= 2048): gamma radii sampled on
+ * the device (gammaRadialDist :76-101), random sequential addition largest
+ * first with the periodic overlap test and a 1 % gap (uniformCenterDist
+ * :103-129), pairwise overlap removal when addition jams, periodic images of
+ * the cylinders that cross the cell edge (correctEdges :131-186).  Packing p's
+ * bases (the n cylinders by ascending radius, region = index + 1, then the
+ * images) go to out[p * max_out ...], their count to nout[p], the cell side
+ * to side[p] and the area fraction to achieved[p].  The same algorithm as
+ * axx_substrate_rps_gamma with the device's own draws: packings agree with
+ * the host packer's in distribution. */
+axx_status axx_substrate_rps_gamma_gpu(axx_ctx *ctx, uint64_t seed, int n, int npack,
+                                       const axx_pack_spec *spec, int max_out, axx_basis *out,
+                                       int *nout, double *side, double *achieved);
+
 /* Monte Carlo intracellular volume fraction (calcf / kernelCalcf,
  * src/util/calcf.cuh:1-38): `points` uniform points in the cell (point i uses
  * words 1..3 of stream (seed, i), as a walker's start), counted when the first
