@@ -304,7 +304,17 @@ uint64_t fnv(uint64_t h, uint64_t v) {
 }
 
 // Shape of a batch for the tuning cache.
+// The batch's shape for the autotuner's cache: per job its mode, walkers,
+// steps, flags and timestep, its substrate (cell, basis types and radii:
+// instances, grid lists and hit rates follow from them) and its sequences'
+// waveforms and directions (the channel capacity follows from them; the
+// amplitudes G do not change the cost).
 uint64_t batch_shape(const axx_job *jobs, int njobs) {
+  auto bits = [](double v) {
+    uint64_t u;
+    std::memcpy(&u, &v, 8);
+    return u;
+  };
   uint64_t h = 1469598103934665603ull;
   h = fnv(h, (uint64_t)njobs);
   for (int j = 0; j < njobs; ++j) {
@@ -315,6 +325,26 @@ uint64_t batch_shape(const axx_job *jobs, int njobs) {
     h = fnv(h, (uint64_t)J.nbasis);
     h = fnv(h, (uint64_t)J.nseq);
     h = fnv(h, (uint64_t)J.params.flags);
+    h = fnv(h, bits(J.params.timestep));
+    if (J.mode == 0) {
+      h = fnv(h, bits(J.lattice.a));
+      h = fnv(h, bits(J.lattice.b));
+      h = fnv(h, bits(J.lattice.c));
+    }
+    for (int k = 0; k < J.nbasis && J.basis; ++k) {
+      h = fnv(h, (uint64_t)J.basis[k].type);
+      h = fnv(h, bits(J.basis[k].radius));
+    }
+    for (int m = 0; m < J.nseq && J.seqs; ++m) {
+      const axx_sequence &q = J.seqs[m];
+      h = fnv(h, (uint64_t)q.kind);
+      h = fnv(h, (uint64_t)q.num_periods);
+      h = fnv(h, bits(q.duration));
+      h = fnv(h, bits(q.spacing));
+      h = fnv(h, bits(q.gx));
+      h = fnv(h, bits(q.gy));
+      h = fnv(h, bits(q.gz));
+    }
   }
   return h;
 }

@@ -427,15 +427,31 @@ std::string plan_lattice(const axx_lattice *lat, const axx_basis *basis, int nba
     }
     return false;
   };
+  // image offsets along one axis that can bring a basis within reach of the
+  // cell: every offset whose translate of [c - R, c + R] meets the dilated
+  // cell (one cell each way for a basis inside the cell and smaller than it;
+  // more for a basis centred far outside or larger than a cell side).  A
+  // plane's images along its normal: one each way is enough for the walls
+  // of a cell.
+  auto offsets = [&](double c, double R, double side, int &lo, int &hi) {
+    lo = std::max(-64, (int)std::floor((-dil - R - c) / side));
+    hi = std::min(64, (int)std::ceil((side + dil + R - c) / side));
+  };
   for (int k = 0; k < nbasis; ++k) {
     const axx_basis &b = basis[k];
     Inst q0{k, b.cx, b.cy, b.cz, b.radius, b.type, {0.0, 0.0, 0.0}};
     if (b.type == AXX_PRIM_PLANE) unit_normal(b, q0.n);
     inst.push_back(q0);
-    const int zr = b.type == AXX_PRIM_CYLINDER_Z ? 0 : 1;
-    for (int i = -1; i <= 1; ++i)
-      for (int j = -1; j <= 1; ++j)
-        for (int l = -zr; l <= zr; ++l) {
+    int i0 = -1, i1 = 1, j0 = -1, j1 = 1, l0 = -1, l1 = 1;
+    if (b.type != AXX_PRIM_PLANE) {
+      offsets(b.cx, b.radius, A, i0, i1);
+      offsets(b.cy, b.radius, B, j0, j1);
+      offsets(b.cz, b.radius, C, l0, l1);
+    }
+    if (b.type == AXX_PRIM_CYLINDER_Z) l0 = l1 = 0;
+    for (int i = i0; i <= i1; ++i)
+      for (int j = j0; j <= j1; ++j)
+        for (int l = l0; l <= l1; ++l) {
           if (i == 0 && j == 0 && l == 0) continue;
           Inst q = q0;
           q.cx += A * i;

@@ -447,3 +447,21 @@ def test_philox_device_stream(dev, orc):
     for seed, w in ((1234, 0), (1234, 65535), (2 ** 40 + 3, 12345678901)):
         np.testing.assert_array_equal(A.philox_words(seed, w, 64, device=dev),
                                       orc.stream_words(seed, w, 64))
+
+
+def test_basis_centred_beyond_one_cell_gets_its_images(dev):
+    """A basis centred more than a cell side outside the cell has reachable
+    periodic images two or three cells away: the walk equals the walk of the
+    same cylinder given inside the cell (its nearest image), move for move."""
+    import axonexa_gb300 as A
+    c, r = 0.010, 0.003
+    lat = A.Lattice(c, c, c, 60.0, 0.0, 2e-6, 1)
+    inside = [A.Cylinder_XY(0.005, 0.005, r, 80.0, 0.0, 2e-6, 1, 0.0)]
+    far = [A.Cylinder_XY(0.005 - 2 * c, 0.005 + 3 * c, r, 80.0, 0.0, 2e-6, 1, 0.0)]
+    kw = dict(relaxation=True, device=dev)
+    a = A.trace_lattice(lat, inside, 64, 1500, 0.002, 21, **kw)
+    b = A.trace_lattice(lat, far, 64, 1500, 0.002, 21, **kw)
+    for k in ("region", "hits", "words"):
+        assert np.array_equal(a[k], b[k]), k
+    assert np.array_equal(a["pos"], b["pos"])
+    assert a["hits"].sum() > 0
