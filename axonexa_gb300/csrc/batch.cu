@@ -44,8 +44,6 @@ constexpr int kBatchMaxSeq = 64;  // sequences per job (shared-memory sums)
 struct BatchJob {
   WalkParams P;       // tables point into the batch arena
   int one;            // single-instance path
-  int sph;            // a single pore that is a sphere (else a cylinder)
-  int cyl;            // a lattice of cylinders along z only
   int M;
   long long part_off; // first partial (in doubles) of this job's items
   long long out_off;  // first output (in doubles) of this job
@@ -59,8 +57,27 @@ struct BatchItem {
   int pad;
 };
 
-template <int KMAX>
-__global__ void __launch_bounds__(AXX_BLOCK, AXX_MIN_BLOCKS_FOR(KMAX))
+// Job classes: each runs its own instantiation of the batch kernel, compiled
+// for the geometry and walk of its jobs alone (fewer code paths, so fewer
+// registers) at the channel capacity of its own jobs.
+enum { BC_SCYL = 0,  // single cylinder pores
+       BC_SSPH = 1,  // single sphere pores
+       BC_LCYL = 2,  // lattices of cylinders along z
+       BC_LMIX = 3,  // other lattices (spheres, mixed types, planes)
+       BC_N = 4 };
+
+// Resident blocks per SM the register budget targets: single pores as the
+// single-instance walk kernels; lattices one block fewer than the list walks
+// from eight channels up (the job switching and the staged parameters cost
+// registers the list walk spills without).
+constexpr int batch_min_blocks(int kmax, int cls) {
+  return (cls <= BC_SSPH && kmax <= 4) ? AXX_MIN_BLOCKS + 1
+         : (cls >= BC_LCYL && kmax >= 8) ? 5
+                                         : AXX_MIN_BLOCKS_FOR(kmax);
+}
+
+template <int KMAX, int CLS>
+__global__ void __launch_bounds__(AXX_BLOCK, batch_min_blocks(KMAX, CLS))
     batch_kernel(const BatchJob *__restrict__ jobs, const BatchItem *__restrict__ items,
                  int nitems, unsigned *item_counter, double *partials) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -70,7 +87,7 @@ __global__ void __launch_bounds__(AXX_BLOCK, AXX_MIN_BLOCKS_FOR(KMAX))
   double *wsum = reinterpret_cast<double *>(smem + p_bytes);
   unsigned char *geo_base = smem + p_bytes + (size_t)warps * kBatchMaxSeq * 5 * sizeof(double);
   __shared__ int s_item;
-  __shared__ int s_one, s_sph, s_cyl;
+  __shared__ int s_one;
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   int cur = -1;
   TraceParams T{};
@@ -88,8 +105,6 @@ __global__ void __launch_bounds__(AXX_BLOCK, AXX_MIN_BLOCKS_FOR(KMAX))
       for (int j = threadIdx.x; j < (int)(sizeof(WalkParams) / 4); j += blockDim.x) dst[j] = src[j];
       if (threadIdx.x == 0) {
         s_one = jobs[item.job].one;
-        s_sph = jobs[item.job].sph;
-        s_cyl = jobs[item.job].cyl;
       }
       __syncthreads();
       float4 *sg = reinterpret_cast<float4 *>(geo_base);
@@ -132,23 +147,32 @@ __global__ void __launch_bounds__(AXX_BLOCK, AXX_MIN_BLOCKS_FOR(KMAX))
       W.t2s = W.t2c = 0.0f;
       if (active) {
         WalkResult r{0u, 0u, false, false};
-        switch (sP.km) {
-          // lattices: the list walk compiled for cylinders when every instance
-          // is one (no per-candidate type tests), else the mixed-type walk
-          case AXX_KM_LAT_IMP:
-            r = one     ? walk_one<AXX_GEOM_MIX, KMAX, AXX_KM_LAT_IMP, false, true>(sP, S, T, wid, W)
-                : s_cyl ? walk_one<AXX_GEOM_CYL, KMAX, AXX_KM_LAT_IMP, false, false>(sP, S, T, wid, W)
-                        : walk_one<AXX_GEOM_MIX, KMAX, AXX_KM_LAT_IMP, false, false>(sP, S, T, wid, W);
-            break;
-          case AXX_KM_LAT_PERM:
-            r = one     ? walk_one<AXX_GEOM_MIX, KMAX, AXX_KM_LAT_PERM, false, true>(sP, S, T, wid, W)
-                : s_cyl ? walk_one<AXX_GEOM_CYL, KMAX, AXX_KM_LAT_PERM, false, false>(sP, S, T, wid, W)
-                        : walk_one<AXX_GEOM_MIX, KMAX, AXX_KM_LAT_PERM, false, false>(sP, S, T, wid, W);
-            break;
-          default:  // a single pore: a cylinder or a sphere, compiled for each
-            r = s_sph ? walk_one<AXX_GEOM_SPH, KMAX, AXX_KM_SINGLE, false, true>(sP, S, T, wid, W)
-                      : walk_one<AXX_GEOM_CYL, KMAX, AXX_KM_SINGLE, false, true>(sP, S, T, wid, W);
-            break;
+        if constexpr (CLS == BC_SCYL) {
+          r = walk_one<AXX_GEOM_CYL, KMAX, AXX_KM_SINGLE, false, true>(sP, S, T, wid, W);
+        } else if constexpr (CLS == BC_SSPH) {
+          r = walk_one<AXX_GEOM_SPH, KMAX, AXX_KM_SINGLE, false, true>(sP, S, T, wid, W);
+        } else if constexpr (CLS == BC_LCYL) {
+          // the single-instance walk up to four channels (as the single-job
+          // kernels), the list walk otherwise and above
+          constexpr bool one_ok = KMAX <= 4;
+          if (sP.km == AXX_KM_LAT_PERM) {
+            r = (one_ok && one)
+                    ? walk_one<AXX_GEOM_CYL, KMAX, AXX_KM_LAT_PERM, false, one_ok>(sP, S, T, wid, W)
+                    : walk_one<AXX_GEOM_CYL, KMAX, AXX_KM_LAT_PERM, false, false>(sP, S, T, wid, W);
+          } else {
+            r = (one_ok && one)
+                    ? walk_one<AXX_GEOM_CYL, KMAX, AXX_KM_LAT_IMP, false, one_ok>(sP, S, T, wid, W)
+                    : walk_one<AXX_GEOM_CYL, KMAX, AXX_KM_LAT_IMP, false, false>(sP, S, T, wid, W);
+          }
+        } else {
+          // other lattices: the mixed-type walk (single instance or list)
+          if (sP.km == AXX_KM_LAT_PERM) {
+            r = one ? walk_one<AXX_GEOM_MIX, KMAX, AXX_KM_LAT_PERM, false, true>(sP, S, T, wid, W)
+                    : walk_one<AXX_GEOM_MIX, KMAX, AXX_KM_LAT_PERM, false, false>(sP, S, T, wid, W);
+          } else {
+            r = one ? walk_one<AXX_GEOM_MIX, KMAX, AXX_KM_LAT_IMP, false, true>(sP, S, T, wid, W)
+                    : walk_one<AXX_GEOM_MIX, KMAX, AXX_KM_LAT_IMP, false, false>(sP, S, T, wid, W);
+          }
         }
         caps += r.caps;
         hits += r.hits;
@@ -216,43 +240,66 @@ __global__ void __launch_bounds__(256)
   if (threadIdx.x == 0) out[J.out_off + jm.y] = red[0];
 }
 
-template <int KMAX>
+template <int KMAX, int CLS>
 static cudaError_t batch_prepare(size_t smem) {
   if (smem > 48 * 1024)
-    return cudaFuncSetAttribute(batch_kernel<KMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)smem);
+    return cudaFuncSetAttribute(batch_kernel<KMAX, CLS>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   return cudaSuccess;
 }
 
-template <int KMAX>
+template <int KMAX, int CLS>
 static int batch_occ(size_t smem) {
-  if (batch_prepare<KMAX>(smem) != cudaSuccess) return 0;
+  if (batch_prepare<KMAX, CLS>(smem) != cudaSuccess) return 0;
   int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_kernel<KMAX>, AXX_BLOCK, smem) !=
-      cudaSuccess)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_kernel<KMAX, CLS>, AXX_BLOCK,
+                                                    smem) != cudaSuccess)
     return 0;
   return n;
 }
 
-static cudaError_t batch_go(int kmax, int grid, size_t smem, cudaStream_t s, const BatchJob *jobs,
-                            const BatchItem *items, int nitems, unsigned *ctr, double *part) {
+template <int CLS>
+static cudaError_t batch_go_cls(int kmax, int grid, size_t smem, cudaStream_t s,
+                                const BatchJob *jobs, const BatchItem *items, int nitems,
+                                unsigned *ctr, double *part) {
   switch (kmax) {
-    case 1: batch_kernel<1><<<grid, AXX_BLOCK, smem, s>>>(jobs, items, nitems, ctr, part); break;
-    case 2: batch_kernel<2><<<grid, AXX_BLOCK, smem, s>>>(jobs, items, nitems, ctr, part); break;
-    case 4: batch_kernel<4><<<grid, AXX_BLOCK, smem, s>>>(jobs, items, nitems, ctr, part); break;
-    case 8: batch_kernel<8><<<grid, AXX_BLOCK, smem, s>>>(jobs, items, nitems, ctr, part); break;
-    default: batch_kernel<16><<<grid, AXX_BLOCK, smem, s>>>(jobs, items, nitems, ctr, part); break;
+    case 1: batch_kernel<1, CLS><<<grid, AXX_BLOCK, smem, s>>>(jobs, items, nitems, ctr, part); break;
+    case 2: batch_kernel<2, CLS><<<grid, AXX_BLOCK, smem, s>>>(jobs, items, nitems, ctr, part); break;
+    case 4: batch_kernel<4, CLS><<<grid, AXX_BLOCK, smem, s>>>(jobs, items, nitems, ctr, part); break;
+    case 8: batch_kernel<8, CLS><<<grid, AXX_BLOCK, smem, s>>>(jobs, items, nitems, ctr, part); break;
+    default: batch_kernel<16, CLS><<<grid, AXX_BLOCK, smem, s>>>(jobs, items, nitems, ctr, part); break;
   }
   return cudaGetLastError();
 }
 
-static int batch_occupancy(int kmax, size_t smem) {
+static cudaError_t batch_go(int cls, int kmax, int grid, size_t smem, cudaStream_t s,
+                            const BatchJob *jobs, const BatchItem *items, int nitems,
+                            unsigned *ctr, double *part) {
+  switch (cls) {
+    case BC_SCYL: return batch_go_cls<BC_SCYL>(kmax, grid, smem, s, jobs, items, nitems, ctr, part);
+    case BC_SSPH: return batch_go_cls<BC_SSPH>(kmax, grid, smem, s, jobs, items, nitems, ctr, part);
+    case BC_LCYL: return batch_go_cls<BC_LCYL>(kmax, grid, smem, s, jobs, items, nitems, ctr, part);
+    default: return batch_go_cls<BC_LMIX>(kmax, grid, smem, s, jobs, items, nitems, ctr, part);
+  }
+}
+
+template <int CLS>
+static int batch_occupancy_cls(int kmax, size_t smem) {
   switch (kmax) {
-    case 1: return batch_occ<1>(smem);
-    case 2: return batch_occ<2>(smem);
-    case 4: return batch_occ<4>(smem);
-    case 8: return batch_occ<8>(smem);
-    default: return batch_occ<16>(smem);
+    case 1: return batch_occ<1, CLS>(smem);
+    case 2: return batch_occ<2, CLS>(smem);
+    case 4: return batch_occ<4, CLS>(smem);
+    case 8: return batch_occ<8, CLS>(smem);
+    default: return batch_occ<16, CLS>(smem);
+  }
+}
+
+static int batch_occupancy(int cls, int kmax, size_t smem) {
+  switch (cls) {
+    case BC_SCYL: return batch_occupancy_cls<BC_SCYL>(kmax, smem);
+    case BC_SSPH: return batch_occupancy_cls<BC_SSPH>(kmax, smem);
+    case BC_LCYL: return batch_occupancy_cls<BC_LCYL>(kmax, smem);
+    default: return batch_occupancy_cls<BC_LMIX>(kmax, smem);
   }
 }
 
@@ -264,6 +311,14 @@ struct axx_batch {
   axx_ctx *ctx = nullptr;
   int njobs = 0, nitems = 0, kmax = 1, tile = 0, bps = 0, grid = 0, nout = 0;
   size_t smem = 0;
+  // per job class (BC_*): its channel capacity, shared memory, grid, item
+  // range, resident blocks per SM; classes without items are skipped
+  int c_kmax[BC_N] = {}, c_grid[BC_N] = {}, c_first[BC_N] = {}, c_items[BC_N] = {},
+      c_bps[BC_N] = {};
+  size_t c_smem[BC_N] = {};
+  // the classes run concurrently: forked from the context stream onto these
+  cudaStream_t cs[BC_N] = {};
+  cudaEvent_t fork = nullptr, join[BC_N] = {};
   void *arena = nullptr;
   BatchJob *d_jobs = nullptr;
   BatchItem *d_items = nullptr;
@@ -453,6 +508,30 @@ extern "C" axx_status axx_autotune_batch(axx_ctx *ctx, const axx_job *jobs, int 
   return AXX_OK;
 }
 
+// The batch's work on stream s: counters reset, the class kernels forked onto
+// their streams (they run concurrently, each over its own items) and joined
+// back, then the per-job reduction.
+static cudaError_t batch_enqueue(axx_batch *b, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(b->d_ctr, 0, 16, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b->d_counters, 0, 8 * AXX_CNT_N * b->njobs, s);
+  if (e == cudaSuccess) e = cudaEventRecord(b->fork, s);
+  for (int c = 0; c < BC_N && e == cudaSuccess; ++c) {
+    if (b->c_items[c] == 0) continue;
+    e = cudaStreamWaitEvent(b->cs[c], b->fork, 0);
+    if (e == cudaSuccess)
+      e = batch_go(c, b->c_kmax[c], b->c_grid[c], b->c_smem[c], b->cs[c], b->d_jobs,
+                   b->d_items + b->c_first[c], b->c_items[c], b->d_ctr + c, b->d_part);
+    if (e == cudaSuccess) e = cudaEventRecord(b->join[c], b->cs[c]);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, b->join[c], 0);
+  }
+  if (e == cudaSuccess && b->nout > 0) {
+    batch_reduce_kernel<<<b->nout, 256, 0, s>>>(b->d_jobs, b->d_outmap, b->d_jobitems, b->d_part,
+                                                b->d_out);
+    e = cudaGetLastError();
+  }
+  return e;
+}
+
 static axx_status batch_build(axx_ctx *ctx, const axx_job *jobs, int njobs,
                               const axx_batch_options &opt, int steps_cap, axx_batch **out) {
   *out = nullptr;
@@ -466,11 +545,13 @@ static axx_status batch_build(axx_ctx *ctx, const axx_job *jobs, int njobs,
     InitSpec init;
     axx_run_params p;
     int mode;
+    int cls;  // BC_*
     double cell[3];
     Frame f;  // arbitrary-axis cylinders: the job in the cylinders' frame
   };
   std::vector<JobPlan> jp(njobs);
   int kmax = 1;
+  int ckmax[BC_N] = {1, 1, 1, 1};
   for (int j = 0; j < njobs; ++j) {
     const axx_job &J = jobs[j];
     JobPlan &q = jp[j];
@@ -507,26 +588,34 @@ static axx_status batch_build(axx_ctx *ctx, const axx_job *jobs, int njobs,
     }
     if (err.empty()) err = plan_sequences(q.f.seqs_p, J.nseq, p.steps, p.timestep, gamma, q.sq);
     if (!err.empty()) return bfail(ctx, AXX_ERR_INVALID_ARG, "job " + std::to_string(j) + ": " + err);
+    q.cls = J.mode == AXX_MODE_SINGLE ? (q.g.geom == AXX_GEOM_SPH ? BC_SSPH : BC_SCYL)
+                                      : (q.g.geom == AXX_GEOM_CYL ? BC_LCYL : BC_LMIX);
     int k = 1;
     while (k < (int)q.sq.channels.size()) k <<= 1;
     kmax = std::max(kmax, k);
+    ckmax[q.cls] = std::max(ckmax[q.cls], k);
   }
   if (kmax > AXX_KMAX) return bfail(ctx, AXX_ERR_UNSUPPORTED, "more than 16 channels in a job");
-  size_t geo_max = 0;
+  size_t geo_max[BC_N] = {};
   std::vector<size_t> job_off(njobs);
   size_t off = 0;
   for (int j = 0; j < njobs; ++j) {
     JobPlan &q = jp[j];
     std::string err = make_kernel_tables(q.g, q.sq, jobs[j].nseq, q.p.steps, q.mode, q.p.flags,
-                                         q.kt, kmax);
+                                         q.kt, ckmax[q.cls]);
     if (err.empty()) err = init_spec(q.g, q.f.basis_p, jobs[j].nbasis, q.mode, &q.p, q.init);
     if (!err.empty()) return bfail(ctx, AXX_ERR_INVALID_ARG, "job " + std::to_string(j) + ": " + err);
-    geo_max = std::max(geo_max, batch_table_bytes(q.g));
+    geo_max[q.cls] = std::max(geo_max[q.cls], batch_table_bytes(q.g));
     job_off[j] = off;
     off = up256(off + arena_layout(q.g, q.kt, jobs[j].nseq).fixed);
   }
   const size_t p_bytes = (sizeof(WalkParams) + 15) & ~(size_t)15;
-  const size_t smem = p_bytes + (size_t)(AXX_BLOCK / 32) * kBatchMaxSeq * 5 * 8 + geo_max;
+  size_t csmem[BC_N] = {};
+  size_t smem = 0;
+  for (int c = 0; c < BC_N; ++c) {
+    csmem[c] = p_bytes + (size_t)(AXX_BLOCK / 32) * kBatchMaxSeq * 5 * 8 + geo_max[c];
+    smem = std::max(smem, csmem[c]);
+  }
   if (smem > AXX_SMEM_MAX) return bfail(ctx, AXX_ERR_UNSUPPORTED, "a job's substrate exceeds shared memory");
   // work items, longest first
   axx_batch_options o = opt;
@@ -561,10 +650,19 @@ static axx_status batch_build(axx_ctx *ctx, const axx_job *jobs, int njobs,
     const JobPlan &q = jp[it.job];
     return (double)it.count * (double)q.p.steps * (1.0 + 0.05 * (double)q.g.geo.size());
   };
-  std::stable_sort(order.begin(), order.end(),
-                   [&](size_t a, size_t b) { return item_cost(items[a]) > item_cost(items[b]); });
+  // by class (each class kernel takes its own range), longest first within it
+  std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) {
+    const int ca = jp[items[a].job].cls, cb = jp[items[b].job].cls;
+    if (ca != cb) return ca < cb;
+    return item_cost(items[a]) > item_cost(items[b]);
+  });
   std::vector<BatchItem> sorted(items.size());
   for (size_t i = 0; i < order.size(); ++i) sorted[i] = items[order[i]];
+  int cfirst[BC_N] = {}, citems[BC_N] = {};
+  for (size_t i = 0; i < sorted.size(); ++i) {
+    const int c = jp[sorted[i].job].cls;
+    if (citems[c]++ == 0) cfirst[c] = (int)i;
+  }
   // partials and outputs
   std::vector<long long> part_off(njobs), out_off(njobs);
   long long npart = 0, nout = 0;
@@ -593,6 +691,12 @@ static axx_status batch_build(axx_ctx *ctx, const axx_job *jobs, int njobs,
   b->kmax = kmax;
   b->tile = o.tile;
   b->smem = smem;
+  for (int c = 0; c < BC_N; ++c) {
+    b->c_kmax[c] = ckmax[c];
+    b->c_smem[c] = csmem[c];
+    b->c_first[c] = cfirst[c];
+    b->c_items[c] = citems[c];
+  }
   b->nout = (int)nout;
   b->use_graph = opt.use_graph != 0;
   e = cudaMalloc(&b->arena, total);
@@ -620,8 +724,7 @@ static axx_status batch_build(axx_ctx *ctx, const axx_job *jobs, int njobs,
                      ctx->abort_dev);
     hj[j].P.counters = b->d_counters + (size_t)AXX_CNT_N * j;
     hj[j].one = (q.g.geom != AXX_GEOM_FREE && q.g.geo.size() == 1 && q.g.cstart.size() == 2) ? 1 : 0;
-    hj[j].sph = (q.mode == AXX_MODE_SINGLE && q.g.geom == AXX_GEOM_SPH) ? 1 : 0;
-    hj[j].cyl = (q.mode == AXX_MODE_LATTICE && q.g.geom == AXX_GEOM_CYL) ? 1 : 0;
+
     hj[j].M = jobs[j].nseq;
     hj[j].part_off = part_off[j];
     hj[j].out_off = out_off[j];
@@ -645,28 +748,43 @@ static axx_status batch_build(axx_ctx *ctx, const axx_job *jobs, int njobs,
     axx_batch_destroy(b);
     return bcuda(ctx, e, "uploading the batch tables");
   }
-  const int occ = batch_occupancy(kmax, smem);
-  if (occ <= 0) {
-    axx_batch_destroy(b);
-    return bfail(ctx, AXX_ERR_CUDA, "batch kernel cannot be resident");
+  // each class kernel: its occupancy, the requested resident blocks, a grid
+  // no larger than its items
+  for (int c = 0; c < BC_N; ++c) {
+    if (citems[c] == 0) continue;
+    const int occ = batch_occupancy(c, ckmax[c], csmem[c]);
+    if (occ <= 0) {
+      axx_batch_destroy(b);
+      return bfail(ctx, AXX_ERR_CUDA, "batch kernel cannot be resident");
+    }
+    int bps = occ;
+    if (o.blocks_per_sm > 0) bps = std::min(occ, o.blocks_per_sm);
+    if (o.blocks_per_sm < 0) bps = std::max(1, occ + o.blocks_per_sm);
+    b->c_bps[c] = bps;
+    b->c_grid[c] = std::max(1, std::min(bps * ctx->nsm, citems[c]));
+    b->bps = std::max(b->bps, bps);
+    b->grid += b->c_grid[c];
+    e = cudaStreamCreateWithFlags(&b->cs[c], cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->join[c], cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+      axx_batch_destroy(b);
+      return bcuda(ctx, e, "batch streams");
+    }
   }
-  int bps = occ;
-  if (o.blocks_per_sm > 0) bps = std::min(occ, o.blocks_per_sm);
-  if (o.blocks_per_sm < 0) bps = std::max(1, occ + o.blocks_per_sm);
-  b->bps = bps;
-  b->grid = std::max(1, std::min(bps * ctx->nsm, b->nitems));
+  e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+  if (e != cudaSuccess) {
+    axx_batch_destroy(b);
+    return bcuda(ctx, e, "batch streams");
+  }
   if (b->use_graph) {
-    // capture: reset the counters, the persistent walk, the reduction
+    // capture: reset the counters, the class kernels (forked onto their
+    // streams and joined back), the reduction
     cudaStream_t s = ctx->stream;
     e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
-      cudaMemsetAsync(b->d_ctr, 0, 16, s);
-      cudaMemsetAsync(b->d_counters, 0, 8 * AXX_CNT_N * njobs, s);
-      batch_go(kmax, b->grid, smem, s, b->d_jobs, b->d_items, b->nitems, b->d_ctr, b->d_part);
-      if (nout > 0)
-        batch_reduce_kernel<<<(int)nout, 256, 0, s>>>(b->d_jobs, b->d_outmap, b->d_jobitems,
-                                                      b->d_part, b->d_out);
-      e = cudaStreamEndCapture(s, &b->graph);
+      e = batch_enqueue(b, s);
+      const cudaError_t e2 = cudaStreamEndCapture(s, &b->graph);
+      if (e == cudaSuccess) e = e2;
     }
     if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec, b->graph, 0);
     if (e != cudaSuccess) {
@@ -690,21 +808,10 @@ extern "C" axx_status axx_batch_launch(axx_batch *b) {
   axx_ctx *ctx = b->ctx;
   *ctx->abort_host = 0;
   cudaError_t e;
-  if (b->use_graph) {
+  if (b->use_graph)
     e = cudaGraphLaunch(b->exec, ctx->stream);
-  } else {
-    cudaStream_t s = ctx->stream;
-    e = cudaMemsetAsync(b->d_ctr, 0, 16, s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(b->d_counters, 0, 8 * AXX_CNT_N * b->njobs, s);
-    if (e == cudaSuccess)
-      e = batch_go(b->kmax, b->grid, b->smem, s, b->d_jobs, b->d_items, b->nitems, b->d_ctr,
-                   b->d_part);
-    if (e == cudaSuccess && b->nout > 0) {
-      batch_reduce_kernel<<<b->nout, 256, 0, s>>>(b->d_jobs, b->d_outmap, b->d_jobitems,
-                                                  b->d_part, b->d_out);
-      e = cudaGetLastError();
-    }
-  }
+  else
+    e = batch_enqueue(b, ctx->stream);
   if (e != cudaSuccess) return bcuda(ctx, e, "axx_batch_launch");
   b->launched = true;
   return AXX_OK;
@@ -759,7 +866,11 @@ extern "C" axx_status axx_batch_info(const axx_batch *b, int *items, int *tile, 
   if (items) *items = b->nitems;
   if (tile) *tile = b->tile;
   if (bps) *bps = b->bps;
-  if (kernel_launches) *kernel_launches = b->nout > 0 ? 2 : 1;
+  if (kernel_launches) {
+    int k = b->nout > 0 ? 1 : 0;
+    for (int c = 0; c < BC_N; ++c) k += b->c_items[c] > 0 ? 1 : 0;
+    *kernel_launches = k;
+  }
   if (walker_steps) *walker_steps = b->walker_steps;
   return AXX_OK;
 }
@@ -769,6 +880,11 @@ extern "C" axx_status axx_batch_destroy(axx_batch *b) {
   if (b->ctx) cudaStreamSynchronize(b->ctx->stream);
   if (b->exec) cudaGraphExecDestroy(b->exec);
   if (b->graph) cudaGraphDestroy(b->graph);
+  for (int c = 0; c < BC_N; ++c) {
+    if (b->cs[c]) cudaStreamDestroy(b->cs[c]);
+    if (b->join[c]) cudaEventDestroy(b->join[c]);
+  }
+  if (b->fork) cudaEventDestroy(b->fork);
   if (b->arena) cudaFree(b->arena);
   delete b;
   return AXX_OK;

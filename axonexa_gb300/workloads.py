@@ -223,7 +223,7 @@ def main(argv=None):
     ap.add_argument("--steps", type=int, default=0, help="cut every walk to this many steps")
     ap.add_argument("--walkers", type=int, default=0)
     ap.add_argument("--reps", type=int, default=3)
-    ap.add_argument("--walker-scale", type=float, default=0.25,
+    ap.add_argument("--walker-scale", type=float, default=1.0,
                     help="batch_256: scale of every job's walker count")
     a = ap.parse_args(argv)
     if a.workload == "mag_lowfield":
@@ -233,7 +233,7 @@ def main(argv=None):
     elif a.workload == "mesh_sphere":
         print(json.dumps(measure_mesh(a.walkers or (1 << 20), a.steps or 6001, a.reps)))
     elif a.workload == "batch_256":
-        print(json.dumps(measure_batch(a.walker_scale, a.steps or 3000, a.reps)))
+        print(json.dumps(measure_batch(a.walker_scale, a.steps or None, a.reps)))
     else:
         print(json.dumps(measure(a.workload, a.steps, a.walkers, a.reps)))
 
@@ -325,7 +325,7 @@ def measure_mesh(walkers: int = 1 << 20, steps: int = 6001, reps: int = 3, devic
             "sphere_walker_steps_per_s": walkers * (steps - 1) / t_s}
 
 
-def measure_batch(walker_scale: float = 0.25, max_steps: int = 3000, reps: int = 3,
+def measure_batch(walker_scale: float = 1.0, max_steps: int = None, reps: int = 3,
                   device=None) -> dict:
     """The uneven 256-substrate batch as one persistent launch replayed from a
     CUDA graph (the autotuned tile): walker-steps/s and signals/s."""

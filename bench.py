@@ -397,12 +397,16 @@ def surrogate_section(A, N, L, dev, queries=1000000, reps=10, plain_subs=2):
     return out
 
 
-def batch_section(A, N, L, dev, reps=3, walker_scale=0.25, max_steps=3000):
-    """The uneven 256-substrate batch (single cylinders, single spheres and
-    hexagonal packs; walkers log-uniform over 1e4-1e6 scaled by
-    `walker_scale`; 8-64 sequences each; walks cut to `max_steps`) as one
-    persistent launch replayed from a CUDA graph with the autotuned tile,
-    against the same jobs as device-resident plans launched one after another."""
+def batch_section(A, N, L, dev, reps=2, walker_scale=1.0, max_steps=None):
+    """The uneven 256-substrate batch as configured: single cylinders (r 1-8
+    um), single spheres (r 2-10 um) and hexagonal packs (f 0.4-0.7, kappa
+    0-0.05 um/ms); walkers log-uniform over 1e4-1e6; 8-64 PGSE, cosine and
+    square-wave OGSE sequences each; full-length walks (TE 45-50 ms at dt
+    5 us).  One launch of the job-class kernels replayed from a CUDA graph with
+    the autotuned tile (best of `reps` after one warm-up), against the same
+    jobs as device-resident plans launched one after another (one pass), and
+    the roofline of the persistent launch (per job the op count of its plan:
+    channels, candidates per move, hits per move)."""
     import ctypes as C
 
     from axonexa_gb300 import workloads as W
@@ -410,14 +414,11 @@ def batch_section(A, N, L, dev, reps=3, walker_scale=0.25, max_steps=3000):
     from axonexa_gb300.batch import Batch
     jobs = W.batch_256(walker_scale=walker_scale, max_steps=max_steps)
 
-    def timed(launch):
-        launch()
-        N.check(L.axx_sync(dev.h), dev.h)
-        return min(time_launches(N, L, dev, launch, reps))
-
     b = Batch(jobs, device=dev)
     info = b.info()
-    ms_batch = timed(b.launch)
+    b.launch()
+    N.check(L.axx_sync(dev.h), dev.h)
+    ms_batch = min(time_launches(N, L, dev, b.launch, reps))
     b.read()
     b.close()
     plans, keep = [], []
@@ -434,26 +435,39 @@ def batch_section(A, N, L, dev, reps=3, walker_scale=0.25, max_steps=3000):
             p = _params(j.num_walkers, j.steps, j.seed, j.timestep, run_flags(True))
             N.check(L.axx_plan_single(dev.h, basis, seqs, len(j.seqs), C.byref(p), C.byref(h)),
                     dev.h)
-        plans.append(h)
+        plans.append((h, len(j.seqs), j.num_walkers * (j.steps - 1),
+                      j.lattice is not None))
         keep += [seqs, basis, p]
 
     def launch_plans():
-        for h in plans:
+        for h, _, _, _ in plans:
             N.check(L.axx_plan_launch(h), dev.h)
 
-    ms_plans = timed(launch_plans)
-    for h in plans:
+    ms_plans = time_launches(N, L, dev, launch_plans, 1)[0]
+    ops = 0.0
+    for h, M, ws_j, lat in plans:
+        ch, cand, hits = plan_facts(N, L, dev, h, M)
+        # single pores walk no periodic wrap
+        ops += ws_j * (ops_per_move(ch, cand, hits) - (0 if lat else 6))
         L.axx_plan_destroy(h)
     ws = info["walker_steps"]
-    return {"workload": "batch_256 (walkers x%.2f, walks cut to %d steps)" % (walker_scale,
-                                                                                max_steps),
+    peak = fma_peak(N, L, dev)
+    return {"workload": "batch_256 (256 substrates, walkers log-uniform 1e4-1e6, "
+                        "full-length walks)" if walker_scale == 1.0 and not max_steps else
+                        "batch_256 (walkers x%.2f, walks cut to %s steps)" % (walker_scale,
+                                                                              max_steps),
             "jobs": len(jobs), "signals": int(sum(len(j.seqs) for j in jobs)),
             "walker_steps": ws, "persistent_graph_ms": ms_batch,
             "persistent_walker_steps_per_s": ws / (ms_batch * 1e-3),
+            "signals_per_s": int(sum(len(j.seqs) for j in jobs)) / (ms_batch * 1e-3),
             "per_job_launches_ms": ms_plans, "per_job_walker_steps_per_s": ws / (ms_plans * 1e-3),
             "speedup": ms_plans / ms_batch, "tile": info["tile"],
             "blocks_per_sm": info["blocks_per_sm"], "work_items": info["items"],
-            "kernel_launches_per_batch": info["kernel_launches"]}
+            "kernel_launches_per_batch": info["kernel_launches"],
+            "roofline": {"bound": "simt", "achieved": ops / (ms_batch * 1e-3) / 1e12,
+                         "peak": peak / 1e12, "unit": "TFLOP/s",
+                         "frac": ops / (ms_batch * 1e-3) / peak,
+                         "ops_per_move": ops / ws}}
 
 
 def measured_peaks():
