@@ -22,8 +22,10 @@ grid.  Results are the reference's unnormalised sums (getMx/getMy).
 """
 from __future__ import annotations
 
+import atexit
 import ctypes as C
 import math
+import weakref
 from typing import List, Sequence
 
 import numpy as np
@@ -289,9 +291,28 @@ class SWOGSEFunc(_GFunc):
         super().__init__(G, gradientDuration, gradientSpacing, numOfPeriods, gHat)
 
 
+# contexts still open at exit are closed (with their objects) before the
+# CUDA runtime unloads
+_LIVE_DEVICES: "weakref.WeakSet[Device]" = weakref.WeakSet()
+
+
+@atexit.register
+def _close_live_devices():
+    for d in list(_LIVE_DEVICES):
+        try:
+            d.close()
+        except Exception:
+            pass
+
+
 # ------------------------------------------------------------------ device ---
 class Device:
-    """One GPU context (axx_create).  Close it or use it as a context manager."""
+    """One GPU context (axx_create).  Close it or use it as a context manager.
+
+    Objects made on the context (batches, networks) register with it:
+    closing the context closes them first, so that no handle outlives the
+    context it was made on, whatever order the interpreter finalises them in
+    (reference cycles, exit)."""
 
     def __init__(self, device: int = 0):
         L = N.lib()
@@ -299,9 +320,21 @@ class Device:
         N.check(L.axx_create(C.byref(h), device))
         self.h = h
         self.device = device
+        self._children = weakref.WeakSet()
+        _LIVE_DEVICES.add(self)
+
+    def adopt(self, obj):
+        """Registers an object holding a handle made on this context; its
+        close() runs before the context is destroyed."""
+        self._children.add(obj)
 
     def close(self):
         if getattr(self, "h", None):
+            for c in list(getattr(self, "_children", ())):
+                try:
+                    c.close()
+                except Exception:
+                    pass
             N.lib().axx_destroy(self.h)
             self.h = None
 

@@ -63,6 +63,7 @@ class Batch:
         N.check(N.lib().axx_batch_create(self.dev.h, self.rec.arr, self.rec.n, C.byref(opt),
                                          C.byref(h)), self.dev.h)
         self.h = h
+        self.dev.adopt(self)
 
     def launch(self):
         N.check(N.lib().axx_batch_launch(self.h), self.dev.h)

@@ -51,6 +51,7 @@ class MLP:
         N.check(N.lib().axx_mlp_create(self.dev.h, in_dim, width, depth, seed, C.byref(h)),
                 self.dev.h)
         self.h = h
+        self.dev.adopt(self)
         self.in_dim, self.width, self.depth = in_dim, width, depth
         n = C.c_int64()
         N.check(N.lib().axx_mlp_num_params(h, C.byref(n)))
