@@ -38,7 +38,8 @@ def main(argv=None):
     ap.add_argument("--walkers", type=int, default=262144)
     ap.add_argument("--timestep", type=float, default=0.001)
     ap.add_argument("--cylinders", type=int, default=400)
-    ap.add_argument("--steps", type=int, default=20000)
+    ap.add_argument("--steps", type=int, default=60000, help="Adam steps of 4,096 pairs")
+    ap.add_argument("--lr", type=float, default=2e-3, help="initial learning rate")
     ap.add_argument("--heldout", type=int, default=2048)
     ap.add_argument("--heldout-walkers", type=int, default=1 << 22)
     ap.add_argument("--realizations", type=int, default=4,
@@ -96,8 +97,9 @@ def main(argv=None):
         d2 = np.abs(Y2 - Yh[:len(Y2)])
         rec.update(_stats(d2, "second_packing_abs_dS_"))
     t0 = time.perf_counter()
-    sur = S.Surrogate.fit(P, Y, steps=a.steps, batch=4096, lr=1e-3, seed=0, device=dev)
+    sur = S.Surrogate.fit(P, Y, steps=a.steps, batch=4096, lr=a.lr, seed=0, device=dev)
     rec["train_steps"] = a.steps
+    rec["train_lr"] = a.lr
     rec["train_s"] = time.perf_counter() - t0
     rec["final_loss"] = float(np.mean(sur.loss[-100:]))
     pred, fb = sur.predict(Ph)
@@ -107,7 +109,7 @@ def main(argv=None):
     if a.save_weights:
         os.makedirs(os.path.dirname(os.path.abspath(a.save_weights)), exist_ok=True)
         meta = {k: rec[k] for k in ("pairs", "walkers", "timestep_ms", "cylinders_per_cell",
-                                    "train_steps", "heldout_walkers") if k in rec}
+                                    "train_steps", "train_lr", "heldout_walkers") if k in rec}
         S.save(sur.mlp, a.save_weights, heldout={"P": Ph, "truth": Yh, "truth_se": SEh},
                meta=meta)
     # inference throughput with device-resident queries (tensor cores)

@@ -59,8 +59,8 @@ PGSE_STEPS, OGSE_STEPS = 25000, 30000
 # DRAM bytes read + written per walker by the headline walk launch (ncu
 # capture at 262,144 walkers, 2,000 steps: block partials and tables only,
 # walker state never leaves registers), scaled by walkers
-WALK_DRAM_BYTES_PER_WALKER = 340000.0 / 262144
-WALK_ISSUE_ACTIVE_NCU = 0.654
+WALK_DRAM_BYTES_PER_WALKER = (155136.0 + 146176.0) / 262144
+WALK_ISSUE_ACTIVE_NCU = 0.648
 
 
 def headline_workload():
@@ -652,7 +652,7 @@ def main():
     }
     if not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        n = int(os.environ.get("AXX_CPU_SAMPLE", "64"))
+        n = int(os.environ.get("AXX_CPU_SAMPLE", "640"))
         v, t, _, ref_sums = cpu_sample(w, n, threads)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                                 "sample": "the first %d walkers x full %d-step walks (%.1f s), "
