@@ -368,25 +368,18 @@ struct Cands {
   }
 };
 
-// Specular boundary handling of one move, general substrates and single
-// instances alike.  A cheap test decides for every candidate whether the
-// segment can meet it at all; the warp votes, and only lanes that may hit
-// run the full nearest-hit loop.
-// L is the move's segment length, Lb its path budget, which replaces L at the
-// first hit (lattice picking: a sqrt(3) L diagonal segment, budget L).
+// The pre-filter of a move: whether any candidate may meet the segment
+// (maybe), and for lists the candidates that may (mmask: bit j for the
+// list's j-th candidate; candidates past the 32nd are always tested).  ONE:
+// the quadratic of the first pass (bh1, c01, c11), which the nearest-hit
+// loop's first pass reuses.
 template <int GEOM, bool PERM, bool ONE>
-__device__ __forceinline__ MoveOut boundary(const WalkParams &P, const Cands<GEOM, ONE> &C,
-                                            float sx, float sy, float sz, float dx, float dy,
-                                            float dz, float L, float v, DevStream &st,
-                                            float Lb) {
+__device__ __forceinline__ bool prefilter(const WalkParams &P, const Cands<GEOM, ONE> &C, float sx,
+                                          float sy, float sz, float dx, float dy, float dz,
+                                          float L, uint32_t &mmask, float &bh1, float &c01,
+                                          float &c11) {
   bool maybe = false;
-  // ONE: the quadratic of the first pass (no instance hit yet, segment L),
-  // reused by the nearest-hit loop's first pass
-  float bh1 = 0.0f, c01 = 0.0f, c11 = 0.0f;
-  // lists: bit j set when the list's j-th candidate may meet the segment
-  // (candidates past the 32nd are always tested); the first pass skips the
-  // others, whose test would reject them the same way
-  uint32_t mmask = 0u;
+  mmask = 0u;
   {
     const float aa_c = fma_f(dx, dx, dy * dy);
     const float aa_s = fma_f(dx, dx, fma_f(dy, dy, dz * dz));
@@ -443,16 +436,20 @@ __device__ __forceinline__ MoveOut boundary(const WalkParams &P, const Cands<GEO
       }
     }
   }
+  return maybe;
+}
+
+// The nearest-hit loop of a move whose pre-filter passed: reflections,
+// transmissions and the end point.
+template <int GEOM, bool PERM, bool ONE>
+__device__ __forceinline__ MoveOut hit_loop(const WalkParams &P, const Cands<GEOM, ONE> &C,
+                                            float sx, float sy, float sz, float dx, float dy,
+                                            float dz, float L, float v, DevStream &st, float Lb,
+                                            uint32_t mmask, float bh1, float c01, float c11) {
   MoveOut o;
   o.hits = 0;
   o.capped = false;
   o.crossed = false;
-  if (!__any_sync(__activemask(), maybe) || !maybe) {
-    o.fx = fma_f(L, dx, sx);
-    o.fy = fma_f(L, dy, sy);
-    o.fz = fma_f(L, dz, sz);
-    return o;
-  }
   float rem = L;
   int last = -1;
   while (true) {
@@ -562,9 +559,48 @@ __device__ __forceinline__ MoveOut boundary(const WalkParams &P, const Cands<GEO
   return o;
 }
 
+// The move's end without a wall met.
+__device__ __forceinline__ MoveOut free_move(float sx, float sy, float sz, float dx, float dy,
+                                             float dz, float L) {
+  MoveOut o;
+  o.hits = 0;
+  o.capped = false;
+  o.crossed = false;
+  o.fx = fma_f(L, dx, sx);
+  o.fy = fma_f(L, dy, sy);
+  o.fz = fma_f(L, dz, sz);
+  return o;
+}
+
+// Specular boundary handling of one move, general substrates and single
+// instances alike.  A cheap test decides for every candidate whether the
+// segment can meet it at all; the warp votes, and only lanes that may hit
+// run the full nearest-hit loop.
+// L is the move's segment length, Lb its path budget, which replaces L at the
+// first hit (lattice picking: a sqrt(3) L diagonal segment, budget L).
+template <int GEOM, bool PERM, bool ONE>
+__device__ __forceinline__ MoveOut boundary(const WalkParams &P, const Cands<GEOM, ONE> &C,
+                                            float sx, float sy, float sz, float dx, float dy,
+                                            float dz, float L, float v, DevStream &st,
+                                            float Lb) {
+  uint32_t mmask;
+  float bh1 = 0.0f, c01 = 0.0f, c11 = 0.0f;
+  const bool maybe =
+      prefilter<GEOM, PERM, ONE>(P, C, sx, sy, sz, dx, dy, dz, L, mmask, bh1, c01, c11);
+  if (!__any_sync(__activemask(), maybe) || !maybe) return free_move(sx, sy, sz, dx, dy, dz, L);
+  return hit_loop<GEOM, PERM, ONE>(P, C, sx, sy, sz, dx, dy, dz, L, v, st, Lb, mmask, bh1, c01,
+                                   c11);
+}
+
 // PAX value of the axis-channel instantiations (channel 3w + a is waveform w
 // along axis a; every axis carries phase: bits x, y, z set, and bit 3)
 #define AXX_PAX_AXES 15
+
+// Lanes of a warp that wait with a move that may meet a wall before the
+// permeable list walk runs its nearest-hit loop for them together.
+#ifndef AXX_DEFER_LANES
+#define AXX_DEFER_LANES 8
+#endif
 
 // A channel's projection p . r, fma(p_z, z, fma(p_y, y, p_x x)), over the
 // axes in PAX: a term of a zero coefficient adds a zero, so leaving it out
@@ -677,91 +713,21 @@ __device__ __forceinline__ float wrap_sel(float x, float a) {
   return (x > a) ? hi : ((x < 0.0f) ? lo : x);
 }
 
-// One move i of walker W with the uniforms (u1, u2); `words` is the stream
-// position after the move's draws (for traces).
-// PICK (single pore, LATTICE_PICKING, kernelPhase.cuh:31-35): the move is
-// +-L along every axis, the signs in bits 0..2 of `signs` (x, y, z): a
-// sqrt(3) L segment along a cube diagonal with path budget L.
-// DEFER: the move's phase terms go to W.part (FP32 sums over a block of
-// moves, folded into the compensated sums by the caller) instead of the
-// compensated sums directly.
-// PAX: the axes some channel projects on (bits x, y, z); the unbounded
-// coordinate of any other axis feeds nothing and is not kept.  Without z
-// (cylinders along z only) z enters neither a boundary test, a region lookup
-// nor a phase term, so the walk keeps no z at all.
-template <int GEOM, int KMAX, int KM, bool TRACE, bool ONE, bool PICK = false, bool DEFER = false,
-          int PAX = 7>
-__device__ __forceinline__ void do_move(const WalkParams &P, const SmemView &S,
-                                        const TraceParams &T, long long wid, int i, float u1,
-                                        float u2, DevStream &st, Walker<KMAX> &W,
-                                        WalkResult &res, const float4 &g0, const float4 &a0,
-                                        uint32_t signs = 0u) {
+// The end of move i of walker W: the position after the boundary handling
+// (fx, fy, fz), its boundary hits and whether it crossed a permeable wall;
+// the wrap, the phase terms, the region and T2 bookkeeping and the trace.
+// s4 holds the slot values the move started with (speed, step, dt/T2).
+template <int GEOM, int KMAX, int KM, bool TRACE, bool ONE, bool DEFER, int PAX>
+__device__ __forceinline__ void move_tail(const WalkParams &P, const SmemView &S,
+                                          const TraceParams &T, long long wid, int i,
+                                          const DevStream &st, Walker<KMAX> &W,
+                                          const Cands<GEOM, ONE> &C, const float4 &s4, float fx,
+                                          float fy, float fz, int hits, bool crossed) {
   constexpr bool single = KM >= AXX_KM_SINGLE;
   constexpr bool perm = KM == AXX_KM_LAT_PERM;
-  constexpr bool reject = KM == AXX_KM_LAT_REJ || KM == AXX_KM_SINGLE_REJ;
-  constexpr bool PX = PAX & 1, PY = PAX & 2, NOZ = !(PAX & 4);
-  // a single pore, or one instance behind impermeable walls: the walker's
-  // slot never changes, and its speed and step stay in registers (the T2
-  // term, .z, is then not read per move)
-  constexpr bool fixed_slot = ONE && (single || KM == AXX_KM_LAT_IMP);
   constexpr bool tracked = KM == AXX_KM_LAT_IMP || KM == AXX_KM_LAT_PERM;
-  // permeable walks hold their slot's values in registers (reloaded when the
-  // slot changes); impermeable list walks read them per move (the registers
-  // would spill there)
-  constexpr bool cached = fixed_slot || perm;
-  const float4 s4 = cached ? make_float4(W.v0, W.L0, W.t2z, 0.0f) : S.slot[W.slot];
-  const float v = s4.x, Lb = s4.y;
-  float dx, dy, dz, L = Lb;
-  if (PICK) {
-    const float k = 0.57735026918962576451f;
-    dx = (signs & 1u) ? k : -k;
-    dy = (signs & 2u) ? k : -k;
-    dz = (signs & 4u) ? k : -k;
-    L = Lb * 1.7320508075688772935f;
-  } else {
-    direction(u1, u2, dx, dy, dz);
-  }
-  Cands<GEOM, ONE> C{S, g0, a0, 0u, 0u};
-  if (GEOM != AXX_GEOM_FREE && !ONE) {
-    const int cell = single ? 0 : cell_of<GEOM>(P, W.x, W.y, W.z);
-    C.b = S.cstart[cell];
-    C.e = S.cstart[cell + 1];
-  }
-  float fx, fy, fz;
-  int hits = 0;
-  bool crossed = false;
-  if (GEOM == AXX_GEOM_FREE) {
-    fx = fma_f(L, dx, W.x);
-    fy = fma_f(L, dy, W.y);
-    fz = fma_f(L, dz, W.z);
-  } else if (reject) {
-    fx = fma_f(L, dx, W.x);
-    fy = fma_f(L, dy, W.y);
-    fz = fma_f(L, dz, W.z);
-    bool back;
-    if (single) {
-      back = !(c0_of(g0, is_sphere<GEOM>(a0), fx, fy, fz) < 0.0f);
-    } else {
-      const int s_new = C.lookup(P.ecs_slot, fx, fy, fz);
-      back = S.region[s_new] != S.region[W.slot];
-    }
-    fx = back ? W.x : fx;
-    fy = back ? W.y : fy;
-    fz = back ? W.z : fz;
-  } else {
-    MoveOut o;
-    if constexpr (ONE && (GEOM == AXX_GEOM_CYL || GEOM == AXX_GEOM_SPH))
-      o = boundary_one<GEOM, perm>(P, C, W.x, W.y, W.z, dx, dy, dz, L, v, st, Lb);
-    else
-      o = boundary<GEOM, perm, ONE>(P, C, W.x, W.y, W.z, dx, dy, dz, L, v, st, Lb);
-    fx = o.fx;
-    fy = o.fy;
-    fz = NOZ ? W.z : o.fz;
-    hits = o.hits;
-    crossed = o.crossed;
-    res.hits += (unsigned)o.hits;
-    res.caps += o.capped ? 1u : 0u;
-  }
+  constexpr bool PX = PAX & 1, PY = PAX & 2, NOZ = !(PAX & 4);
+  const float4 g0 = C.g0, a0 = C.a0;
   float px, py, pz;  // position seen by the phase
   bool wrapped = false;
   if (single) {
@@ -899,7 +865,95 @@ __device__ __forceinline__ void do_move(const WalkParams &P, const SmemView &S,
     T.region[o] = (!single && rs == P.ecs_slot) ? -1 : rs;
     T.hits[o] = hits;
     T.words[o] = (int32_t)st.words_used();
+  }}
+
+// One move i of walker W with the uniforms (u1, u2); `words` is the stream
+// position after the move's draws (for traces).
+// PICK (single pore, LATTICE_PICKING, kernelPhase.cuh:31-35): the move is
+// +-L along every axis, the signs in bits 0..2 of `signs` (x, y, z): a
+// sqrt(3) L segment along a cube diagonal with path budget L.
+// DEFER: the move's phase terms go to W.part (FP32 sums over a block of
+// moves, folded into the compensated sums by the caller) instead of the
+// compensated sums directly.
+// PAX: the axes some channel projects on (bits x, y, z); the unbounded
+// coordinate of any other axis feeds nothing and is not kept.  Without z
+// (cylinders along z only) z enters neither a boundary test, a region lookup
+// nor a phase term, so the walk keeps no z at all.
+template <int GEOM, int KMAX, int KM, bool TRACE, bool ONE, bool PICK = false, bool DEFER = false,
+          int PAX = 7>
+__device__ __forceinline__ void do_move(const WalkParams &P, const SmemView &S,
+                                        const TraceParams &T, long long wid, int i, float u1,
+                                        float u2, DevStream &st, Walker<KMAX> &W,
+                                        WalkResult &res, const float4 &g0, const float4 &a0,
+                                        uint32_t signs = 0u) {
+  constexpr bool single = KM >= AXX_KM_SINGLE;
+  constexpr bool perm = KM == AXX_KM_LAT_PERM;
+  constexpr bool reject = KM == AXX_KM_LAT_REJ || KM == AXX_KM_SINGLE_REJ;
+  constexpr bool PX = PAX & 1, PY = PAX & 2, NOZ = !(PAX & 4);
+  // a single pore, or one instance behind impermeable walls: the walker's
+  // slot never changes, and its speed and step stay in registers (the T2
+  // term, .z, is then not read per move)
+  constexpr bool fixed_slot = ONE && (single || KM == AXX_KM_LAT_IMP);
+  constexpr bool tracked = KM == AXX_KM_LAT_IMP || KM == AXX_KM_LAT_PERM;
+  // permeable walks hold their slot's values in registers (reloaded when the
+  // slot changes); impermeable list walks read them per move (the registers
+  // would spill there)
+  constexpr bool cached = fixed_slot || perm;
+  const float4 s4 = cached ? make_float4(W.v0, W.L0, W.t2z, 0.0f) : S.slot[W.slot];
+  const float v = s4.x, Lb = s4.y;
+  float dx, dy, dz, L = Lb;
+  if (PICK) {
+    const float k = 0.57735026918962576451f;
+    dx = (signs & 1u) ? k : -k;
+    dy = (signs & 2u) ? k : -k;
+    dz = (signs & 4u) ? k : -k;
+    L = Lb * 1.7320508075688772935f;
+  } else {
+    direction(u1, u2, dx, dy, dz);
   }
+  Cands<GEOM, ONE> C{S, g0, a0, 0u, 0u};
+  if (GEOM != AXX_GEOM_FREE && !ONE) {
+    const int cell = single ? 0 : cell_of<GEOM>(P, W.x, W.y, W.z);
+    C.b = S.cstart[cell];
+    C.e = S.cstart[cell + 1];
+  }
+  float fx, fy, fz;
+  int hits = 0;
+  bool crossed = false;
+  if (GEOM == AXX_GEOM_FREE) {
+    fx = fma_f(L, dx, W.x);
+    fy = fma_f(L, dy, W.y);
+    fz = fma_f(L, dz, W.z);
+  } else if (reject) {
+    fx = fma_f(L, dx, W.x);
+    fy = fma_f(L, dy, W.y);
+    fz = fma_f(L, dz, W.z);
+    bool back;
+    if (single) {
+      back = !(c0_of(g0, is_sphere<GEOM>(a0), fx, fy, fz) < 0.0f);
+    } else {
+      const int s_new = C.lookup(P.ecs_slot, fx, fy, fz);
+      back = S.region[s_new] != S.region[W.slot];
+    }
+    fx = back ? W.x : fx;
+    fy = back ? W.y : fy;
+    fz = back ? W.z : fz;
+  } else {
+    MoveOut o;
+    if constexpr (ONE && (GEOM == AXX_GEOM_CYL || GEOM == AXX_GEOM_SPH))
+      o = boundary_one<GEOM, perm>(P, C, W.x, W.y, W.z, dx, dy, dz, L, v, st, Lb);
+    else
+      o = boundary<GEOM, perm, ONE>(P, C, W.x, W.y, W.z, dx, dy, dz, L, v, st, Lb);
+    fx = o.fx;
+    fy = o.fy;
+    fz = NOZ ? W.z : o.fz;
+    hits = o.hits;
+    crossed = o.crossed;
+    res.hits += (unsigned)o.hits;
+    res.caps += o.capped ? 1u : 0u;
+  }
+  move_tail<GEOM, KMAX, KM, TRACE, ONE, DEFER, PAX>(P, S, T, wid, i, st, W, C, s4, fx, fy, fz,
+                                                    hits, crossed);
 }
 
 // One walker.  On return W holds the channel sums (value, Kahan
@@ -1023,18 +1077,81 @@ __device__ __forceinline__ WalkResult walk_one(const WalkParams &P, const SmemVi
       for (int c = 0; c < KMAX; ++c) kahan_add(W.acc[c], W.cmp[c], W.part[c]);
     }
   }
-  for (; i < P.steps; ++i) {
-    if ((i & 1023) == 0 && P.abort_flag != nullptr && *P.abort_flag) {
-      res.aborted = true;
-      break;
+  if constexpr (perm && !ONE && GEOM != AXX_GEOM_FREE) {
+    // Permeable list walks: a lane whose move may meet a wall keeps the
+    // move's direction and waits; the nearest-hit loop runs once
+    // AXX_DEFER_LANES lanes of the warp wait (or no other lane can move), so
+    // one pass of the divergent loop serves several lanes.  Every lane keeps
+    // its own move index: its draws, its moves and their order are those of
+    // the walk without waiting, and so are its sums.
+    constexpr bool NOZ = !(PAX & 4);
+    const unsigned lanes = __activemask();
+    int il = i;
+    bool waiting = false;
+    float wdx = 0.0f, wdy = 0.0f, wdz = 0.0f;
+    uint32_t wmm = 0u;
+    for (uint32_t it = 1;; ++it) {
+      const bool active = il < P.steps;
+      if (__ballot_sync(lanes, active) == 0u) break;
+      // (the warp leaves together: every lane takes part in the votes)
+      if ((it & 1023u) == 0u && P.abort_flag != nullptr &&
+          __any_sync(lanes, *P.abort_flag != 0)) {
+        res.aborted = true;
+        break;
+      }
+      const float4 s4 = make_float4(W.v0, W.L0, W.t2z, 0.0f);
+      const float v = s4.x, L = s4.y;
+      Cands<GEOM, false> C{S, g0, a0, 0u, 0u};
+      const int cell = cell_of<GEOM>(P, W.x, W.y, W.z);
+      C.b = S.cstart[cell];
+      C.e = S.cstart[cell + 1];
+      float dx = wdx, dy = wdy, dz = wdz;
+      if (active && !waiting) {
+        float u1, u2;
+        st.next2_eager(P, u1, u2);
+        direction(u1, u2, dx, dy, dz);
+        uint32_t mm;
+        float bh1, c01, c11;
+        if (prefilter<GEOM, true, false>(P, C, W.x, W.y, W.z, dx, dy, dz, L, mm, bh1, c01, c11)) {
+          waiting = true;
+          wdx = dx;
+          wdy = dy;
+          wdz = dz;
+          wmm = mm;
+        }
+      }
+      const unsigned wm = __ballot_sync(lanes, waiting);
+      const unsigned fm = __ballot_sync(lanes, active && !waiting);
+      const bool resolve = waiting && (__popc(wm) >= AXX_DEFER_LANES || fm == 0u);
+      if (resolve || (active && !waiting)) {
+        const MoveOut o =
+            resolve ? hit_loop<GEOM, true, false>(P, C, W.x, W.y, W.z, dx, dy, dz, L, v, st, L,
+                                                  wmm, 0.0f, 0.0f, 0.0f)
+                    : free_move(W.x, W.y, W.z, dx, dy, dz, L);
+        waiting = false;
+        res.hits += (unsigned)o.hits;
+        res.caps += o.capped ? 1u : 0u;
+        move_tail<GEOM, KMAX, KM, TRACE, false, false, PAX>(P, S, T, wid, il, st, W, C, s4, o.fx,
+                                                           o.fy, NOZ ? W.z : o.fz, o.hits,
+                                                           o.crossed);
+        ++il;
+      }
     }
-    float u1, u2;
-    if (perm)
-      st.next2_eager(P, u1, u2);
-    else
-      st.next2(P, u1, u2);
-    do_move<GEOM, KMAX, KM, TRACE, ONE, false, false, PAX>(P, S, T, wid, i, u1, u2, st, W, res,
-                                                          g0, a0);
+    i = il;
+  } else {
+    for (; i < P.steps; ++i) {
+      if ((i & 1023) == 0 && P.abort_flag != nullptr && *P.abort_flag) {
+        res.aborted = true;
+        break;
+      }
+      float u1, u2;
+      if (perm)
+        st.next2_eager(P, u1, u2);
+      else
+        st.next2(P, u1, u2);
+      do_move<GEOM, KMAX, KM, TRACE, ONE, false, false, PAX>(P, S, T, wid, i, u1, u2, st, W, res,
+                                                            g0, a0);
+    }
   }
   if (!single && KM == AXX_KM_LAT_IMP && ONE) {  // the T2 sum of the walker's one region
     const double t = (double)(i - 1) * (double)S.slot[W.slot].z;
