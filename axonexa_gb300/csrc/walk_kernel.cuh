@@ -596,12 +596,6 @@ __device__ __forceinline__ MoveOut boundary(const WalkParams &P, const Cands<GEO
 // along axis a; every axis carries phase: bits x, y, z set, and bit 3)
 #define AXX_PAX_AXES 15
 
-// Lanes of a warp that wait with a move that may meet a wall before the
-// permeable list walk runs its nearest-hit loop for them together.
-#ifndef AXX_DEFER_LANES
-#define AXX_DEFER_LANES 8
-#endif
-
 // A channel's projection p . r, fma(p_z, z, fma(p_y, y, p_x x)), over the
 // axes in PAX: a term of a zero coefficient adds a zero, so leaving it out
 // gives the same value (up to the sign of a zero sum).
@@ -1077,82 +1071,20 @@ __device__ __forceinline__ WalkResult walk_one(const WalkParams &P, const SmemVi
       for (int c = 0; c < KMAX; ++c) kahan_add(W.acc[c], W.cmp[c], W.part[c]);
     }
   }
-  if constexpr (perm && !ONE && GEOM != AXX_GEOM_FREE) {
-    // Permeable list walks: a lane whose move may meet a wall keeps the
-    // move's direction and waits; the nearest-hit loop runs once
-    // AXX_DEFER_LANES lanes of the warp wait (or no other lane can move), so
-    // one pass of the divergent loop serves several lanes.  Every lane keeps
-    // its own move index: its draws, its moves and their order are those of
-    // the walk without waiting, and so are its sums.
-    constexpr bool NOZ = !(PAX & 4);
-    const unsigned lanes = __activemask();
-    int il = i;
-    bool waiting = false;
-    float wdx = 0.0f, wdy = 0.0f, wdz = 0.0f;
-    uint32_t wmm = 0u;
-    for (uint32_t it = 1;; ++it) {
-      const bool active = il < P.steps;
-      if (__ballot_sync(lanes, active) == 0u) break;
-      // (the warp leaves together: every lane takes part in the votes)
-      if ((it & 1023u) == 0u && P.abort_flag != nullptr &&
-          __any_sync(lanes, *P.abort_flag != 0)) {
-        res.aborted = true;
-        break;
-      }
-      const float4 s4 = make_float4(W.v0, W.L0, W.t2z, 0.0f);
-      const float v = s4.x, L = s4.y;
-      Cands<GEOM, false> C{S, g0, a0, 0u, 0u};
-      const int cell = cell_of<GEOM>(P, W.x, W.y, W.z);
-      C.b = S.cstart[cell];
-      C.e = S.cstart[cell + 1];
-      float dx = wdx, dy = wdy, dz = wdz;
-      if (active && !waiting) {
-        float u1, u2;
-        st.next2_eager(P, u1, u2);
-        direction(u1, u2, dx, dy, dz);
-        uint32_t mm;
-        float bh1, c01, c11;
-        if (prefilter<GEOM, true, false>(P, C, W.x, W.y, W.z, dx, dy, dz, L, mm, bh1, c01, c11)) {
-          waiting = true;
-          wdx = dx;
-          wdy = dy;
-          wdz = dz;
-          wmm = mm;
-        }
-      }
-      const unsigned wm = __ballot_sync(lanes, waiting);
-      const unsigned fm = __ballot_sync(lanes, active && !waiting);
-      const bool resolve = waiting && (__popc(wm) >= AXX_DEFER_LANES || fm == 0u);
-      if (resolve || (active && !waiting)) {
-        const MoveOut o =
-            resolve ? hit_loop<GEOM, true, false>(P, C, W.x, W.y, W.z, dx, dy, dz, L, v, st, L,
-                                                  wmm, 0.0f, 0.0f, 0.0f)
-                    : free_move(W.x, W.y, W.z, dx, dy, dz, L);
-        waiting = false;
-        res.hits += (unsigned)o.hits;
-        res.caps += o.capped ? 1u : 0u;
-        move_tail<GEOM, KMAX, KM, TRACE, false, false, PAX>(P, S, T, wid, il, st, W, C, s4, o.fx,
-                                                           o.fy, NOZ ? W.z : o.fz, o.hits,
-                                                           o.crossed);
-        ++il;
-      }
+  for (; i < P.steps; ++i) {
+    if ((i & 1023) == 0 && P.abort_flag != nullptr && *P.abort_flag) {
+      res.aborted = true;
+      break;
     }
-    i = il;
-  } else {
-    for (; i < P.steps; ++i) {
-      if ((i & 1023) == 0 && P.abort_flag != nullptr && *P.abort_flag) {
-        res.aborted = true;
-        break;
-      }
-      float u1, u2;
-      if (perm)
-        st.next2_eager(P, u1, u2);
-      else
-        st.next2(P, u1, u2);
-      do_move<GEOM, KMAX, KM, TRACE, ONE, false, false, PAX>(P, S, T, wid, i, u1, u2, st, W, res,
-                                                            g0, a0);
-    }
+    float u1, u2;
+    if (perm)
+      st.next2_eager(P, u1, u2);
+    else
+      st.next2(P, u1, u2);
+    do_move<GEOM, KMAX, KM, TRACE, ONE, false, false, PAX>(P, S, T, wid, i, u1, u2, st, W, res,
+                                                          g0, a0);
   }
+
   if (!single && KM == AXX_KM_LAT_IMP && ONE) {  // the T2 sum of the walker's one region
     const double t = (double)(i - 1) * (double)S.slot[W.slot].z;
     W.t2s = (float)t;
