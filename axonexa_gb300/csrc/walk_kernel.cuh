@@ -412,6 +412,7 @@ __device__ __forceinline__ bool prefilter(const WalkParams &P, const Cands<GEOM,
       const float mx = fma_f(hl, dx, sx), my = fma_f(hl, dy, sy);
       uint32_t keep = 0u;
       bool far = false;  // a candidate past the 32nd kept (always tested)
+#pragma unroll 2
       for (uint32_t j = C.b; j < C.e; ++j) {
         const uint32_t bit = j - C.b;
         const bool k = annulus_keeps(C.S.geo[C.S.clist[j]], mx, my, P.ann_h2x2);
@@ -477,13 +478,11 @@ __device__ __forceinline__ MoveOut hit_loop(const WalkParams &P, const Cands<GEO
       // lists; the instance just hit is tested from its surface)
       const float hl = 0.5f * rem;
       const float mx = fma_f(hl, dx, sx), my = fma_f(hl, dy, sy);
-      for (uint32_t j = C.b; j < C.e; ++j) {
-        const uint32_t bit = j - C.b;
-        if (last < 0 && bit < 32u && !((mmask >> bit) & 1u)) continue;
+      auto test = [&](uint32_t j) {
         const int k = C.S.clist[j];
         if (GEOM == AXX_GEOM_CYL && PERM && last >= 0 && k != last &&
             !annulus_keeps(C.S.geo[k], mx, my, P.ann_h2x2))
-          continue;
+          return;
         const float4 aux = C.S.aux[k];
         const bool sph = is_sphere<GEOM>(aux);
         const float s =
@@ -495,6 +494,14 @@ __device__ __forceinline__ MoveOut hit_loop(const WalkParams &P, const Cands<GEO
           best = s;
           bk = k;
         }
+      };
+      if (last < 0) {
+        // first pass: the candidates the pre-filter kept, in list order (the
+        // others would be rejected the same way), then any past the 32nd
+        for (uint32_t m = mmask; m != 0u; m &= m - 1u) test(C.b + (uint32_t)(__ffs(m) - 1));
+        for (uint32_t j = C.b + 32u; j < C.e; ++j) test(j);
+      } else {
+        for (uint32_t j = C.b; j < C.e; ++j) test(j);
       }
       if (bk >= 0) {
         bg = C.S.geo[bk];
