@@ -83,6 +83,11 @@ __device__ __forceinline__ unsigned long long global_ns() {
   return t;
 }
 
+// Suspend-time hint of the mbarrier waits (ns): a waiting thread is woken at
+// least this often, so it resumes soon after the phase completes (measured:
+// the default hint left the inference kernel's MMA issue 8 % slower).
+constexpr uint32_t kMbarSuspendNs = 32;
+
 // Waits for the phase of parity `parity` to complete.  Gives up (false) when
 // *fail is set by another role or after limit_ns of wall-clock time.
 __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity, volatile int *fail,
@@ -93,11 +98,11 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity, volati
     asm volatile(
         "{\n"
         ".reg .pred p;\n"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
         "selp.u32 %0, 1, 0, p;\n"
         "}\n"
         : "=r"(done)
-        : "r"(mbar), "r"(parity)
+        : "r"(mbar), "r"(parity), "r"(kMbarSuspendNs)
         : "memory");
     if (done) return true;
     if ((it & 63u) == 0u) {
