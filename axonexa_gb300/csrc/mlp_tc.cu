@@ -269,14 +269,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) mlp_tc_kernel(const __grid_cons
           const uint32_t tacc = tmem + lane_base + (uint32_t)(t * TC_N);
           float ys = 0.f;
 #pragma unroll 1
-          for (int cb = c0; cb < c0 + TC_GCOLS; cb += 64) {
-            uint32_t v[64];
+          for (int cb = c0; cb < c0 + TC_GCOLS; cb += 32) {
+            // 32 columns per TMEM read: 32 registers of accumulator in flight
+            uint32_t v[32];
             AXX_TMEM_LD32(tacc + (uint32_t)cb, v);
-            AXX_TMEM_LD32(tacc + (uint32_t)(cb + 32), (v + 32));
             asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
             if (last) {
 #pragma unroll
-              for (int q = 0; q < 16; ++q) {
+              for (int q = 0; q < 8; ++q) {
                 const float4 b4 = *reinterpret_cast<const float4 *>(bl + cb + 4 * q);
                 const float4 w4 = *reinterpret_cast<const float4 *>(sbias + 8 * TC_N + cb + 4 * q);
                 const float bb[4] = {b4.x, b4.y, b4.z, b4.w}, ww[4] = {w4.x, w4.y, w4.z, w4.w};
@@ -286,7 +286,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) mlp_tc_kernel(const __grid_cons
               }
             } else {
 #pragma unroll
-              for (int q = 0; q < 8; ++q) {
+              for (int q = 0; q < 4; ++q) {
                 const float4 b0 = *reinterpret_cast<const float4 *>(bl + cb + 8 * q);
                 const float4 b1 = *reinterpret_cast<const float4 *>(bl + cb + 8 * q + 4);
                 const float bb[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
