@@ -30,11 +30,16 @@
 #define AXX_BLOCK 128        // threads per block of the walk kernels
 #define AXX_INIT_TRIES 100000
 
+#ifndef AXX_MIN_BLOCKS
 #define AXX_MIN_BLOCKS 6      // resident blocks per SM the register budget targets
+#endif
 // 16 channels (32 accumulator registers) spill under the 80 registers of 6
 // resident blocks; 5 blocks (102 registers) measured 2 % faster than 6 and
 // 10 % faster than 4 on the 400-cylinder pack.
-#define AXX_MIN_BLOCKS_FOR(kmax) ((kmax) >= 12 ? 5 : AXX_MIN_BLOCKS)
+#ifndef AXX_MIN_BLOCKS_WIDE
+#define AXX_MIN_BLOCKS_WIDE 5
+#endif
+#define AXX_MIN_BLOCKS_FOR(kmax) ((kmax) >= 12 ? AXX_MIN_BLOCKS_WIDE : AXX_MIN_BLOCKS)
 #define AXX_SMEM_MAX (200 * 1024)
 
 enum { AXX_MODE_LATTICE = 0, AXX_MODE_SINGLE = 1 };

@@ -13,6 +13,7 @@ tests/test_oracle_pin.py):
      walk, and within 1e-5*N of the FP32 formulation (same trajectories).
 """
 import math
+import os
 
 import numpy as np
 import pytest
@@ -408,6 +409,62 @@ def test_full_size_cylinder_properties(dev):
     b = A.run_lattice(L, B, S, half, steps, 0.002, 1234, relaxation=True, device=dev,
                       walker_offset=half)
     np.testing.assert_allclose(a.mx + b.mx, r1.mx, rtol=0, atol=1e-8 * n)
+    # the OGSE acquisition as measured: its own 30,000-step walk (TE 60 ms);
+    # the cosine signal rises with frequency (shorter diffusion times see less
+    # restriction-free dephasing at fixed G) and stays within (0, G=0 decay]
+    ogse = [A.CosGFunc(100e-6, 20.0, 20.0, k) for k in (1, 2, 4)]
+    r3 = A.run_lattice(L, B, ogse, n, 30000, 0.002, 1234, relaxation=True, device=dev)
+    assert r3.cap_hits == 0 and r3.walker_steps == n * 29999
+    TE3 = 29999 * 0.002
+    s0 = f * math.exp(-TE3 / 80.0) + (1 - f) * math.exp(-TE3 / 60.0)
+    assert np.all(r3.signal > 0) and np.all(r3.signal <= s0 + 4 * r3.stderr + 2e-4)
+    assert np.all(np.diff(r3.signal) > -3 * r3.stderr[1:])
+
+
+def _oracle_records(w, O):
+    lat = w["lattice"]
+    L = O.Lattice(lat.a, lat.b, lat.c, lat.T2, lat.T1, lat.D)
+    B = [O.Basis(0, c.region, c.centerX, c.centerY, 0.0, c.radius, c.D, c.T2, c.T1,
+                 c.permeability, c.eps) for c in w["basis"]]
+    Q = [O.Sequence(q.kind, q.num_periods, q.G, q.duration, q.spacing, q.ghat[0], q.ghat[1],
+                    q.ghat[2]) for q in w["seqs"]]
+    return L, B, Q
+
+
+def test_full_size_gamma_pack_properties(dev, orc):
+    """The headline job as measured: 400 gamma-radius cylinders, permeable,
+    4,194,304 walkers x 49,999 moves at dt 1 us, 64 sequences.  Sharding by
+    walker ranges reproduces the whole walk, no move hits the reflection cap,
+    the hit rate is the profiled one, and the first 64 walkers' signals agree
+    with the FP64 reference-order oracle on the same streams (statistically:
+    FP32 and FP64 paths split after enough reflections in a dense pack)."""
+    import axonexa_gb300 as A
+    from axonexa_gb300 import workloads as W
+    w = W.gamma_pack()
+    n, steps = w["num_walkers"], w["steps"]
+    kw = dict(relaxation=True, permeable=True, device=dev)
+    whole = A.run_lattice(w["lattice"], w["basis"], w["seqs"], n, steps, w["timestep"],
+                          w["seed"], **kw)
+    assert whole.cap_hits == 0 and whole.walker_steps == n * (steps - 1)
+    assert 0.015 < whole.hits / whole.walker_steps < 0.03
+    assert np.all(np.isfinite(whole.signal)) and np.all((whole.signal >= 0) & (whole.signal < 1))
+    half = n // 2
+    a = A.run_lattice(w["lattice"], w["basis"], w["seqs"], half, steps, w["timestep"], w["seed"],
+                      **kw)
+    b = A.run_lattice(w["lattice"], w["basis"], w["seqs"], half, steps, w["timestep"], w["seed"],
+                      walker_offset=half, **kw)
+    np.testing.assert_allclose(a.mx + b.mx, whole.mx, rtol=0, atol=1e-8 * n)
+    np.testing.assert_allclose(a.my + b.my, whole.my, rtol=0, atol=1e-8 * n)
+    # FP64 oracle on the first 64 walkers, the same streams
+    m = 64
+    first = A.run_lattice(w["lattice"], w["basis"], w["seqs"], m, steps, w["timestep"], w["seed"],
+                          **kw)
+    L, B, Q = _oracle_records(w, orc)
+    p = orc.Params(m, steps, 0, 0, 1 | 2, w["seed"], w["timestep"], 0.0, 0)
+    sums, _, _ = orc.walk(L, B, Q, p, orc.REF64, nthreads=os.cpu_count() or 1)
+    s_ref = np.hypot(sums[:, 0], sums[:, 1]) / m
+    z = np.abs(first.signal - s_ref) / np.maximum(first.stderr, 1e-12)
+    assert z.max() < 5.0 and z.mean() < 1.5, (z.max(), z.mean())
 
 
 def test_edge_cases(dev, orc):
