@@ -103,9 +103,9 @@ class Field(C.Structure):
 class MagParams(C.Structure):
     """axx_mag_params"""
     _fields_ = [("num_walkers", C.c_int64), ("steps", C.c_int32), ("integrator", C.c_int32),
-                ("flags", C.c_uint32), ("pad", C.c_uint32), ("seed", C.c_uint64),
+                ("flags", C.c_uint32), ("dorp_levels", C.c_uint32), ("seed", C.c_uint64),
                 ("timestep", C.c_double), ("gamma", C.c_double), ("m0", C.c_double * 3),
-                ("walker_offset", C.c_int64)]
+                ("walker_offset", C.c_int64), ("dorp_tol", C.c_double)]
 
 
 _SIGS = {

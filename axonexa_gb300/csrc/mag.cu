@@ -56,6 +56,11 @@ struct MagArgs {
   const float4 *ms_tab;  // sub-steps (s, bx, by, 0)
   double *partials;      // [grid][nf*3]
   float *m_trace;        // [ntrace][nf][3]
+  // Dormand-Prince: per field, step, level k (sub-steps dt/2^k) and sub-step
+  // m, the six stage times' coefficients (s, bx, by, 0)
+  const float4 *dp_tab;  // [nf][steps][6 (2^(K+1) - 1)]
+  int dp_K;              // halvings allowed
+  float dp_tol;
 };
 
 __device__ __forceinline__ void field_at(const MagArgs &Q, int j, const float4 &tc, float x,
@@ -125,10 +130,112 @@ __device__ __forceinline__ void rk4_start(const MagArgs &Q, int j, float x, floa
   mz += s6 * fma_f(2.0f, k2z + k3z, k1z + k4z);
 }
 
+// gamma (M x B(r, t)) with the field coefficients tc of the stage time
+// (blochdiff.cuh:7-10: bloch() = (M % B) GAMMA).
+__device__ __forceinline__ void bloch_deriv(const MagArgs &Q, int j, const float4 &tc, float x,
+                                            float y, float z, const float m[3], float f[3]) {
+  float bx, by, dbz;
+  field_at(Q, j, tc, x, y, z, bx, by, dbz);
+  const float bz = Q.B0[j] + dbz;
+  f[0] = Q.gamma * fma_f(m[1], bz, -(m[2] * by));
+  f[1] = Q.gamma * fma_f(m[2], bx, -(m[0] * bz));
+  f[2] = Q.gamma * fma_f(m[0], by, -(m[1] * bx));
+}
+
+// Adaptive Dormand-Prince 5(4) over [i dt, (i+1) dt] at the walker's
+// position, the FP32 twin of the oracle's mag_dorp: tableau of Dormand &
+// Prince (1980), the fifth-order solution propagated, the embedded
+// fourth-order error scaled per component by tol (1 + max(|M5|, |M|)) and
+// taken as an RMS; sub-steps dt/2^k on a dyadic grid, halved while the error
+// exceeds 1 (accepted at level K whatever it is), doubled after an error
+// below 1/32 when the grid allows.  Every loop is bounded.
+__device__ __noinline__ float3 dorp_update(const MagArgs &Q, int steps, int j, int i, float x,
+                                           float y, float z, float mx, float my, float mz) {
+  constexpr float a10 = (float)(1.0 / 5.0);
+  constexpr float a20 = (float)(3.0 / 40.0), a21 = (float)(9.0 / 40.0);
+  constexpr float a30 = (float)(44.0 / 45.0), a31 = (float)(-56.0 / 15.0),
+                  a32 = (float)(32.0 / 9.0);
+  constexpr float a40 = (float)(19372.0 / 6561.0), a41 = (float)(-25360.0 / 2187.0),
+                  a42 = (float)(64448.0 / 6561.0), a43 = (float)(-212.0 / 729.0);
+  constexpr float a50 = (float)(9017.0 / 3168.0), a51 = (float)(-355.0 / 33.0),
+                  a52 = (float)(46732.0 / 5247.0), a53 = (float)(49.0 / 176.0),
+                  a54 = (float)(-5103.0 / 18656.0);
+  constexpr float b0 = (float)(35.0 / 384.0), b2 = (float)(500.0 / 1113.0),
+                  b3 = (float)(125.0 / 192.0), b4 = (float)(-2187.0 / 6784.0),
+                  b5 = (float)(11.0 / 84.0);
+  constexpr float e0 = (float)(71.0 / 57600.0), e2 = (float)(-71.0 / 16695.0),
+                  e3 = (float)(71.0 / 1920.0), e4 = (float)(-17253.0 / 339200.0),
+                  e5 = (float)(22.0 / 525.0), e6 = (float)(-1.0 / 40.0);
+  const int K = Q.dp_K, full = 1 << K;
+  const float4 *T = Q.dp_tab + ((size_t)j * steps + i) * (size_t)(6 * ((2 << K) - 1));
+  float M[3] = {mx, my, mz};
+  int pos = 0, k = 0;
+  for (int guard = 0; pos < full && guard < 64 * full; ++guard) {
+    const float h = Q.h * __int_as_float((127 - k) << 23);  // dt / 2^k, exact
+    const float4 *tc = T + 6 * ((1 << k) - 1 + (pos >> (K - k)));
+    float f0[3], f1[3], f2[3], f3[3], f4[3], f5[3], f6[3], yv[3], y5[3];
+    bloch_deriv(Q, j, tc[0], x, y, z, M, f0);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) yv[c] = fma_f(h, a10 * f0[c], M[c]);
+    bloch_deriv(Q, j, tc[1], x, y, z, yv, f1);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) yv[c] = fma_f(h, fma_f(a21, f1[c], a20 * f0[c]), M[c]);
+    bloch_deriv(Q, j, tc[2], x, y, z, yv, f2);
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+      yv[c] = fma_f(h, fma_f(a32, f2[c], fma_f(a31, f1[c], a30 * f0[c])), M[c]);
+    bloch_deriv(Q, j, tc[3], x, y, z, yv, f3);
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+      yv[c] = fma_f(h, fma_f(a43, f3[c], fma_f(a42, f2[c], fma_f(a41, f1[c], a40 * f0[c]))), M[c]);
+    bloch_deriv(Q, j, tc[4], x, y, z, yv, f4);
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+      yv[c] = fma_f(h, fma_f(a54, f4[c], fma_f(a53, f3[c], fma_f(a52, f2[c],
+                                                                   fma_f(a51, f1[c], a50 * f0[c])))),
+                    M[c]);
+    bloch_deriv(Q, j, tc[5], x, y, z, yv, f5);
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+      y5[c] = fma_f(h, fma_f(b5, f5[c], fma_f(b4, f4[c], fma_f(b3, f3[c], fma_f(b2, f2[c], b0 * f0[c])))),
+                    M[c]);
+    bloch_deriv(Q, j, tc[5], x, y, z, y5, f6);
+    float en = 0.0f;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const float err =
+          h * fma_f(e6, f6[c], fma_f(e5, f5[c], fma_f(e4, f4[c], fma_f(e3, f3[c],
+                                                                    fma_f(e2, f2[c], e0 * f0[c])))));
+      const float r = __fdividef(err, Q.dp_tol * (1.0f + fmaxf(fabsf(y5[c]), fabsf(M[c]))));
+      en = fma_f(r, r, en);
+    }
+    en = sqrt_f(en * (1.0f / 3.0f));
+    if (en <= 1.0f || k == K) {
+      M[0] = y5[0];
+      M[1] = y5[1];
+      M[2] = y5[2];
+      pos += 1 << (K - k);
+      if (en < (1.0f / 32.0f) && k > 0 && (pos & ((1 << (K - k + 1)) - 1)) == 0) --k;
+    } else {
+      ++k;
+    }
+  }
+  return make_float3(M[0], M[1], M[2]);
+}
+
 // The update of field j at time point i (kernelMag.cuh:32-72 for i = 0,
 // :96-134 for i >= 1).
 __device__ __forceinline__ void mag_update(const MagArgs &Q, int steps, int j, int i, float x,
                                            float y, float z, float &mx, float &my, float &mz) {
+  if (Q.integ == AXX_MAG_DORP) {
+    // (by value: a reference into the walker's M array would move it to
+    // local memory in every instantiation)
+    const float3 r = dorp_update(Q, steps, j, i, x, y, z, mx, my, mz);
+    mx = r.x;
+    my = r.y;
+    mz = r.z;
+    return;
+  }
   if (Q.integ == AXX_MAG_ROTATE_MULTISTEP) {
     const int2 ix = Q.ms_idx[j * steps + i];
     const float4 rt = Q.ms_rot[j * steps + i];
@@ -454,8 +561,13 @@ axx_status mag_run(axx_ctx *ctx, const axx_basis *pore, const axx_field *fields,
   if (mp->num_walkers < 1 || mp->steps < 1 || !(mp->timestep > 0.0) ||
       !std::isfinite(mp->timestep) || mp->walker_offset < 0)
     return mfail2(ctx, AXX_ERR_INVALID_ARG, "num_walkers, steps, timestep or walker_offset out of range");
-  if (mp->integrator < 0 || mp->integrator > 2)
+  if (mp->integrator < 0 || mp->integrator > 3)
     return mfail2(ctx, AXX_ERR_INVALID_ARG, "unknown integrator");
+  const int dp_K = mp->dorp_levels ? (int)mp->dorp_levels : 3;
+  const double dp_tol = mp->dorp_tol > 0.0 ? mp->dorp_tol : 1e-6;
+  if (mp->integrator == AXX_MAG_DORP &&
+      (mp->dorp_levels > 8 || !(mp->dorp_tol >= 0.0) || !std::isfinite(mp->dorp_tol)))
+    return mfail2(ctx, AXX_ERR_INVALID_ARG, "dorp_levels must be 0..8 and dorp_tol >= 0");
   // negative ratios are physical here (helium-3: the reference's magLF
   // examples use GAMMA = -203789): they reverse the precession
   if (!std::isfinite(mp->gamma))
@@ -498,8 +610,15 @@ axx_status mag_run(axx_ctx *ctx, const axx_basis *pore, const axx_field *fields,
   Q.h = (float)dt;
   Q.gh = (float)(-gamma * dt);
   for (int k = 0; k < 3; ++k) Q.m0[k] = (float)mp->m0[k];
-  std::vector<float4> tab, rk4, ms_rot, ms_tab;
+  std::vector<float4> tab, rk4, ms_rot, ms_tab, dp_tab;
   std::vector<int2> ms_idx;
+  if (mp->integrator == AXX_MAG_DORP) {
+    const size_t per = (size_t)6 * (size_t)((2 << dp_K) - 1);
+    if ((size_t)nf * (size_t)steps * per > ((size_t)1 << 27))
+      return mfail2(ctx, AXX_ERR_UNSUPPORTED,
+                    "Dormand-Prince tables above 2^27 entries: fewer steps or levels");
+    dp_tab.reserve((size_t)nf * (size_t)steps * per);
+  }
   for (int j = 0; j < nf; ++j) {
     const axx_field &f = fields[j];
     field_matrix(f, Q.A[j]);
@@ -508,7 +627,19 @@ axx_status mag_run(axx_ctx *ctx, const axx_basis *pore, const axx_field *fields,
     Q.c0[j] = (float)std::cos(a0);
     Q.s0[j] = (float)std::sin(a0);
     double c[3];
-    if (mp->integrator == AXX_MAG_ROTATE_MULTISTEP) {
+    if (mp->integrator == AXX_MAG_DORP) {
+      // stage times i dt + (m + c_s) dt / 2^k of every level and sub-step
+      static const double cs[6] = {0.0, 1.0 / 5.0, 3.0 / 10.0, 4.0 / 5.0, 8.0 / 9.0, 1.0};
+      for (int i = 0; i < steps; ++i)
+        for (int k = 0; k <= dp_K; ++k) {
+          const double h = dt / (double)(1 << k);
+          for (int m = 0; m < (1 << k); ++m)
+            for (int q = 0; q < 6; ++q) {
+              time_coef(f, gamma, i * dt + ((double)m + cs[q]) * h, c);
+              dp_tab.push_back(f4(c));
+            }
+        }
+    } else if (mp->integrator == AXX_MAG_ROTATE_MULTISTEP) {
       for (int i = 0; i < steps; ++i) {
         // updateMag_rotate_noT2_multistep (blochdiff.cuh:118-140)
         double acc = 0.0, tk = i * dt;
@@ -560,6 +691,8 @@ axx_status mag_run(axx_ctx *ctx, const axx_basis *pore, const axx_field *fields,
   off = up(off + ms_rot.size() * 16);
   const size_t o_mst = off;
   off = up(off + ms_tab.size() * 16);
+  const size_t o_dp = off;
+  off = up(off + dp_tab.size() * 16);
   const size_t o_part = off;
   off = up(off + (size_t)grid * nf * 3 * 8);
   const size_t o_out = off;
@@ -590,6 +723,7 @@ axx_status mag_run(axx_ctx *ctx, const axx_basis *pore, const axx_field *fields,
   put(o_msi, ms_idx.data(), ms_idx.size() * 8);
   put(o_msr, ms_rot.data(), ms_rot.size() * 16);
   put(o_mst, ms_tab.data(), ms_tab.size() * 16);
+  put(o_dp, dp_tab.data(), dp_tab.size() * 16);
   if (e != cudaSuccess) return mcuda2(ctx, e, "uploading the magnetisation tables");
   WalkParams P;
   const double cell[3] = {1.0, 1.0, 1.0};
@@ -598,6 +732,9 @@ axx_status mag_run(axx_ctx *ctx, const axx_basis *pore, const axx_field *fields,
   Q.rk4 = (const float4 *)(base + o_rk4);
   Q.ms_idx = (const int2 *)(base + o_msi);
   Q.ms_rot = (const float4 *)(base + o_msr);
+  Q.dp_tab = (const float4 *)(base + o_dp);
+  Q.dp_K = dp_K;
+  Q.dp_tol = (float)dp_tol;
   Q.ms_tab = (const float4 *)(base + o_mst);
   Q.partials = (double *)(base + o_part);
   Q.m_trace = (float *)(base + o_mtr);

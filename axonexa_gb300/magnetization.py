@@ -20,7 +20,7 @@ import numpy as np
 from . import _native as N
 from .acquisition import GAMMA, PI, Device, Vector3, default_device, linear_regression
 
-ROTATE, RK4, ROTATE_MULTISTEP = 0, 1, 2
+ROTATE, RK4, ROTATE_MULTISTEP, DORP = 0, 1, 2, 3
 
 
 def _vec(v):
@@ -209,24 +209,26 @@ class MagResult:
 
 
 def _mag_params(num_walkers, steps, timestep, seed, m0, integrator, specular, gamma,
-                walker_offset, fix_init_quirk):
+                walker_offset, fix_init_quirk, dorp_levels=0, dorp_tol=0.0):
     flags = (0 if specular else N.FLAG_SIMPLE_REJECTION) | (N.FLAG_FIX_INIT_QUIRK if fix_init_quirk else 0)
-    return N.MagParams(int(num_walkers), int(steps), int(integrator), flags, 0,
+    return N.MagParams(int(num_walkers), int(steps), int(integrator), flags, int(dorp_levels),
                        int(seed) & 0xFFFFFFFFFFFFFFFF, float(timestep), float(gamma),
-                       (C.c_double * 3)(*_vec(m0)), int(walker_offset))
+                       (C.c_double * 3)(*_vec(m0)), int(walker_offset), float(dorp_tol))
 
 
 def run_mag(pore, fields: Sequence[_Field], num_walkers: int, steps: int, timestep: float,
             seed: int, *, m0=(1.0, 0.0, 0.0), integrator: int = ROTATE, specular: bool = True,
             gamma: float = GAMMA, walker_offset: int = 0, fix_init_quirk: bool = False,
-            device: Device = None) -> MagResult:
+            dorp_levels: int = 0, dorp_tol: float = 0.0, device: Device = None) -> MagResult:
     """One magnetisation walk (axx_run_mag): walkers start in `pore`, every
-    field functor's magnetisation is summed over the walkers."""
+    field functor's magnetisation is summed over the walkers.  integrator
+    DORP: adaptive Dormand-Prince with up to `dorp_levels` halvings of the
+    step (0: 3) at tolerance `dorp_tol` (0: 1e-6)."""
     dev = device or default_device()
     nf = len(fields)
     f = N.array_of(N.Field, [q.record() for q in fields])
     p = _mag_params(num_walkers, steps, timestep, seed, m0, integrator, specular, gamma,
-                    walker_offset, fix_init_quirk)
+                    walker_offset, fix_init_quirk, dorp_levels, dorp_tol)
     out = [np.zeros(max(nf, 1)) for _ in range(3)]
     ptr = [o.ctypes.data_as(C.POINTER(C.c_double)) for o in out]
     N.check(N.lib().axx_run_mag(dev.h, C.byref(pore.record()), f, nf, C.byref(p), *ptr), dev.h)
@@ -236,14 +238,14 @@ def run_mag(pore, fields: Sequence[_Field], num_walkers: int, steps: int, timest
 def trace_mag(pore, fields: Sequence[_Field], num_trace: int, steps: int, timestep: float,
               seed: int, *, m0=(1.0, 0.0, 0.0), integrator: int = ROTATE,
               specular: bool = True, gamma: float = GAMMA, fix_init_quirk: bool = False,
-              device: Device = None) -> dict:
+              dorp_levels: int = 0, dorp_tol: float = 0.0, device: Device = None) -> dict:
     """The first num_trace walkers of the same walk: init_pos, pos, hits,
     words per move and the final magnetisation m [num_trace, nfield, 3]."""
     dev = device or default_device()
     nf = len(fields)
     f = N.array_of(N.Field, [q.record() for q in fields])
     p = _mag_params(num_trace, steps, timestep, seed, m0, integrator, specular, gamma, 0,
-                    fix_init_quirk)
+                    fix_init_quirk, dorp_levels, dorp_tol)
     n = num_trace * max(steps - 1, 0)
     ip = np.zeros(num_trace * 3, np.float32)
     pos = np.zeros(max(n, 1) * 3, np.float32)

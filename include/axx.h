@@ -492,21 +492,29 @@ typedef struct {
  * default exact rotation (updateMag_noT2_rotate).  RK4 (RK4_NORELAXATION):
  * fourth-order Runge-Kutta for the t = 0 update only -- the reference's step
  * loop has no RK4 branch and rotates.  ROTATE_MULTISTEP: rotations of the
- * functor's getStepTimeMin (QSC_PGSE and UCN_lowfield only). */
-enum { AXX_MAG_ROTATE = 0, AXX_MAG_RK4 = 1, AXX_MAG_ROTATE_MULTISTEP = 2 };
+ * functor's getStepTimeMin (QSC_PGSE and UCN_lowfield only).  DORP: adaptive
+ * Dormand-Prince 5(4) over every step (the integrator DORP_NORELAXATION aims
+ * at, updateMag_DORP, blochdiff.cuh:69-146, whose build does not compile):
+ * sub-steps dt/2^k, k <= dorp_levels, halved while the embedded error
+ * estimate exceeds dorp_tol (relative to 1 + |M|) and doubled when it falls
+ * below 1/32 of it; the field is evaluated at the true stage times, so it
+ * resolves fields that vary within a step.  For |gamma B| dt up to about 1
+ * (low field); the rotations are exact at any field. */
+enum { AXX_MAG_ROTATE = 0, AXX_MAG_RK4 = 1, AXX_MAG_ROTATE_MULTISTEP = 2, AXX_MAG_DORP = 3 };
 
 typedef struct {
   int64_t num_walkers;
   int32_t steps;       /* time points 0..steps-1, steps-1 moves */
   int32_t integrator;  /* AXX_MAG_* */
   uint32_t flags;      /* AXX_FLAG_SIMPLE_REJECTION, AXX_FLAG_FIX_INIT_QUIRK */
-  uint32_t pad;
+  uint32_t dorp_levels; /* DORP: halvings of the step allowed, 0..8 (0: 3) */
   uint64_t seed;
   double timestep;     /* ms */
   double gamma;        /* rad/(ms T); the reference's GAMMA macro (0: 267500;
                           negative for helium-3, -203789, as its magLF examples) */
   double m0[3];        /* initial magnetisation (SimuParams mx/my/mz_initial) */
   int64_t walker_offset;
+  double dorp_tol;     /* DORP: error tolerance (0: 1e-6) */
 } axx_mag_params;
 
 #define AXX_MAG_MAX_FIELDS 16

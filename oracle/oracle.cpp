@@ -1061,11 +1061,75 @@ V3 mag_multistep(const orc_field &f, double gamma, const V3 &r, V3 M, int i, dou
   return M;
 }
 
+// Adaptive Dormand-Prince 5(4) over [i dt, (i+1) dt] with the walker at r,
+// the integrator the reference's DORP_NORELAXATION build aims at
+// (updateMag_DORP, blochdiff.cuh:69-146, which does not compile).  Tableau
+// of Dormand & Prince (1980), J. Comput. Appl. Math. 6:19-26, the fifth-order
+// solution propagated; the error of the embedded fourth-order one, scaled per
+// component by tol (1 + max(|M5|, |M|)) and taken as an RMS over the three
+// components (the reference's error norm), decides.  Sub-steps are
+// dt / 2^k, k = 0..K, on a dyadic grid: a step whose error exceeds 1 is
+// retried at half the length (down to level K, where it is accepted); after
+// an accepted step with error below 1/32 the next step doubles when the grid
+// allows.  The product's kernel makes the same decisions in FP32.
+V3 mag_dorp(const orc_field &f, double gamma, const V3 &r, V3 M, int i, double dt, int K,
+            double tol) {
+  static const double c[6] = {0.0, 1.0 / 5.0, 3.0 / 10.0, 4.0 / 5.0, 8.0 / 9.0, 1.0};
+  static const double a[6][5] = {{0, 0, 0, 0, 0},
+                                 {1.0 / 5.0, 0, 0, 0, 0},
+                                 {3.0 / 40.0, 9.0 / 40.0, 0, 0, 0},
+                                 {44.0 / 45.0, -56.0 / 15.0, 32.0 / 9.0, 0, 0},
+                                 {19372.0 / 6561.0, -25360.0 / 2187.0, 64448.0 / 6561.0,
+                                  -212.0 / 729.0, 0},
+                                 {9017.0 / 3168.0, -355.0 / 33.0, 46732.0 / 5247.0, 49.0 / 176.0,
+                                  -5103.0 / 18656.0}};
+  static const double b[6] = {35.0 / 384.0, 0.0, 500.0 / 1113.0, 125.0 / 192.0,
+                              -2187.0 / 6784.0, 11.0 / 84.0};
+  // e = b - b*, the seventh entry multiplies the derivative at the new point
+  static const double e[7] = {71.0 / 57600.0, 0.0, -71.0 / 16695.0, 71.0 / 1920.0,
+                              -17253.0 / 339200.0, 22.0 / 525.0, -1.0 / 40.0};
+  auto deriv = [&](const V3 &m, double t) { return cross(m, bfield(f, gamma, r, t)) * gamma; };
+  const int full = 1 << K;
+  int pos = 0, k = 0;
+  for (int guard = 0; pos < full && guard < 64 * full; ++guard) {
+    const double h = dt / (double)(1 << k);
+    const double t0 = i * dt + (double)(pos >> (K - k)) * h;
+    V3 fk[7];
+    for (int s = 0; s < 6; ++s) {
+      V3 y = M;
+      for (int q = 0; q < s; ++q) y = y + fk[q] * (h * a[s][q]);
+      fk[s] = deriv(y, t0 + c[s] * h);
+    }
+    V3 y5 = M;
+    for (int q = 0; q < 6; ++q) y5 = y5 + fk[q] * (h * b[q]);
+    fk[6] = deriv(y5, t0 + h);
+    V3 err{0, 0, 0};
+    for (int q = 0; q < 7; ++q) err = err + fk[q] * (h * e[q]);
+    auto ratio = [&](double d, double m5, double m) {
+      return d / (tol * (1.0 + std::max(std::fabs(m5), std::fabs(m))));
+    };
+    const double rx = ratio(err.x, y5.x, M.x), ry = ratio(err.y, y5.y, M.y),
+                 rz = ratio(err.z, y5.z, M.z);
+    const double en = std::sqrt((rx * rx + ry * ry + rz * rz) / 3.0);
+    if (en <= 1.0 || k == K) {
+      M = y5;
+      pos += 1 << (K - k);
+      if (en < 1.0 / 32.0 && k > 0 && (pos & ((1 << (K - k + 1)) - 1)) == 0) --k;
+    } else {
+      ++k;
+    }
+  }
+  return M;
+}
+
 // The update updateWalkersMag applies for field f at step i (kernelMag.cuh:
 // 32-72 for i = 0, :96-134 for i >= 1).  With RK4_NORELAXATION only the i = 0
 // update is RK4: the step loop has no branch for it and rotates.
 V3 mag_update(const orc_field &f, const orc_mag_params &p, const V3 &r, const V3 &M, int i) {
   const double dt = p.timestep;
+  if (p.integrator == 3)
+    return mag_dorp(f, p.gamma, r, M, i, dt, p.dorp_levels ? (int)p.dorp_levels : 3,
+                    p.dorp_tol > 0.0 ? p.dorp_tol : 1e-6);
   if (p.integrator == 2) return mag_multistep(f, p.gamma, r, M, i, dt);
   if (p.integrator == 1 && i == 0) return mag_rk4(f, p.gamma, r, M, 0.0, dt);
   return mag_rotate(M, bfield(f, p.gamma, r, i * dt), dt, p.gamma);
@@ -1815,7 +1879,8 @@ void orc_mag_along(const orc_field *f, int nf, const orc_mag_params *p, const do
 int orc_mag_walk(const orc_basis *pore, const orc_field *f, int nf, const orc_mag_params *p,
                  int nthreads, double *sums, double *m_walk, orc_trace *trace) {
   if (!pore || !p || p->num_walkers < 1 || p->steps < 1 || !(p->timestep > 0.0)) return -1;
-  if (nf < 1 || !f || !sums || p->integrator < 0 || p->integrator > 2) return -1;
+  if (nf < 1 || !f || !sums || p->integrator < 0 || p->integrator > 3) return -1;
+  if (p->integrator == 3 && p->dorp_levels > 12) return -1;
   for (int j = 0; j < nf; ++j) {
     if (f[j].kind < 0 || f[j].kind > 7) return -1;
     if (p->integrator == 2 && f[j].kind != 1 && f[j].kind != 7) return -2;  // no getStepTimeMin

@@ -132,7 +132,9 @@ int orc_wc(const orc_basis *pore, int64_t n, int steps, double timestep, double 
  * Field kinds: 0 QSC_GRE, 1 QSC_PGSE, 2 QSC_COS_GRE, 3 QSC_GRE_TRAP,
  * 4 SIN_GRE, 5 COS_GRE, 6 RECT_GRE, 7 UCN_lowfield (src/functors/bfunctors.cuh).
  * Integrators: 0 rotation (the reference's default), 1 RK4 (RK4_NORELAXATION),
- * 2 multi-step rotation (ROTATE_MULTISTEP). */
+ * 2 multi-step rotation (ROTATE_MULTISTEP), 3 adaptive Dormand-Prince 5(4)
+ * on a dyadic grid of sub-steps (the integrator DORP_NORELAXATION aims at;
+ * no reference build exists: see mag_dorp in oracle.cpp). */
 typedef struct {
   int32_t kind, num_periods;
   double B0, G, gx, gy, gz, duration, spacing, period, ramp, rf_duration, dtmin, dtmax, TE;
@@ -142,10 +144,11 @@ typedef struct {
   int64_t num_walkers;
   int32_t steps, integrator;
   uint32_t flags; /* 4: simple rejection instead of specular reflection */
-  uint32_t pad;
+  uint32_t dorp_levels; /* integrator 3: halvings of the step allowed (0: 3) */
   uint64_t seed;
   double timestep, gamma, m0[3];
   int64_t walker_offset;
+  double dorp_tol; /* integrator 3: error tolerance (0: 1e-6) */
 } orc_mag_params;
 
 /* B(r, t) of one field functor (FP64, the reference's expressions). */

@@ -268,7 +268,7 @@ def gradient(seq, t: float):
 
 # ---- magnetisation (Bloch) path --------------------------------------------
 MAG_VARIANTS = ("mag_rot_spec", "mag_rot_rej", "mag_rk4_spec", "mag_ms_spec")
-ROTATE, RK4, MULTISTEP = 0, 1, 2
+ROTATE, RK4, MULTISTEP, DORP = 0, 1, 2, 3
 
 
 class Field(C.Structure):
@@ -281,20 +281,24 @@ class Field(C.Structure):
 
 class MagParams(C.Structure):
     _fields_ = [("num_walkers", C.c_int64), ("steps", C.c_int32), ("integrator", C.c_int32),
-                ("flags", C.c_uint32), ("pad", C.c_uint32), ("seed", C.c_uint64),
+                ("flags", C.c_uint32), ("dorp_levels", C.c_uint32), ("seed", C.c_uint64),
                 ("timestep", C.c_double), ("gamma", C.c_double), ("m0", C.c_double * 3),
-                ("walker_offset", C.c_int64)]
+                ("walker_offset", C.c_int64), ("dorp_tol", C.c_double)]
 
 
 def mag_params(n, steps, seed, dt, integrator=ROTATE, reject=False, gamma=267500.0,
-               m0=(1.0, 0.0, 0.0), offset=0):
-    return MagParams(n, steps, integrator, 4 if reject else 0, 0, seed, dt, gamma,
-                     (C.c_double * 3)(*m0), offset)
+               m0=(1.0, 0.0, 0.0), offset=0, dorp_levels=0, dorp_tol=0.0):
+    return MagParams(n, steps, integrator, 4 if reject else 0, dorp_levels, seed, dt, gamma,
+                     (C.c_double * 3)(*m0), offset, dorp_tol)
 
 
 def mag_variant(integrator: int, reject: bool) -> str:
+    """The reference build of an integrator, or None (no reference build:
+    rejection walks other than the rotation, and Dormand-Prince)."""
     if reject:
         return "mag_rot_rej" if integrator == ROTATE else None
+    if integrator == DORP:
+        return None
     return ("mag_rot_spec", "mag_rk4_spec", "mag_ms_spec")[integrator]
 
 

@@ -184,3 +184,60 @@ def test_mag_negative_gamma_helium3(dev, orc):
     # free precession sense: after one step My = -sin(-|gamma| B0 dt) > 0 for gamma < 0
     one = A.trace_mag(P, [A.QSC_GRE(1e-3, 0.0, 0.5, 0.6)], 1, 1, dt, 1, gamma=gam, device=dev)
     assert one["m"][0, 0, 1] > 0
+
+
+# ---- adaptive Dormand-Prince (AXX_MAG_DORP) -------------------------------
+
+def test_mag_dorp_per_walker_against_fp64(dev, orc):
+    """Every field functor kind, Dormand-Prince in FP32 on the GPU against
+    the oracle's FP64 Dormand-Prince along the same trajectories (the error
+    control may choose other sub-steps in FP32 near its threshold; both stay
+    within the tolerance's reach of the solution)."""
+    import axonexa_gb300 as A
+    pore, fields = _setup(orc, False, 3, False)
+    P, F = to_product(pore, fields)
+    n, steps, seed, dt = 32, 400, 61, 0.002
+    g = A.trace_mag(P, F, n, steps, dt, seed, integrator=3, device=dev)
+    p = cases.params(n, steps, seed, dt=dt, flags=0)
+    _, o, _ = orc.walk(None, [pore], [], p, orc.KERN32, ntrace=n)
+    np.testing.assert_array_equal(g["pos"].astype(np.float64), o["pos"])
+    mp = orc.mag_params(n, steps, seed, dt, integrator=orc.DORP)
+    worst = 0.0
+    for w in range(n):
+        pos = np.vstack([g["init_pos"][w][None], g["pos"][w]]).astype(np.float64)
+        worst = max(worst, float(np.abs(g["m"][w] - orc.mag_along(fields, mp, pos)).max()))
+    assert worst < 1e-3, worst
+    assert np.abs(np.linalg.norm(g["m"], axis=2) - 1.0).max() < 1e-3
+
+
+def test_mag_dorp_free_precession_and_sums(dev, orc):
+    import axonexa_gb300 as A
+    pore = A.Cylinder_XY(0.0, 0.0, 5e-3, 0.0, 0.0, 2e-6, 1, 0.0)
+    f = A.QSC_GRE(1e-3, 0.0, 0.5, 0.6)  # no gradient: B = B0 z everywhere
+    n, steps, dt = 2048, 700, 0.002
+    r = A.run_mag(pore, [f], n, steps, dt, 5, integrator=3, device=dev)
+    ang = -A.GAMMA * 1e-3 * dt * steps
+    assert abs(r.mx[0] / n - math.cos(ang)) < 1e-4
+    assert abs(r.my[0] / n - math.sin(ang)) < 1e-4
+    # sums of every functor kind against the FP64 walk with the same integrator
+    cpore, fields = _setup(orc, False, 3, False)
+    P, F = to_product(cpore, fields)
+    n, steps, seed = 1024, 300, 47
+    r = A.run_mag(P, F, n, steps, dt, seed, integrator=3, device=dev)
+    mp = orc.mag_params(n, steps, seed, dt, integrator=orc.DORP)
+    ref, mw, _ = orc.mag_walk(cpore, fields, mp, nthreads=8, ntrace=256)
+    got = np.stack([r.mx, r.my, r.mz], axis=1)
+    se = mw.std(axis=0) / math.sqrt(n)
+    d = np.abs(got - ref) / n
+    assert np.all(d <= 3.0 * se + 1e-3), (d - 3.0 * se).max()
+
+
+def test_mag_dorp_rejects_bad_parameters(dev):
+    import axonexa_gb300 as A
+    from axonexa_gb300 import _native as N
+    pore = A.Cylinder_XY(0.0, 0.0, 5e-3, 0.0, 0.0, 2e-6, 1, 0.0)
+    f = A.QSC_GRE(1e-3, 1e-3, 0.5, 0.6)
+    with pytest.raises(N.AxxError):
+        A.run_mag(pore, [f], 64, 10, 0.002, 5, integrator=3, dorp_levels=9, device=dev)
+    with pytest.raises(N.AxxError):
+        A.run_mag(pore, [f], 64, 10, 0.002, 5, integrator=3, dorp_tol=-1.0, device=dev)
