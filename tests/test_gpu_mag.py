@@ -217,8 +217,10 @@ def test_mag_dorp_free_precession_and_sums(dev, orc):
     n, steps, dt = 2048, 700, 0.002
     r = A.run_mag(pore, [f], n, steps, dt, 5, integrator=3, device=dev)
     ang = -A.GAMMA * 1e-3 * dt * steps
-    assert abs(r.mx[0] / n - math.cos(ang)) < 1e-4
-    assert abs(r.my[0] / n - math.sin(ang)) < 1e-4
+    # 374.5 rad over 700 steps: the phase error may grow by up to the
+    # tolerance (1e-6) per step
+    assert abs(r.mx[0] / n - math.cos(ang)) < 7e-4
+    assert abs(r.my[0] / n - math.sin(ang)) < 7e-4
     # sums of every functor kind against the FP64 walk with the same integrator
     cpore, fields = _setup(orc, False, 3, False)
     P, F = to_product(cpore, fields)
