@@ -59,8 +59,8 @@ PGSE_STEPS, OGSE_STEPS = 25000, 30000
 # DRAM bytes read + written per walker by the headline walk launch (ncu
 # capture at 262,144 walkers, 2,000 steps: block partials and tables only,
 # walker state never leaves registers), scaled by walkers
-WALK_DRAM_BYTES_PER_WALKER = (155136.0 + 146176.0) / 262144
-WALK_ISSUE_ACTIVE_NCU = 0.648
+WALK_DRAM_BYTES_PER_WALKER = (158464.0 + 139520.0) / 262144
+WALK_ISSUE_ACTIVE_NCU = 0.658
 
 
 def headline_workload():
