@@ -62,9 +62,10 @@ struct BatchItem {
 // registers) at the channel capacity of its own jobs.
 enum { BC_SCYL = 0,  // single cylinder pores
        BC_SSPH = 1,  // single sphere pores
-       BC_LCYL = 2,  // lattices of cylinders along z
+       BC_LCYL = 2,  // permeable lattices of cylinders along z
        BC_LMIX = 3,  // other lattices (spheres, mixed types, planes)
-       BC_N = 4 };
+       BC_LCYI = 4,  // impermeable lattices of cylinders along z
+       BC_N = 5 };
 
 // Resident blocks per SM the register budget targets: single pores as the
 // single-instance walk kernels; lattices one block fewer than the list walks
@@ -151,19 +152,16 @@ __global__ void __launch_bounds__(AXX_BLOCK, batch_min_blocks(KMAX, CLS))
           r = walk_one<AXX_GEOM_CYL, KMAX, AXX_KM_SINGLE, false, true>(sP, S, T, wid, W);
         } else if constexpr (CLS == BC_SSPH) {
           r = walk_one<AXX_GEOM_SPH, KMAX, AXX_KM_SINGLE, false, true>(sP, S, T, wid, W);
-        } else if constexpr (CLS == BC_LCYL) {
+        } else if constexpr (CLS == BC_LCYL || CLS == BC_LCYI) {
           // the single-instance walk up to four channels (as the single-job
-          // kernels), the list walk otherwise and above
+          // kernels), the list walk otherwise and above; permeable and
+          // impermeable lattices are separate classes, so that each kernel
+          // holds one walk (the two together spilled 148 bytes at eight
+          // channels, the permeable walk alone 32)
           constexpr bool one_ok = KMAX <= 4;
-          if (sP.km == AXX_KM_LAT_PERM) {
-            r = (one_ok && one)
-                    ? walk_one<AXX_GEOM_CYL, KMAX, AXX_KM_LAT_PERM, false, one_ok>(sP, S, T, wid, W)
-                    : walk_one<AXX_GEOM_CYL, KMAX, AXX_KM_LAT_PERM, false, false>(sP, S, T, wid, W);
-          } else {
-            r = (one_ok && one)
-                    ? walk_one<AXX_GEOM_CYL, KMAX, AXX_KM_LAT_IMP, false, one_ok>(sP, S, T, wid, W)
-                    : walk_one<AXX_GEOM_CYL, KMAX, AXX_KM_LAT_IMP, false, false>(sP, S, T, wid, W);
-          }
+          constexpr int km = CLS == BC_LCYL ? AXX_KM_LAT_PERM : AXX_KM_LAT_IMP;
+          r = (one_ok && one) ? walk_one<AXX_GEOM_CYL, KMAX, km, false, one_ok>(sP, S, T, wid, W)
+                              : walk_one<AXX_GEOM_CYL, KMAX, km, false, false>(sP, S, T, wid, W);
         } else {
           // other lattices: the mixed-type walk (single instance or list)
           if (sP.km == AXX_KM_LAT_PERM) {
@@ -279,6 +277,7 @@ static cudaError_t batch_go(int cls, int kmax, int grid, size_t smem, cudaStream
     case BC_SCYL: return batch_go_cls<BC_SCYL>(kmax, grid, smem, s, jobs, items, nitems, ctr, part);
     case BC_SSPH: return batch_go_cls<BC_SSPH>(kmax, grid, smem, s, jobs, items, nitems, ctr, part);
     case BC_LCYL: return batch_go_cls<BC_LCYL>(kmax, grid, smem, s, jobs, items, nitems, ctr, part);
+    case BC_LCYI: return batch_go_cls<BC_LCYI>(kmax, grid, smem, s, jobs, items, nitems, ctr, part);
     default: return batch_go_cls<BC_LMIX>(kmax, grid, smem, s, jobs, items, nitems, ctr, part);
   }
 }
@@ -299,6 +298,7 @@ static int batch_occupancy(int cls, int kmax, size_t smem) {
     case BC_SCYL: return batch_occupancy_cls<BC_SCYL>(kmax, smem);
     case BC_SSPH: return batch_occupancy_cls<BC_SSPH>(kmax, smem);
     case BC_LCYL: return batch_occupancy_cls<BC_LCYL>(kmax, smem);
+    case BC_LCYI: return batch_occupancy_cls<BC_LCYI>(kmax, smem);
     default: return batch_occupancy_cls<BC_LMIX>(kmax, smem);
   }
 }
@@ -551,7 +551,7 @@ static axx_status batch_build(axx_ctx *ctx, const axx_job *jobs, int njobs,
   };
   std::vector<JobPlan> jp(njobs);
   int kmax = 1;
-  int ckmax[BC_N] = {1, 1, 1, 1};
+  int ckmax[BC_N] = {1, 1, 1, 1, 1};
   for (int j = 0; j < njobs; ++j) {
     const axx_job &J = jobs[j];
     JobPlan &q = jp[j];
@@ -588,8 +588,12 @@ static axx_status batch_build(axx_ctx *ctx, const axx_job *jobs, int njobs,
     }
     if (err.empty()) err = plan_sequences(q.f.seqs_p, J.nseq, p.steps, p.timestep, gamma, q.sq);
     if (!err.empty()) return bfail(ctx, AXX_ERR_INVALID_ARG, "job " + std::to_string(j) + ": " + err);
-    q.cls = J.mode == AXX_MODE_SINGLE ? (q.g.geom == AXX_GEOM_SPH ? BC_SSPH : BC_SCYL)
-                                      : (q.g.geom == AXX_GEOM_CYL ? BC_LCYL : BC_LMIX);
+    if (J.mode == AXX_MODE_SINGLE)
+      q.cls = q.g.geom == AXX_GEOM_SPH ? BC_SSPH : BC_SCYL;
+    else if (q.g.geom == AXX_GEOM_CYL)
+      q.cls = walk_mode(J.mode, q.g.geom, p.flags) == AXX_KM_LAT_PERM ? BC_LCYL : BC_LCYI;
+    else
+      q.cls = BC_LMIX;
     int k = 1;
     while (k < (int)q.sq.channels.size()) k <<= 1;
     kmax = std::max(kmax, k);

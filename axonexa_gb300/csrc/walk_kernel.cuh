@@ -890,12 +890,11 @@ __device__ __forceinline__ void do_move(const WalkParams &P, const SmemView &S,
   constexpr bool single = KM >= AXX_KM_SINGLE;
   constexpr bool perm = KM == AXX_KM_LAT_PERM;
   constexpr bool reject = KM == AXX_KM_LAT_REJ || KM == AXX_KM_SINGLE_REJ;
-  constexpr bool PX = PAX & 1, PY = PAX & 2, NOZ = !(PAX & 4);
+  constexpr bool NOZ = !(PAX & 4);
   // a single pore, or one instance behind impermeable walls: the walker's
   // slot never changes, and its speed and step stay in registers (the T2
   // term, .z, is then not read per move)
   constexpr bool fixed_slot = ONE && (single || KM == AXX_KM_LAT_IMP);
-  constexpr bool tracked = KM == AXX_KM_LAT_IMP || KM == AXX_KM_LAT_PERM;
   // permeable walks hold their slot's values in registers (reloaded when the
   // slot changes); impermeable list walks read them per move (the registers
   // would spill there)

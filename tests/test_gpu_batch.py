@@ -53,9 +53,10 @@ def test_batch_graph_replay_is_deterministic(dev):
         np.testing.assert_array_equal(a.my, c.my)
     info = b.info()
     # one persistent kernel per job class present (single cylinders, single
-    # spheres, lattices) and the partial-sum reduction
-    classes = {("lattice" if j.lattice is not None else type(j.basis[0]).__name__)
-               for j in b_jobs}
+    # spheres, permeable and impermeable cylinder lattices) and the
+    # partial-sum reduction
+    classes = {(("lattice_perm" if j.permeable else "lattice") if j.lattice is not None
+                else type(j.basis[0]).__name__) for j in b_jobs}
     assert info["items"] > 12 and info["kernel_launches"] == 1 + len(classes)
     b.close()
 
