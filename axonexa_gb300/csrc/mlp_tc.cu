@@ -3,7 +3,7 @@
 // A persistent CTA per SM carries two 128-row tiles of queries through every
 // layer, with three warp roles (576 threads):
 //   * warp 16 (producer) streams the packed BF16 weights, chunk by chunk
-//     (N 256 x K 32, 16 KB), into a 5-slot shared-memory ring with
+//     (N 256 x K 64, 32 KB), into a 3-slot shared-memory ring with
 //     cp.async.bulk; each slot has a "full" mbarrier (transaction bytes) and
 //     an "empty" one (released by the tensor cores when the chunk's MMAs are
 //     done);
@@ -14,11 +14,16 @@
 //     mbarrier;
 //   * warps 0-15 (epilogue; warp w reads TMEM lanes 32(w%4).. -- one row per
 //     thread -- and the 64 columns 64(w/4)..) read the accumulator with
-//     tcgen05.ld, add the bias, apply SiLU (z sigmoid z = h + h tanh h with
-//     h = z/2, on the MUFU tanh) and write the BF16 activations back into the
-//     tile's shared-memory operand; after the last hidden layer the four
-//     column groups' parts of y = h . w_out meet in shared memory (an
-//     mbarrier) and the first group adds b_out and stores y.
+//     tcgen05.ld, add the bias (read through L1: one address per warp), apply
+//     SiLU (z sigmoid z = h + h tanh h with h = z/2, on the MUFU tanh) and
+//     write the BF16 activations back into the tile's shared-memory operand;
+//     after the last hidden layer the four column groups' parts of
+//     y = h . w_out meet in the tail of the tile's operand (an mbarrier) and
+//     the first group adds b_out and stores y.
+// Shared memory holds the two 64 KB operands and the 96 KB ring and nothing
+// else: 64-column chunks halve the MMA warp's waits per MMA against 32-column
+// ones (a wait between MMAs lets the tensor pipe drain), and three of them
+// fit only with the biases out of shared memory.
 // The MMA warp alternates the two tiles, so one tile's epilogue overlaps the
 // other tile's MMAs, and weight copies run ahead of both.
 // Operand layout (A activations and B weight chunks): canonical K-major
@@ -43,18 +48,18 @@ namespace axx {
 
 constexpr int TC_ROWS = 128;
 constexpr int TC_N = 256;
-constexpr int TC_KC = 32;                          // K columns per weight chunk
-constexpr int TC_CHUNK_BYTES = TC_N * TC_KC * 2;   // 16 KB
-constexpr int TC_STAGES = 5;
+constexpr int TC_KC = 64;                          // K columns per weight chunk
+constexpr int TC_CHUNK_BYTES = TC_N * TC_KC * 2;   // 32 KB
+constexpr int TC_STAGES = 3;
 constexpr int TC_TILES = 2;                        // row tiles in flight
 constexpr int TC_ACT_BYTES = TC_ROWS * TC_N * 2;   // 64 KB per row tile
 constexpr int TC_OFF_RING = TC_TILES * TC_ACT_BYTES;
-constexpr int TC_OFF_BIAS = TC_OFF_RING + TC_STAGES * TC_CHUNK_BYTES;
-constexpr int TC_BIAS_FLOATS = 9 * TC_N;           // up to 8 hidden biases + w_out
 constexpr int TC_GROUPS = 4;                       // epilogue column groups
 constexpr int TC_GCOLS = TC_N / TC_GROUPS;
-constexpr int TC_OFF_YPART = TC_OFF_BIAS + TC_BIAS_FLOATS * 4;  // [group-1][tile][row] parts of y
-constexpr int TC_OFF_BAR = TC_OFF_YPART + (TC_GROUPS - 1) * TC_TILES * TC_ROWS * 4;
+// the column groups' parts of y meet in the last 1.5 KB of the tile's
+// operand, which the tile's last-layer MMAs have finished reading
+constexpr int TC_YPART_BYTES = (TC_GROUPS - 1) * TC_ROWS * 4;
+constexpr int TC_OFF_BAR = TC_OFF_RING + TC_STAGES * TC_CHUNK_BYTES;
 constexpr int TC_SMEM = TC_OFF_BAR + 256;
 constexpr int TC_EPI_THREADS = TC_GROUPS * TC_ROWS;
 constexpr int TC_THREADS = TC_EPI_THREADS + 64;
@@ -91,8 +96,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1) mlp_tc_kernel(const __grid_cons
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ volatile int s_fail;
   __shared__ uint32_t s_tmem;
-  float *sbias = reinterpret_cast<float *>(smem + TC_OFF_BIAS);
-  float *ypart = reinterpret_cast<float *>(smem + TC_OFF_YPART);
   const uint32_t bar0 = smem_u32(smem + TC_OFF_BAR);
   // barrier addresses: full[5], empty[5], act_ready[2], acc_full[2], drain,
   // y_half[2]
@@ -105,10 +108,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1) mlp_tc_kernel(const __grid_cons
   const uint32_t act0 = smem_u32(smem), ring0 = smem_u32(smem + TC_OFF_RING);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
-  // biases pre-halved: the epilogue works on h = z/2
-  for (int i = tid; i < a.depth * TC_N; i += TC_THREADS)
-    sbias[i] = 0.5f * a.bias[i / TC_N][i % TC_N];
-  for (int i = tid; i < TC_N; i += TC_THREADS) sbias[8 * TC_N + i] = a.w_out[i];
   if (tid == 0) {
     s_fail = 0;
     for (int s = 0; s < TC_STAGES; ++s) {
@@ -254,7 +253,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) mlp_tc_kernel(const __grid_cons
       float yacc[TC_TILES] = {0.f, 0.f};
       for (int l = 0; l < a.depth && ok; ++l) {
         const bool last = (l == a.depth - 1);
-        const float *bl = sbias + l * TC_N;
+        const float *bl = a.bias[l];  // read through L1: the same address across a warp
 #pragma unroll
         for (int t = 0; t < TC_TILES; ++t) {
           if (base + t >= ntiles) continue;
@@ -277,9 +276,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1) mlp_tc_kernel(const __grid_cons
             if (last) {
 #pragma unroll
               for (int q = 0; q < 8; ++q) {
-                const float4 b4 = *reinterpret_cast<const float4 *>(bl + cb + 4 * q);
-                const float4 w4 = *reinterpret_cast<const float4 *>(sbias + 8 * TC_N + cb + 4 * q);
-                const float bb[4] = {b4.x, b4.y, b4.z, b4.w}, ww[4] = {w4.x, w4.y, w4.z, w4.w};
+                const float4 b4 = __ldg(reinterpret_cast<const float4 *>(bl + cb + 4 * q));
+                const float4 w4 = __ldg(reinterpret_cast<const float4 *>(a.w_out + cb + 4 * q));
+                // the biases halved (exact): the epilogue works on h = z/2
+                const float bb[4] = {0.5f * b4.x, 0.5f * b4.y, 0.5f * b4.z, 0.5f * b4.w},
+                            ww[4] = {w4.x, w4.y, w4.z, w4.w};
 #pragma unroll
                 for (int j = 0; j < 4; ++j)
                   ys = fmaf(silu_half(__uint_as_float(v[4 * q + j]), bb[j]), ww[j], ys);
@@ -287,9 +288,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) mlp_tc_kernel(const __grid_cons
             } else {
 #pragma unroll
               for (int q = 0; q < 4; ++q) {
-                const float4 b0 = *reinterpret_cast<const float4 *>(bl + cb + 8 * q);
-                const float4 b1 = *reinterpret_cast<const float4 *>(bl + cb + 8 * q + 4);
-                const float bb[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+                const float4 b0 = __ldg(reinterpret_cast<const float4 *>(bl + cb + 8 * q));
+                const float4 b1 = __ldg(reinterpret_cast<const float4 *>(bl + cb + 8 * q + 4));
+                const float bb[8] = {0.5f * b0.x, 0.5f * b0.y, 0.5f * b0.z, 0.5f * b0.w,
+                                     0.5f * b1.x, 0.5f * b1.y, 0.5f * b1.z, 0.5f * b1.w};
                 __align__(16) __nv_bfloat162 hb[4];
 #pragma unroll
                 for (int j = 0; j < 4; ++j)
@@ -317,7 +319,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) mlp_tc_kernel(const __grid_cons
       for (int t = 0; t < TC_TILES; ++t) {
         if (base + t >= ntiles) continue;
         if (grp > 0) {
-          ypart[((grp - 1) * TC_TILES + t) * TC_ROWS + r] = yacc[t];
+          reinterpret_cast<float *>(smem + (t + 1) * TC_ACT_BYTES - TC_YPART_BYTES)[(grp - 1) * TC_ROWS + r] =
+              yacc[t];
           mbar_arrive(yh_bar(t));
         } else {
           const bool got = mbar_wait(yh_bar(t), py[t], &s_fail);
@@ -327,8 +330,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) mlp_tc_kernel(const __grid_cons
           }
           const int gr = (base + t) * TC_ROWS + r;
           float yv = yacc[t];
+          const float *yp =
+              reinterpret_cast<const float *>(smem + (t + 1) * TC_ACT_BYTES - TC_YPART_BYTES);
 #pragma unroll
-          for (int g2 = 1; g2 < TC_GROUPS; ++g2) yv += ypart[((g2 - 1) * TC_TILES + t) * TC_ROWS + r];
+          for (int g2 = 1; g2 < TC_GROUPS; ++g2) yv += yp[(g2 - 1) * TC_ROWS + r];
           if (gr < a.n) a.y[gr] = yv + __ldg(a.b_out);
         }
         py[t] ^= 1u;
