@@ -693,7 +693,7 @@ class phaseAcquisitionStream:
     def runAcquisitionWC(self, num, basis, timestep, blocks=None, threads=None):
         """runAcquisitionWC (phaseAcquisitionStream.cuh:193-252): per
         measurement the WCDMC walker (axx_run_wc) with the functor's G(j dt)
-        table.  The driver's host draws (per-walker xorshift states and
+        table.  The host-side draws (per-walker xorshift states and
         start points in the pore) come from a generator seeded with the
         acquisition's seed instead of srand/rand."""
         acq = self.acqSet[num]
