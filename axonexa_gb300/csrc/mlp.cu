@@ -369,9 +369,12 @@ extern "C" axx_status axx_mlp_create(axx_ctx *ctx, int in_dim, int width, int de
   return AXX_OK;
 }
 
+static void predict_io_free(axx_mlp *m);
+
 extern "C" axx_status axx_mlp_destroy(axx_mlp *m) {
   if (!m) return AXX_OK;
   if (m->ctx) cudaStreamSynchronize(m->ctx->stream);
+  predict_io_free(m);
   if (m->params) cudaFree(m->params);
   if (m->wb_all) cudaFree(m->wb_all);
   if (m->work) cudaFree(m->work);
@@ -480,23 +483,94 @@ extern "C" axx_status axx_mlp_train(axx_mlp *m, const float *X, const float *y, 
   return tc_status(m);
 }
 
+// The device buffers, streams and events of inference from host memory,
+// made at the first call and kept (the buffers grown when a call needs more
+// rows; every earlier call has drained its streams before returning).
+static cudaError_t predict_io(axx_mlp *m, long long n) {
+  cudaError_t e = cudaSuccess;
+  auto event = [&](cudaEvent_t &ev) {
+    if (e == cudaSuccess && !ev) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+  };
+  if (!m->s_in) e = cudaStreamCreateWithFlags(&m->s_in, cudaStreamNonBlocking);
+  if (e == cudaSuccess && !m->s_out) e = cudaStreamCreateWithFlags(&m->s_out, cudaStreamNonBlocking);
+  event(m->ev_start);
+  for (int i = 0; i < axx_mlp::kMaxChunks; ++i) {
+    event(m->ev_in[i]);
+    event(m->ev_done[i]);
+  }
+  if (e == cudaSuccess && n > m->io_rows) {
+    if (m->io) cudaFree(m->io);
+    m->io = nullptr;
+    m->io_rows = 0;
+    e = cudaMalloc(&m->io, (size_t)n * (m->in_dim + 1) * 4);
+    if (e == cudaSuccess) m->io_rows = n;
+  }
+  return e;
+}
+
+static void predict_io_free(axx_mlp *m) {
+  if (m->io) cudaFree(m->io);
+  if (m->s_in) cudaStreamDestroy(m->s_in);
+  if (m->s_out) cudaStreamDestroy(m->s_out);
+  if (m->ev_start) cudaEventDestroy(m->ev_start);
+  for (int i = 0; i < axx_mlp::kMaxChunks; ++i) {
+    if (m->ev_in[i]) cudaEventDestroy(m->ev_in[i]);
+    if (m->ev_done[i]) cudaEventDestroy(m->ev_done[i]);
+  }
+}
+
+// Inference from host memory as a pipeline of up to four chunks (whole waves
+// of the persistent kernel, about a quarter of the rows each): chunk i's
+// queries cross on one copy stream while chunk i-1 runs on the context's
+// stream, and the outputs come back on another copy stream.  The rows of a
+// chunk are computed exactly as in one launch over all rows (every row is
+// independent), so the outputs equal axx_mlp_predict_device's bit for bit.
 extern "C" axx_status axx_mlp_predict(axx_mlp *m, const float *X, int n, float *y) {
   if (!m || !X || !y || n < 0) return AXX_ERR_INVALID_ARG;
   if (n == 0) return AXX_OK;
-  float *dX = nullptr, *dY = nullptr;
-  cudaError_t e = upload_xy(m, X, nullptr, n, &dX, &dY);
+  cudaError_t e = predict_io(m, n);
+  if (e != cudaSuccess) return mcuda(m->ctx, e, "axx_mlp_predict");
+  const cudaStream_t s = m->ctx->stream;
+  const long long wave = mlp_tc_rows_per_wave(m), d = m->in_dim;
+  const long long chunk = ((n + axx_mlp::kMaxChunks - 1) / axx_mlp::kMaxChunks + wave - 1) / wave * wave;
+  const int nch = (int)((n + chunk - 1) / chunk);
+  float *dX = m->io, *dY = m->io + (size_t)n * d;
   axx_status st = AXX_OK;
-  if (e == cudaSuccess) st = axx_mlp_predict_device(m, dX, n, dY);
-  if (e == cudaSuccess && st == AXX_OK) e = cudaStreamSynchronize(m->ctx->stream);
-  if (e == cudaSuccess && st == AXX_OK) e = cudaMemcpy(y, dY, (size_t)n * 4, cudaMemcpyDeviceToHost);
+  // the copy streams start after the work already queued on the context
+  e = cudaEventRecord(m->ev_start, s);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(m->s_in, m->ev_start, 0);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(m->s_out, m->ev_start, 0);
+  int queued = 0;
+  for (int i = 0; i < nch && e == cudaSuccess && st == AXX_OK; ++i) {
+    const long long r0 = i * chunk, rn = std::min<long long>(chunk, n - r0);
+    e = cudaMemcpyAsync(dX + r0 * d, X + r0 * d, (size_t)(rn * d) * 4, cudaMemcpyHostToDevice,
+                        m->s_in);
+    if (e == cudaSuccess) e = cudaEventRecord(m->ev_in[i], m->s_in);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, m->ev_in[i], 0);
+    if (e == cudaSuccess) st = axx_mlp_predict_device(m, dX + r0 * d, (int)rn, dY + r0);
+    if (e == cudaSuccess && st == AXX_OK) e = cudaEventRecord(m->ev_done[i], s);
+    if (e == cudaSuccess && st == AXX_OK) ++queued;
+  }
+  // the outputs once every chunk is queued (a copy into pageable memory
+  // returns only when it has completed)
+  for (int i = 0; i < queued && e == cudaSuccess; ++i) {
+    const long long r0 = i * chunk, rn = std::min<long long>(chunk, n - r0);
+    e = cudaStreamWaitEvent(m->s_out, m->ev_done[i], 0);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(y + r0, dY + r0, (size_t)rn * 4, cudaMemcpyDeviceToHost, m->s_out);
+  }
+  // drain all three streams whatever happened: no copy may still touch the
+  // caller's memory after the return
+  const cudaError_t e_in = cudaStreamSynchronize(m->s_in);
+  const cudaError_t e_run = cudaStreamSynchronize(s);
+  const cudaError_t e_out = cudaStreamSynchronize(m->s_out);
+  if (e == cudaSuccess) e = e_in != cudaSuccess ? e_in : (e_run != cudaSuccess ? e_run : e_out);
   int tc_err = 0;
   if (e == cudaSuccess && st == AXX_OK) e = cudaMemcpy(&tc_err, m->tc_error, 4, cudaMemcpyDeviceToHost);
   if (e == cudaSuccess && st == AXX_OK && tc_err) {
     cudaMemset(m->tc_error, 0, 4);
     st = mfail(m->ctx, AXX_ERR_TIMEOUT, "a tensor-core completion wait ran out");
   }
-  if (dX) cudaFree(dX);
-  if (dY) cudaFree(dY);
   if (st != AXX_OK) return st;
   if (e != cudaSuccess) return mcuda(m->ctx, e, "axx_mlp_predict");
   return AXX_OK;

@@ -26,6 +26,14 @@ struct axx_mlp {
   float *tb = nullptr, *yb = nullptr, *dy = nullptr, *Cb = nullptr, *Z = nullptr, *dH = nullptr,
         *dZ = nullptr, *loss = nullptr;
   float *kpart = nullptr;  // split-K partials of the weight-gradient GEMMs
+  // inference from host memory: device copies of the queries and outputs
+  // (grown on demand, kept between calls), and the copy streams and events
+  // of the chunk pipeline (queries of chunk i+1 cross while chunk i runs)
+  static constexpr int kMaxChunks = 4;
+  float *io = nullptr;
+  long long io_rows = 0;
+  cudaStream_t s_in = nullptr, s_out = nullptr;
+  cudaEvent_t ev_start = nullptr, ev_in[kMaxChunks] = {}, ev_done[kMaxChunks] = {};
   float *weight(int l) const { return params + w_off[l]; }
   float *bias(int l) const { return params + b_off[l]; }
   float *grad_weight(int l) const { return grad + w_off[l]; }
@@ -48,4 +56,6 @@ cudaError_t gemm_tc_init();
 // tensor-core inference (mlp_tc.cu)
 cudaError_t mlp_tc_init(axx_mlp *m);
 void mlp_tc_free(axx_mlp *m);
+// Rows one wave of the persistent inference kernel covers on this device.
+long long mlp_tc_rows_per_wave(const axx_mlp *m);
 void mlp_pack_tc(axx_mlp *m);

@@ -393,6 +393,10 @@ void mlp_tc_free(axx_mlp *m) {
   m->wtc = nullptr;
 }
 
+long long mlp_tc_rows_per_wave(const axx_mlp *m) {
+  return (long long)TC_ROWS * TC_TILES * m->ctx->nsm;
+}
+
 void mlp_pack_tc(axx_mlp *m) {
   for (int l = 0; l < m->depth; ++l) {
     const int in = l == 0 ? m->in_dim : TC_N, pad = l == 0 ? m->in_pad : TC_N;

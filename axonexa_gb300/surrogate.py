@@ -115,9 +115,16 @@ class MLP:
                                       loss.ctypes.data_as(C.POINTER(C.c_float))), self.dev.h)
         return loss[:steps]
 
-    def predict(self, X) -> np.ndarray:
+    def predict(self, X, out=None) -> np.ndarray:
+        """Outputs for the rows of X (host memory); out: a float32 array of
+        len(X) to write them into (pinned host memory lets the chunks' copies
+        overlap the kernel)."""
         X, px = self._f(X)
-        y = np.zeros(len(X), np.float32)
+        if out is None:
+            out = np.zeros(len(X), np.float32)
+        if out.dtype != np.float32 or out.shape != (len(X),) or not out.flags.c_contiguous:
+            raise ValueError("out must be a contiguous float32 array of len(X)")
+        y = out
         N.check(N.lib().axx_mlp_predict(self.h, px, len(X),
                                         y.ctypes.data_as(C.POINTER(C.c_float))), self.dev.h)
         return y

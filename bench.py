@@ -366,17 +366,27 @@ def surrogate_section(A, N, L, dev, queries=1000000, reps=10, plain_subs=2):
                                                              y.data_ptr()), reps)
     ms = float(np.median(times))
     flops = m.flops_per_row() * queries
-    Xh = X.cpu().numpy()
+    # end to end: queries in and outputs out through pinned host memory
+    Xp = torch.empty((queries, 10), dtype=torch.float32, pin_memory=True)
+    Xp.copy_(X)
+    yp = torch.empty(queries, dtype=torch.float32, pin_memory=True)
+    Xh, yh = Xp.numpy(), yp.numpy()
     m.predict(Xh[:4096])
-    t0 = time.perf_counter()
-    yh = m.predict(Xh)
-    e2e_s = time.perf_counter() - t0
+    e2e = []
+    for _ in range(5):
+        t0 = time.perf_counter()
+        m.predict(Xh, out=yh)
+        e2e.append(time.perf_counter() - t0)
+    e2e_s = float(np.median(e2e))
     assert np.array_equal(yh, y.cpu().numpy()), "host and device inference disagree"
     peaks = measured_peaks()
     pk = peaks.get("bf16_tflops")
     out.update({"queries": queries, "signals_per_s": queries / (ms * 1e-3), "ms": ms,
                 "e2e_signals_per_s": queries / e2e_s, "h2d_bytes": int(Xh.nbytes),
                 "d2h_bytes": int(4 * queries), "kernel_launches_per_call": 1,
+                "e2e_path": "axx_mlp_predict from pinned host memory (median of 5 calls): "
+                            "up to 4 chunks of whole kernel waves, each chunk's copy in "
+                            "overlapping the previous chunk's kernel",
                 "roofline": {"bound": "tensor", "achieved": flops / (ms * 1e-3) / 1e12,
                              "peak": pk, "unit": "TFLOP/s",
                              "frac": (flops / (ms * 1e-3) / 1e12 / pk) if pk else None,

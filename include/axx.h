@@ -365,7 +365,11 @@ axx_status axx_mlp_gradients(axx_mlp *m, const float *X, const float *y, int n, 
  * entries) receives each batch loss. */
 axx_status axx_mlp_train(axx_mlp *m, const float *X, const float *y, int n, int batch, int steps,
                          float lr, uint64_t seed, float *loss_out);
-/* Predictions for host inputs (X[n][in_dim] -> y[n]) on the tensor cores. */
+/* Predictions for host inputs (X[n][in_dim] -> y[n]) on the tensor cores.
+ * The rows cross in up to four chunks whose copies overlap the kernel (the
+ * overlap needs pinned host memory); the outputs equal
+ * axx_mlp_predict_device's bit for bit.  The device copies of X and y are
+ * kept with the network and grow to the largest n seen. */
 axx_status axx_mlp_predict(axx_mlp *m, const float *X, int n, float *y);
 /* Device-resident prediction for timing: X and y are device pointers. */
 axx_status axx_mlp_predict_device(axx_mlp *m, const float *dX, int n, float *dy);

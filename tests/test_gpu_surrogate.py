@@ -87,6 +87,31 @@ def test_tensor_core_forward_matches_fp64_cpu(dev):
     assert err.mean() < 5e-3, err.mean()
 
 
+def test_host_memory_chunks_equal_device_inference(dev):
+    """Inference from host memory runs as a pipeline of chunks (whole waves
+    of the persistent kernel); every row is independent, so the outputs equal
+    one device-resident launch over all rows bit for bit, for a ragged row
+    count over several chunks, into a caller's array, and again on the kept
+    buffers with fewer rows."""
+    import torch
+    from axonexa_gb300.surrogate import MLP
+    rng = np.random.default_rng(4)
+    m = MLP(seed=7, device=dev)
+    for n in (100_003, 38_913, 1):
+        Q = rng.uniform(-1, 1, size=(n, 10)).astype(np.float32)
+        X = torch.from_numpy(Q).cuda()
+        y = torch.empty(n, device="cuda")
+        m.predict_device(X.data_ptr(), n, y.data_ptr())
+        torch.cuda.synchronize()
+        out = np.full(n, np.nan, np.float32)
+        got = m.predict(Q, out=out)
+        assert got is out
+        np.testing.assert_array_equal(out, y.cpu().numpy())
+    with pytest.raises(ValueError):
+        m.predict(Q, out=np.zeros(n + 1, np.float32))
+    m.close()
+
+
 def test_training_reduces_loss(dev):
     from axonexa_gb300.surrogate import MLP
     rng = np.random.default_rng(2)
