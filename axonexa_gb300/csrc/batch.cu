@@ -77,6 +77,21 @@ constexpr int batch_min_blocks(int kmax, int cls) {
                                          : AXX_MIN_BLOCKS_FOR(kmax);
 }
 
+// Table budget of a lattice job's plan (the finer cell grids of the list
+// walk, which leave fewer candidates per move): the shared memory of one
+// block at the lattice classes' minimum resident blocks for the job's
+// channels (228 KB per SM, 1 KB of it reserved per block), less the staged
+// parameters, the per-warp sums and the slot table.
+static size_t batch_list_budget(int channels, int nbasis) {
+  int k = 1;
+  while (k < channels) k <<= 1;
+  const size_t per_block = (size_t)228 * 1024 / batch_min_blocks(k, BC_LCYL) - 1024;
+  const size_t fixed = ((sizeof(WalkParams) + 15) & ~(size_t)15) +
+                       (size_t)(AXX_BLOCK / 32) * kBatchMaxSeq * 5 * sizeof(double) +
+                       (size_t)(nbasis + 2) * 20;
+  return per_block > fixed ? per_block - fixed : 0;
+}
+
 template <int KMAX, int CLS>
 __global__ void __launch_bounds__(AXX_BLOCK, batch_min_blocks(KMAX, CLS))
     batch_kernel(const BatchJob *__restrict__ jobs, const BatchItem *__restrict__ items,
@@ -579,14 +594,18 @@ static axx_status batch_build(axx_ctx *ctx, const axx_job *jobs, int njobs,
       q.cell[0] = q.cell[1] = q.cell[2] = 1.0;
     } else {
       err = frame_lattice(&J.lattice, J.basis, J.nbasis, J.seqs, J.nseq, q.f);
-      if (err.empty()) err = plan_lattice(q.f.lat_p, q.f.basis_p, J.nbasis, p.timestep, p.flags, q.g);
+      if (err.empty()) err = plan_sequences(q.f.seqs_p, J.nseq, p.steps, p.timestep, gamma, q.sq);
+      if (err.empty())
+        err = plan_lattice(q.f.lat_p, q.f.basis_p, J.nbasis, p.timestep, p.flags, q.g,
+                           batch_list_budget((int)q.sq.channels.size(), J.nbasis));
       if (err.empty()) {
         q.cell[0] = q.f.lat_p->a;
         q.cell[1] = q.f.lat_p->b;
         q.cell[2] = q.f.lat_p->c;
       }
     }
-    if (err.empty()) err = plan_sequences(q.f.seqs_p, J.nseq, p.steps, p.timestep, gamma, q.sq);
+    if (err.empty() && J.mode == AXX_MODE_SINGLE)
+      err = plan_sequences(q.f.seqs_p, J.nseq, p.steps, p.timestep, gamma, q.sq);
     if (!err.empty()) return bfail(ctx, AXX_ERR_INVALID_ARG, "job " + std::to_string(j) + ": " + err);
     if (J.mode == AXX_MODE_SINGLE)
       q.cls = q.g.geom == AXX_GEOM_SPH ? BC_SSPH : BC_SCYL;
