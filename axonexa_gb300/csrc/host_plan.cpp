@@ -485,9 +485,11 @@ std::string plan_lattice(const axx_lattice *lat, const axx_basis *basis, int nba
   // Finer 2-D grids leave fewer candidates per move (a grid cell about a
   // third of a basis across lists about 1.3 cylinders, against 3.3 at one
   // basis per cell), as long as the staged tables stay within the budget.
+  // Cells of few bases (a hexagonal cell of four) fit grids up to 16 times
+  // finer, which leave under one candidate per move.
   if (list_budget > 0 && flat && inst.size() > 1) {
     const size_t fixed = inst.size() * 32;
-    for (double f : {4.0, 3.5, 3.0, 2.5, 2.0, 1.5}) {
+    for (double f : {16.0, 12.0, 8.0, 6.0, 5.0, 4.0, 3.5, 3.0, 2.5, 2.0, 1.5}) {
       const int gx = cells_along(A, h / f, 256), gy = cells_along(B, h / f, 256);
       if (gx <= g.gx && gy <= g.gy) break;
       // a cheap lower bound first: the cell starts alone
