@@ -352,9 +352,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) mlp_tc_kernel(const __grid_cons
                  "r"(TC_TILES * TC_N));
 }
 
-// Packs W [256][in] (FP32 master, row-major) into BF16 K-chunks of 32
-// columns (16 KB each; the last may hold 16), each chunk in the canonical
-// layout with its own K, zero padded to in_pad columns.
+// Packs W [256][in] (FP32 master, row-major) into BF16 K-chunks of TC_KC
+// (64) columns (32 KB each; the last holds what is left, e.g. 16 columns of
+// a 16-column input layer), each chunk in the canonical layout with its own
+// K, zero padded to in_pad columns.
 __global__ void pack_tc_kernel(const float *__restrict__ W, __nv_bfloat16 *__restrict__ out,
                                int in, int in_pad) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
