@@ -5,7 +5,7 @@ or that contains the move's start, is in the candidate list of the cell the
 walk kernel files the start under, for random starts and starts within a
 few ulps of the grid lines; hexagonal cells and random packs, planned with
 the walk's table budgets (grids up to 16 times finer than one basis per
-cell) and without one (Lattice::boundaryCheck tests every basis,
+cell) and without one, and random sphere packs (Lattice::boundaryCheck tests every basis,
 src/substrate/lattice.cuh:158-247, so a list that misses a reachable image
 would change the walk)."""
 import os
@@ -50,7 +50,7 @@ def plans():
 
 
 def test_every_reachable_image_is_listed(plans):
-    assert len(plans) == 24
+    assert len(plans) == 26
     for key, p in plans.items():
         assert p["checked"] > 1000, key
         assert p["bad"] == 0, (key, p)
