@@ -3,13 +3,13 @@ counts, one persistent launch replayed from a CUDA graph (axx_batch_*)."""
 from __future__ import annotations
 
 import ctypes as C
-from dataclasses import dataclass, field
+from dataclasses import dataclass
 from typing import List, Optional, Sequence
 
 import numpy as np
 
 from . import _native as N
-from .acquisition import GAMMA, Device, Lattice, RunResult, _params, default_device, run_flags
+from .acquisition import Device, Lattice, RunResult, _params, default_device, run_flags
 
 
 @dataclass

@@ -28,7 +28,7 @@ from typing import Dict, List, Optional, Tuple
 import numpy as np
 
 from . import _native as N
-from .acquisition import CosGFunc, Device, Lattice, RectGrad, default_device
+from .acquisition import CosGFunc, Device, RectGrad, default_device
 from .batch import Job, run_batch
 from .substrate import gamma_quantile_radii, pack_radii
 

@@ -7,7 +7,6 @@ describes: point i = words 1..3 of stream (seed, i) scaled by the cell
 (Lattice::initializeUniformly), counted when Lattice::inRegion is > 0."""
 import math
 
-import numpy as np
 import pytest
 
 import cases

@@ -1,6 +1,5 @@
 """Batched acquisitions (one persistent launch, CUDA-graph replay, autotuned
 tile) against the same acquisitions run one by one."""
-import os
 
 import numpy as np
 import pytest

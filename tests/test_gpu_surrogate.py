@@ -1,6 +1,5 @@
 """The surrogate network's kernels against an FP64 CPU MLP, and what the
 trained network gains over plain Monte Carlo."""
-import math
 import time
 
 import numpy as np

@@ -8,7 +8,6 @@ makes the input winding irrelevant; a cube's walk across x equals the
 parallel-plate walk of the same width (the same streams move x alike); the
 GPU trace equals the FP32 mirror bit for bit.
 """
-import math
 
 import numpy as np
 import pytest

@@ -1,5 +1,4 @@
 """Philox4x32-10 known-answer vectors, the stream layout and the direction math."""
-import math
 
 import numpy as np
 

@@ -10,8 +10,6 @@ import math
 import numpy as np
 import pytest
 
-import cases
-
 
 def pgse_table(G, delta, Delta, dt, steps):
     t = np.arange(steps) * dt
